@@ -1,0 +1,421 @@
+"""GB300-native D3Q19 channel-flow time step (host-side Python mirror).
+
+This package is a thin ctypes layer over ``liblbm_gb300.so``, whose
+``extern "C"`` boundary is declared in ``include/lbm_gb300.h``.  It mirrors the
+reference's drop-in interface for the hot path:
+
+* :func:`para` restates the run constants of ``Channel-Flow/para.f90:59-141``
+  (laminar/turbulent channel, MRT rate sets) for a lattice of any size;
+* :class:`Lattice` owns the device state and exposes the reference's
+  subroutines as methods -- ``initpop`` (initial.f90:19-46), ``step``
+  (collision_MRT + collisionExchnge + macrovar, collision.f90:24-463),
+  ``prerelax`` (main.f90:69-90), ``macrovar``, ``diag`` and ``profiles``
+  (saveload.f90:1202-1676), ``save_flow``/``load_flow`` (saveload.f90:102-332);
+* :data:`CHANNEL_CONFIGS` holds the benchmark channel workloads.
+
+Arrays use the reference layout: populations ``f(0:18, nx, ny, nz)`` and
+fields ``(nx, ny, nz)``, Fortran order, float64; x is wall-normal, y
+streamwise, z spanwise.
+
+There is no CPU fallback: importing works without a GPU, but creating a
+:class:`Lattice` needs the built library and a CUDA device, and raises
+otherwise.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from dataclasses import dataclass, field
+from pathlib import Path
+
+import numpy as np
+
+PKG_DIR = Path(__file__).resolve().parent
+LIB_PATH = PKG_DIR / "liblbm_gb300.so"
+
+PREC_FP64, PREC_FP32, PREC_FP16 = 0, 1, 2
+PRECISIONS = {"fp64": PREC_FP64, "fp32": PREC_FP32, "fp16": PREC_FP16}
+MRT_STABLE, MRT_LBGK, MRT_LOWDISS = 1, 2, 3
+PROFILE_COLS = 12
+PROFILE_NAMES = ("ux", "uy", "uz", "uxuz", "uxuy", "uyuz", "uxux", "uyuy", "uzuz", "rho", "rhorho", "count")
+
+# Every symbol include/lbm_gb300.h declares.
+EXPORTS = (
+    "lbm_strerror", "lbm_last_error", "lbm_version", "lbm_params_init", "lbm_create", "lbm_destroy",
+    "lbm_device_bytes", "lbm_upload_f", "lbm_download_f", "lbm_initpop", "lbm_init_channel",
+    "lbm_channel_velocity", "lbm_step", "lbm_step_async", "lbm_synchronize", "lbm_stream",
+    "lbm_step_count", "lbm_prerelax", "lbm_macrovar", "lbm_diag", "lbm_profiles", "lbm_avedensity",
+    "lbm_save_flow", "lbm_load_flow",
+)
+
+
+class LBMError(RuntimeError):
+    """A negative status code returned by the C ABI."""
+
+    def __init__(self, code: int, where: str, detail: str):
+        super().__init__(f"{where}: {detail} (code {code})")
+        self.code = code
+
+
+class LBMParams(ctypes.Structure):
+    _fields_ = [
+        ("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("nz", ctypes.c_int32),
+        ("precision", ctypes.c_int32),
+        ("s1", ctypes.c_double), ("s2", ctypes.c_double), ("s4", ctypes.c_double),
+        ("s9", ctypes.c_double), ("s10", ctypes.c_double), ("s13", ctypes.c_double),
+        ("s16", ctypes.c_double),
+        ("omegepsl", ctypes.c_double), ("omegepslj", ctypes.c_double), ("omegxx", ctypes.c_double),
+        ("force", ctypes.c_double * 3),
+        ("fp16_scale", ctypes.c_double),
+        ("device", ctypes.c_int32), ("reserved", ctypes.c_int32),
+    ]
+
+
+class LBMStats(ctypes.Structure):
+    _fields_ = [
+        ("nfluid", ctypes.c_int64), ("rho_sum", ctypes.c_double),
+        ("mom_sum", ctypes.c_double * 3), ("usq_sum", ctypes.c_double * 3),
+        ("rho_max", ctypes.c_double), ("rho_min", ctypes.c_double), ("vmax", ctypes.c_double),
+        ("vmax_at", ctypes.c_int32 * 3), ("nonfinite", ctypes.c_int32),
+    ]
+
+
+_lib = None
+
+
+def library_path() -> Path:
+    return LIB_PATH
+
+
+def load_library(path: Path | str | None = None) -> ctypes.CDLL:
+    """Load liblbm_gb300.so (built by ``__graft_entry__.build()``); raise if absent."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path is not None else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: build it with __graft_entry__.build() (needs nvcc)")
+    lib = ctypes.CDLL(str(p))
+    dp = ctypes.POINTER(ctypes.c_double)
+    ctx = ctypes.c_void_p
+    sig = {
+        "lbm_strerror": (ctypes.c_char_p, [ctypes.c_int]),
+        "lbm_last_error": (ctypes.c_char_p, []),
+        "lbm_version": (ctypes.c_int, []),
+        "lbm_params_init": (ctypes.c_int, [ctypes.POINTER(LBMParams), ctypes.c_int32, ctypes.c_int32,
+                                           ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double,
+                                           ctypes.c_int32]),
+        "lbm_create": (ctypes.c_int, [ctypes.POINTER(LBMParams), ctypes.POINTER(ctx)]),
+        "lbm_destroy": (ctypes.c_int, [ctx]),
+        "lbm_device_bytes": (ctypes.c_int, [ctx, ctypes.POINTER(ctypes.c_size_t)]),
+        "lbm_upload_f": (ctypes.c_int, [ctx, dp]),
+        "lbm_download_f": (ctypes.c_int, [ctx, dp]),
+        "lbm_initpop": (ctypes.c_int, [ctx, dp, dp, dp]),
+        "lbm_init_channel": (ctypes.c_int, [ctx, ctypes.c_double, ctypes.c_double, ctypes.c_uint64]),
+        "lbm_channel_velocity": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                                ctypes.c_double, ctypes.c_uint64, dp, dp, dp]),
+        "lbm_step": (ctypes.c_int, [ctx, ctypes.c_int32]),
+        "lbm_step_async": (ctypes.c_int, [ctx, ctypes.c_int32]),
+        "lbm_synchronize": (ctypes.c_int, [ctx]),
+        "lbm_stream": (ctypes.c_int, [ctx, ctypes.POINTER(ctypes.c_void_p)]),
+        "lbm_step_count": (ctypes.c_int, [ctx, ctypes.POINTER(ctypes.c_int64)]),
+        "lbm_prerelax": (ctypes.c_int, [ctx, dp, dp, dp, ctypes.c_double, ctypes.c_int32,
+                                        ctypes.POINTER(ctypes.c_int32), dp]),
+        "lbm_macrovar": (ctypes.c_int, [ctx, dp, dp, dp, dp]),
+        "lbm_diag": (ctypes.c_int, [ctx, ctypes.POINTER(LBMStats)]),
+        "lbm_profiles": (ctypes.c_int, [ctx, dp]),
+        "lbm_avedensity": (ctypes.c_int, [ctx, dp]),
+        "lbm_save_flow": (ctypes.c_int, [ctx, ctypes.c_char_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]),
+        "lbm_load_flow": (ctypes.c_int, [ctx, ctypes.c_char_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _check(lib, rc: int, where: str) -> None:
+    if rc != 0:
+        detail = lib.lbm_last_error().decode() or lib.lbm_strerror(rc).decode()
+        raise LBMError(rc, where, detail)
+
+
+def _dptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+# --------------------------------------------------------------------------
+# run constants (para.f90)
+# --------------------------------------------------------------------------
+@dataclass
+class RunParams:
+    """The scalars para.f90 sets for the channel (para.f90:59-141)."""
+
+    nx: int              # wall-normal nodes (walls at x = 1/2 and nx + 1/2)
+    ny: int              # streamwise nodes (periodic)
+    nz: int              # spanwise nodes (periodic)
+    visc: float
+    force_y: float       # streamwise body force (force_in_y * force_mag)
+    mrt_type: int = MRT_STABLE
+    ustar: float = 0.0
+    precision: int = PREC_FP64
+    fp16_scale: float = 32768.0
+    device: int = 0
+    extra: dict = field(default_factory=dict)
+
+    def to_c(self) -> LBMParams:
+        p = LBMParams()
+        lib = load_library()
+        _check(lib, lib.lbm_params_init(ctypes.byref(p), self.nx, self.ny, self.nz, self.mrt_type,
+                                        self.visc, self.force_y, self.precision), "lbm_params_init")
+        p.fp16_scale = self.fp16_scale
+        p.device = self.device
+        return p
+
+    def rates(self) -> dict:
+        """MRT rates and equilibrium coefficients (para.f90:106-141), computed in Python."""
+        tau = 3.0 * self.visc + 0.5
+        s9 = 1.0 / tau
+        if self.mrt_type == MRT_STABLE:
+            r = dict(s1=1.5, s2=1.4, s4=1.2, s10=1.4, s16=1.98, omegepsl=0.0, omegepslj=-475.0 / 63.0, omegxx=0.0)
+        elif self.mrt_type == MRT_LBGK:
+            r = dict(s1=s9, s2=s9, s4=s9, s10=s9, s16=s9, omegepsl=3.0, omegepslj=-11.0 / 2.0, omegxx=-0.5)
+        elif self.mrt_type == MRT_LOWDISS:
+            r = dict(s1=1.8, s2=1.8, s4=s9, s10=1.8, s16=1.8, omegepsl=3.0, omegepslj=-11.0 / 2.0, omegxx=-0.5)
+        else:
+            raise ValueError("mrt_type must be 1, 2 or 3")
+        r.update(s9=s9, s13=s9)
+        return r
+
+
+def para(nx: int, ny: int, nz: int, laminar: bool = True, **kw) -> RunParams:
+    """Constants of para.f90:59-88 for an nx (wall-normal) x ny x nz lattice.
+
+    laminar=True  -> Rstar=20, ustar=0.05 (centreline), visc = 2 ustar nx / Rstar,
+                     force = 8 visc ustar / nx^2, MRTtype 2 (LBGK)
+    laminar=False -> visc=0.0036, Rstar=180, ustar = 2 Rstar visc / nx,
+                     force = 2 rho0 ustar^2 / nx, MRTtype 1
+    """
+    if laminar:
+        rstar, ustar = 20.0, 0.05
+        visc = 2.0 * ustar * nx / rstar
+        force = 8.0 * visc * ustar / nx**2
+        mrt = MRT_LBGK
+    else:
+        visc, rstar = 0.0036, 180.0
+        ustar = 2.0 * rstar * visc / nx
+        force = 2.0 * 1.0 * ustar * ustar / nx
+        mrt = MRT_STABLE
+    kw.setdefault("mrt_type", mrt)
+    return RunParams(nx=nx, ny=ny, nz=nz, visc=visc, force_y=force, ustar=ustar, **kw)
+
+
+@dataclass(frozen=True)
+class ChannelConfig:
+    """A channel workload in the benchmark's axes (x streamwise, y spanwise,
+    z wall-normal) with its reference-axis lattice (nx wall-normal, ny
+    streamwise, nz spanwise)."""
+
+    name: str
+    stream: int
+    span: int
+    wall: int
+    visc: float
+    ustar: float
+    h: float
+    steps: int
+    precision: str = "fp64"
+    uc: float = 0.05
+    amp: float = 0.05
+    seed: int = 20240611
+    spheres: int = 0
+    radius: float = 0.0
+
+    @property
+    def force(self) -> float:
+        return self.ustar**2 / self.h          # gx = u*^2 / h
+
+    @property
+    def nodes(self) -> int:
+        return self.stream * self.span * self.wall
+
+    def params(self, precision: str | None = None, **kw) -> RunParams:
+        prec = PRECISIONS[precision or self.precision]
+        return RunParams(nx=self.wall, ny=self.stream, nz=self.span, visc=self.visc, force_y=self.force,
+                         mrt_type=MRT_STABLE, ustar=self.ustar, precision=prec, **kw)
+
+
+CHANNEL_CONFIGS = {
+    # plain turbulent channel, Re_tau ~ 93
+    "c0": ChannelConfig("c0-channel-128x64x64", 128, 64, 64, visc=0.0012, ustar=0.0035, h=32, steps=2000),
+    # particle-laden channel, Re_tau ~ 181 (fluid part)
+    "c1": ChannelConfig("c1-particles-256x128x128", 256, 128, 128, visc=0.0012, ustar=0.0034, h=64,
+                        steps=5000, spheres=256, radius=4.0),
+    # precision sweep, Re_tau ~ 181
+    "c2": ChannelConfig("c2-precision-512x256x256", 512, 256, 256, visc=0.0024, ustar=0.0034, h=128,
+                        steps=20000, spheres=2048, radius=8.0),
+    # large channel, FP32 compute / FP16 storage, Re_tau ~ 363
+    "c4": ChannelConfig("c4-large-1024x512x512", 1024, 512, 512, visc=0.0024, ustar=0.0034, h=256,
+                        steps=2000, precision="fp16", spheres=16384, radius=8.0),
+}
+
+
+# --------------------------------------------------------------------------
+# device lattice
+# --------------------------------------------------------------------------
+class Lattice:
+    """Device-resident D3Q19 channel state (one GPU, one stream)."""
+
+    def __init__(self, params: RunParams | LBMParams):
+        self.lib = load_library()
+        self.cparams = params.to_c() if isinstance(params, RunParams) else params
+        self.nx, self.ny, self.nz = self.cparams.nx, self.cparams.ny, self.cparams.nz
+        self._ctx = ctypes.c_void_p()
+        _check(self.lib, self.lib.lbm_create(ctypes.byref(self.cparams), ctypes.byref(self._ctx)), "lbm_create")
+
+    # lifetime ---------------------------------------------------------------
+    def close(self) -> None:
+        if self._ctx:
+            self.lib.lbm_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # helpers ----------------------------------------------------------------
+    @property
+    def shape(self) -> tuple[int, int, int]:
+        return (self.nx, self.ny, self.nz)
+
+    @property
+    def nodes(self) -> int:
+        return self.nx * self.ny * self.nz
+
+    def _field(self, a: np.ndarray, name: str) -> np.ndarray:
+        a = np.asarray(a, dtype=np.float64)
+        if a.size != self.nodes:
+            raise ValueError(f"{name} must have {self.nodes} values (nx*ny*nz)")
+        return np.asfortranarray(a.reshape(self.shape, order="F"))
+
+    def _call(self, name: str, *args) -> None:
+        _check(self.lib, getattr(self.lib, name)(self._ctx, *args), name)
+
+    # reference interface ------------------------------------------------------
+    def upload_f(self, f: np.ndarray) -> None:
+        f = np.asarray(f, dtype=np.float64)
+        if f.size != 19 * self.nodes:
+            raise ValueError("f must have 19*nx*ny*nz values")
+        f = np.asfortranarray(f.reshape((19,) + self.shape, order="F"))
+        self._call("lbm_upload_f", _dptr(f))
+
+    def download_f(self, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty((19,) + self.shape, dtype=np.float64, order="F")
+        self._call("lbm_download_f", _dptr(out))
+        return out
+
+    def initpop(self, ux, uy, uz) -> None:
+        a, b, c = (self._field(v, n) for v, n in ((ux, "ux"), (uy, "uy"), (uz, "uz")))
+        self._call("lbm_initpop", _dptr(a), _dptr(b), _dptr(c))
+
+    def init_channel(self, uc: float, amp: float, seed: int) -> None:
+        self._call("lbm_init_channel", ctypes.c_double(uc), ctypes.c_double(amp), ctypes.c_uint64(seed))
+
+    def step(self, n: int = 1) -> None:
+        self._call("lbm_step", n)
+
+    def step_async(self, n: int = 1) -> None:
+        self._call("lbm_step_async", n)
+
+    def synchronize(self) -> None:
+        self._call("lbm_synchronize")
+
+    def stream(self) -> int:
+        s = ctypes.c_void_p()
+        self._call("lbm_stream", ctypes.byref(s))
+        return s.value or 0
+
+    def step_count(self) -> int:
+        n = ctypes.c_int64()
+        self._call("lbm_step_count", ctypes.byref(n))
+        return n.value
+
+    def device_bytes(self) -> int:
+        n = ctypes.c_size_t()
+        self._call("lbm_device_bytes", ctypes.byref(n))
+        return n.value
+
+    def prerelax(self, ux, uy, uz, eps: float = 1e-5, maxit: int = 15000) -> tuple[int, float]:
+        a, b, c = (self._field(v, n) for v, n in ((ux, "ux"), (uy, "uy"), (uz, "uz")))
+        it = ctypes.c_int32()
+        err = ctypes.c_double()
+        self._call("lbm_prerelax", _dptr(a), _dptr(b), _dptr(c), eps, maxit, ctypes.byref(it), ctypes.byref(err))
+        return it.value, err.value
+
+    def macrovar(self) -> tuple[np.ndarray, np.ndarray, np.ndarray, np.ndarray]:
+        outs = [np.empty(self.shape, dtype=np.float64, order="F") for _ in range(4)]
+        self._call("lbm_macrovar", *map(_dptr, outs))
+        return tuple(outs)
+
+    def diag(self) -> LBMStats:
+        st = LBMStats()
+        self._call("lbm_diag", ctypes.byref(st))
+        return st
+
+    def profiles(self) -> np.ndarray:
+        """Plane sums (nx, 12) in the column order of PROFILE_NAMES."""
+        out = np.empty((self.nx, PROFILE_COLS), dtype=np.float64)
+        self._call("lbm_profiles", _dptr(out))
+        return out
+
+    def avedensity(self) -> float:
+        m = ctypes.c_double()
+        self._call("lbm_avedensity", ctypes.byref(m))
+        return m.value
+
+    def save_flow(self, path: str | Path, kind: int, ints) -> None:
+        arr = (ctypes.c_int32 * 3)(*list(ints) + [0] * (3 - len(ints)))
+        self._call("lbm_save_flow", str(path).encode(), kind, arr)
+
+    def load_flow(self, path: str | Path, kind: int) -> list[int]:
+        arr = (ctypes.c_int32 * 3)()
+        self._call("lbm_load_flow", str(path).encode(), kind, arr)
+        return list(arr)[: (1 if kind == 0 else 3)]
+
+
+def channel_velocity(nx: int, ny: int, nz: int, uc: float, amp: float, seed: int):
+    """Host copy of the device channel initial velocity (reference layout)."""
+    lib = load_library()
+    out = [np.empty((nx, ny, nz), dtype=np.float64, order="F") for _ in range(3)]
+    _check(lib, lib.lbm_channel_velocity(nx, ny, nz, uc, amp, ctypes.c_uint64(seed), *map(_dptr, out)),
+           "lbm_channel_velocity")
+    return tuple(out)
+
+
+def statistics(prof: np.ndarray, ustar: float) -> dict:
+    """statistc2 normalisation (saveload.f90:1442-1462) of plane sums:
+    means by u*, variances and stresses by u*^2, pressure <rho>/u*^2."""
+    n = prof[:, 11]
+    mean = prof[:, 0:3] / n[:, None] / ustar
+    sq = prof[:, 6:9] / n[:, None] / ustar**2 - mean**2
+    st = prof[:, 3:6] / n[:, None] / ustar**2
+    stress = np.stack([st[:, 0] - mean[:, 0] * mean[:, 2],     # xz
+                       st[:, 1] - mean[:, 0] * mean[:, 1],     # xy (wall-normal x streamwise)
+                       st[:, 2] - mean[:, 1] * mean[:, 2]], 1)  # yz
+    pr = prof[:, 9] / n / ustar**2
+    prsq = prof[:, 10] / n / ustar**4 - pr * pr
+    return dict(mean=mean, sq=sq, stress=stress, pressure=pr, pressure_sq=prsq, volf_fluid=n / n.max())

@@ -1,0 +1,89 @@
+"""Build the in-tree CUDA library ``liblbm_gb300.so`` for sm_103a.
+
+The library holds every kernel of the time step and the ``extern "C"``
+boundary declared in ``include/lbm_gb300.h``.  Translation units are compiled
+in parallel with nvcc and linked into the package directory; nothing is
+installed into site-packages.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG_DIR = Path(__file__).resolve().parent
+REPO = PKG_DIR.parent
+CSRC = PKG_DIR / "csrc"
+OBJ_DIR = PKG_DIR / "_build"
+LIB_PATH = PKG_DIR / "liblbm_gb300.so"
+HOST_DIR = PKG_DIR / "host"
+DRIVER_PATH = PKG_DIR / "channel_gb300"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = [
+    "-O3", "-std=c++17", "-lineinfo", *ARCH,
+    "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
+    "--expt-relaxed-constexpr",
+]
+SOURCES = ["lbm_step.cu", "lbm_fields.cu", "lbm_capi.cu"]
+
+
+def nvcc() -> str:
+    exe = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not Path(exe).exists():
+        raise RuntimeError("nvcc not found: the CUDA toolkit is required to build liblbm_gb300.so")
+    return exe
+
+
+def _deps() -> list[Path]:
+    return sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + [REPO / "include" / "lbm_gb300.h"]
+
+
+def _stale(target: Path, inputs: list[Path]) -> bool:
+    if not target.exists():
+        return True
+    t = target.stat().st_mtime
+    return any(p.stat().st_mtime > t for p in inputs)
+
+
+def _run(cmd: list[str]) -> None:
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    if proc.returncode != 0:
+        raise RuntimeError(f"command failed ({proc.returncode}): {' '.join(cmd)}\n{proc.stdout}\n{proc.stderr}")
+
+
+def build_library(force: bool = False, verbose: bool = False) -> Path:
+    """Compile and link liblbm_gb300.so if any source changed; return its path."""
+    OBJ_DIR.mkdir(exist_ok=True)
+    exe = nvcc()
+    deps = _deps()
+    jobs = []
+    objs = []
+    for src in SOURCES:
+        s = CSRC / src
+        o = OBJ_DIR / (src + ".o")
+        objs.append(o)
+        if force or _stale(o, [s, *deps]):
+            extra = ["-Xptxas", "-v"] if verbose and src.endswith(".cu") else []
+            jobs.append([exe, *NVCC_FLAGS, *extra, "-I", str(REPO / "include"), "-c", str(s), "-o", str(o)])
+    if jobs:
+        with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 1)) as ex:
+            list(ex.map(_run, jobs))
+    if force or jobs or _stale(LIB_PATH, objs):
+        tmp = LIB_PATH.with_suffix(".so.tmp")
+        _run([exe, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"])
+        os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+def build_driver(force: bool = False) -> Path:
+    """Compile the C++ channel driver (mirror of the reference's main.f90)."""
+    lib = build_library()
+    src = HOST_DIR / "channel_main.cpp"
+    if force or _stale(DRIVER_PATH, [src, lib, REPO / "include" / "lbm_gb300.h"]):
+        cxx = shutil.which("g++") or "g++"
+        _run([cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-I", str(REPO / "include"), str(src),
+              "-o", str(DRIVER_PATH), "-L", str(PKG_DIR), "-llbm_gb300", f"-Wl,-rpath,{PKG_DIR}"])
+    return DRIVER_PATH

@@ -1,0 +1,656 @@
+// extern "C" boundary of liblbm_gb300.so: context management, host<->device
+// layout conversion, the step loop, pre-relaxation, diagnostics and
+// checkpoint files.  See include/lbm_gb300.h for the contract.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "lbm_internal.h"
+
+using namespace lbm;
+
+struct lbm_ctx {
+    lbm_params p{};
+    DeviceState s{};
+    cudaStream_t stream = nullptr;
+    int parity = 0;            // 0: natural orientation, 1: after an even AA step
+    int64_t nsteps = 0;
+    double* d_stage = nullptr; // FP64 staging for layout conversion
+    size_t stage_elems = 0;
+    double* d_red = nullptr;   // reduction partials
+    size_t red_elems = 0;
+    double* d_uf = nullptr;    // frozen velocity for pre-relaxation (GPU layout)
+    double* d_rho = nullptr;   // pre-relaxation density
+    unsigned long long* d_max = nullptr;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    return fail(LBM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                                   \
+    do {                                                           \
+        cudaError_t e_ = (call);                                   \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);        \
+    } while (0)
+
+// Reference-layout element counts
+size_t nodes(const lbm_params& p) { return (size_t)p.nx * p.ny * p.nz; }
+size_t plane_nodes(const lbm_params& p) { return (size_t)p.nx * p.ny; }   // one ref z plane
+
+template <typename R>
+CollideConsts<R> make_consts(const lbm_params& p, double S) {
+    CollideConsts<R> c;
+    c.S = (R)S; c.invS = (R)(1.0 / S);
+    c.Fx = (R)p.force[0]; c.Fy = (R)p.force[1]; c.Fz = (R)p.force[2];
+    c.hFx = (R)(0.5 * S * p.force[0]); c.hFy = (R)(0.5 * S * p.force[1]); c.hFz = (R)(0.5 * S * p.force[2]);
+    c.ajx = (R)(S * p.force[0] / 10.0); c.ajy = (R)(S * p.force[1] / 10.0); c.ajz = (R)(S * p.force[2] / 10.0);
+    c.fqx = (R)(-(2.0 / 3.0) * S * p.force[0] / 40.0);
+    c.fqy = (R)(-(2.0 / 3.0) * S * p.force[1] / 40.0);
+    c.fqz = (R)(-(2.0 / 3.0) * S * p.force[2] / 40.0);
+    c.thFx = (R)(S * p.force[0] / 3.0); c.thFy = (R)(S * p.force[1] / 3.0); c.thFz = (R)(S * p.force[2] / 3.0);
+    c.ke = (R)(p.s1 / 2394.0);
+    c.keps = (R)(p.s2 / 252.0);
+    c.kq = (R)(p.s4 / 40.0);
+    c.kp = (R)(p.s9 / 36.0);
+    c.kpi = (R)(p.s10 / 72.0);
+    c.kxy = (R)(p.s13 / 4.0);
+    c.km = (R)(p.s16 / 8.0);
+    c.oeps = (R)p.omegepsl; c.oepsj = (R)p.omegepslj; c.oxx = (R)p.omegxx;
+    return c;
+}
+
+size_t elem_size(int prec) {
+    return prec == LBM_PREC_FP64 ? 8 : (prec == LBM_PREC_FP32 ? 4 : 2);
+}
+
+int check_ctx(const lbm_ctx* c) {
+    if (!c) return fail(LBM_ERR_INVALID_ARG, "null context");
+    return LBM_OK;
+}
+
+int set_device(const lbm_ctx* c) {
+    CK(cudaSetDevice(c->p.device));
+    return LBM_OK;
+}
+
+// planes of the reference z axis that fit in the staging buffer for k arrays
+int chunk_planes(const lbm_ctx* c, size_t per_node_doubles) {
+    const size_t per_plane = plane_nodes(c->p) * per_node_doubles;
+    size_t k = c->stage_elems / per_plane;
+    if (k < 1) k = 1;
+    if (k > (size_t)c->p.nz) k = c->p.nz;
+    return (int)k;
+}
+
+int ensure_stage(lbm_ctx* c, size_t elems) {
+    if (c->stage_elems >= elems) return LBM_OK;
+    if (c->d_stage) cudaFree(c->d_stage);
+    c->d_stage = nullptr;
+    c->stage_elems = 0;
+    CK(cudaMalloc(&c->d_stage, elems * sizeof(double)));
+    c->stage_elems = elems;
+    return LBM_OK;
+}
+
+int ensure_red(lbm_ctx* c, size_t elems) {
+    if (c->red_elems >= elems) return LBM_OK;
+    if (c->d_red) cudaFree(c->d_red);
+    c->d_red = nullptr;
+    c->red_elems = 0;
+    CK(cudaMalloc(&c->d_red, elems * sizeof(double)));
+    c->red_elems = elems;
+    return LBM_OK;
+}
+
+int sync(lbm_ctx* c) {
+    CK(cudaStreamSynchronize(c->stream));
+    return LBM_OK;
+}
+
+// ---- Fortran unformatted sequential records (gfortran convention) -------
+constexpr int64_t kMaxSub = 2147483639;  // bytes of data per sub-record
+
+bool write_marker(FILE* fp, int32_t v) { return fwrite(&v, 4, 1, fp) == 1; }
+
+struct RecordWriter {
+    // Writes one logical record of `total` bytes in sub-records; data arrives
+    // in pieces through put().
+    FILE* fp;
+    int64_t total, done = 0, sub_left = 0, sub_len = 0;
+    bool first = true, ok = true;
+    RecordWriter(FILE* f, int64_t t) : fp(f), total(t) {
+        if (total == 0) { ok = write_marker(fp, 0) && write_marker(fp, 0); }
+    }
+    void open_sub() {
+        sub_len = std::min<int64_t>(kMaxSub, total - done);
+        const bool more = done + sub_len < total;
+        ok = ok && write_marker(fp, (int32_t)(more ? -sub_len : sub_len));
+        sub_left = sub_len;
+    }
+    void close_sub() {
+        ok = ok && write_marker(fp, (int32_t)(first ? sub_len : -sub_len));
+        first = false;
+    }
+    void put(const void* data, int64_t n) {
+        const char* b = static_cast<const char*>(data);
+        while (n > 0 && ok) {
+            if (sub_left == 0) open_sub();
+            const int64_t k = std::min(n, sub_left);
+            ok = ok && fwrite(b, 1, (size_t)k, fp) == (size_t)k;
+            b += k; n -= k; sub_left -= k; done += k;
+            if (sub_left == 0) close_sub();
+        }
+    }
+};
+
+struct RecordReader {
+    FILE* fp;
+    int64_t sub_left = 0, total = 0;
+    bool more = true, ok = true, first = true;
+    explicit RecordReader(FILE* f) : fp(f) { next_sub(); }
+    void next_sub() {
+        int32_t m;
+        if (fread(&m, 4, 1, fp) != 1) { ok = false; return; }
+        more = m < 0;
+        sub_left = m < 0 ? -(int64_t)m : m;
+        total += sub_left;
+    }
+    void end_sub() {
+        int32_t m;
+        if (fread(&m, 4, 1, fp) != 1) { ok = false; return; }
+        const int64_t len = m < 0 ? -(int64_t)m : m;
+        (void)len;
+        first = false;
+    }
+    // read exactly n bytes of user data, crossing sub-records
+    bool get(void* data, int64_t n) {
+        char* b = static_cast<char*>(data);
+        while (n > 0 && ok) {
+            if (sub_left == 0) {
+                if (!more) { ok = false; break; }
+                end_sub();
+                next_sub();
+                continue;
+            }
+            const int64_t k = std::min(n, sub_left);
+            if (fread(b, 1, (size_t)k, fp) != (size_t)k) { ok = false; break; }
+            b += k; n -= k; sub_left -= k;
+        }
+        return ok;
+    }
+    // skip the rest of the record and its trailing marker; true if the record
+    // held exactly the data consumed
+    bool finish() {
+        if (!ok) return false;
+        const bool exact = sub_left == 0 && !more;
+        while (ok && (sub_left > 0 || more)) {
+            if (sub_left > 0) {
+                if (fseek(fp, (long)sub_left, SEEK_CUR) != 0) ok = false;
+                sub_left = 0;
+            } else { end_sub(); next_sub(); }
+        }
+        if (ok) end_sub();
+        return ok && exact;
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+const char* lbm_strerror(int code) {
+    switch (code) {
+        case LBM_OK: return "success";
+        case LBM_ERR_INVALID_ARG: return "invalid argument";
+        case LBM_ERR_CUDA: return "CUDA runtime error";
+        case LBM_ERR_OOM: return "out of memory";
+        case LBM_ERR_STATE: return "invalid state for this call";
+        case LBM_ERR_NOT_CONVERGED: return "pre-relaxation did not converge";
+        case LBM_ERR_IO: return "checkpoint file error";
+        case LBM_ERR_NONFINITE: return "non-finite populations";
+        case LBM_ERR_UNSUPPORTED: return "unsupported";
+    }
+    return "unknown error";
+}
+
+const char* lbm_last_error(void) { return g_last_error.c_str(); }
+
+int lbm_version(void) { return 100; }
+
+int lbm_params_init(lbm_params* p, int32_t nx, int32_t ny, int32_t nz, int32_t mrt_type,
+                    double visc, double force_y, int32_t precision) {
+    if (!p) return fail(LBM_ERR_INVALID_ARG, "null params");
+    if (nx < 1 || ny < 1 || nz < 1) return fail(LBM_ERR_INVALID_ARG, "lattice size must be positive");
+    if (!(visc > 0.0)) return fail(LBM_ERR_INVALID_ARG, "viscosity must be positive");
+    std::memset(p, 0, sizeof(*p));
+    p->nx = nx; p->ny = ny; p->nz = nz;
+    p->precision = precision;
+    // para.f90:106-141
+    const double tau = 3.0 * visc + 0.5;
+    p->s9 = 1.0 / tau;
+    p->s13 = p->s9;
+    switch (mrt_type) {
+        case LBM_MRT_STABLE:
+            p->s1 = 1.5; p->s2 = 1.4; p->s4 = 1.2; p->s10 = 1.4; p->s16 = 1.98;
+            p->omegepsl = 0.0; p->omegepslj = -475.0 / 63.0; p->omegxx = 0.0;
+            break;
+        case LBM_MRT_LBGK:
+            p->s1 = p->s9; p->s2 = p->s9; p->s4 = p->s9; p->s10 = p->s9; p->s16 = p->s9;
+            p->omegepsl = 3.0; p->omegepslj = -11.0 / 2.0; p->omegxx = -1.0 / 2.0;
+            break;
+        case LBM_MRT_LOWDISS:
+            p->s1 = 1.8; p->s2 = p->s1; p->s4 = p->s9; p->s10 = p->s1; p->s16 = p->s1;
+            p->omegepsl = 3.0; p->omegepslj = -11.0 / 2.0; p->omegxx = -1.0 / 2.0;
+            break;
+        default:
+            return fail(LBM_ERR_INVALID_ARG, "MRT type must be 1, 2 or 3");
+    }
+    p->force[0] = 0.0; p->force[1] = force_y; p->force[2] = 0.0;   // FORCING, collision.f90:522-524
+    p->fp16_scale = 32768.0;
+    p->device = 0;
+    if (precision < LBM_PREC_FP64 || precision > LBM_PREC_FP16)
+        return fail(LBM_ERR_INVALID_ARG, "precision must be LBM_PREC_FP64/FP32/FP16");
+    return LBM_OK;
+}
+
+int lbm_create(const lbm_params* p, lbm_ctx** out) {
+    if (!p || !out) return fail(LBM_ERR_INVALID_ARG, "null argument");
+    *out = nullptr;
+    if (p->nx < 1 || p->ny < 1 || p->nz < 1) return fail(LBM_ERR_INVALID_ARG, "lattice size must be positive");
+    if (p->nz > 65535 || p->nx > 65535) return fail(LBM_ERR_INVALID_ARG, "nx and nz are limited to 65535");
+    if (nodes(*p) >= (size_t)1 << 32) return fail(LBM_ERR_INVALID_ARG, "more than 2^32-1 nodes");
+    if (p->precision < LBM_PREC_FP64 || p->precision > LBM_PREC_FP16)
+        return fail(LBM_ERR_INVALID_ARG, "bad precision");
+    const double S = p->precision == LBM_PREC_FP16 ? (p->fp16_scale > 0 ? p->fp16_scale : 32768.0) : 1.0;
+    if (!std::isfinite(S)) return fail(LBM_ERR_INVALID_ARG, "bad fp16 scale");
+    for (double v : {p->s1, p->s2, p->s4, p->s9, p->s10, p->s13, p->s16, p->omegepsl, p->omegepslj,
+                     p->omegxx, p->force[0], p->force[1], p->force[2]})
+        if (!std::isfinite(v)) return fail(LBM_ERR_INVALID_ARG, "non-finite parameter");
+
+    lbm_ctx* c = new (std::nothrow) lbm_ctx();
+    if (!c) return fail(LBM_ERR_OOM, "host allocation failed");
+    c->p = *p;
+    if (c->p.precision == LBM_PREC_FP16) c->p.fp16_scale = S;
+    cudaError_t e = cudaSetDevice(p->device);
+    if (e != cudaSuccess) { delete c; return cuda_fail(e, "cudaSetDevice"); }
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete c; return cuda_fail(e, "cudaStreamCreate"); }
+
+    DeviceState& s = c->s;
+    s.prec = p->precision;
+    s.g.NX = p->ny; s.g.NY = p->nz; s.g.NZ = p->nx;
+    s.g.NXY = (uint32_t)p->ny * (uint32_t)p->nz;
+    s.N = nodes(*p);
+    // planes start on 256-byte boundaries
+    const size_t es = elem_size(s.prec);
+    const size_t align = 256 / es;
+    s.pstride = (s.N + align - 1) / align * align;
+    e = cudaMalloc(&s.f, (size_t)Q * s.pstride * es);
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(c->stream);
+        delete c;
+        return fail(e == cudaErrorMemoryAllocation ? LBM_ERR_OOM : LBM_ERR_CUDA,
+                    std::string("population allocation: ") + cudaGetErrorString(e));
+    }
+    s.cd = make_consts<double>(c->p, S);
+    s.cf = make_consts<float>(c->p, S);
+    // staging: up to 256 MB, at least one reference z plane of AoS populations
+    const size_t want = std::max<size_t>(plane_nodes(*p) * Q, (size_t)32 << 20);
+    const size_t stage = std::min<size_t>(want, std::max<size_t>(plane_nodes(*p) * Q, s.N * Q));
+    int rc = ensure_stage(c, stage);
+    if (rc != LBM_OK) { lbm_destroy(c); return rc; }
+    cudaMemsetAsync(s.f, 0, (size_t)Q * s.pstride * es, c->stream);
+    rc = sync(c);
+    if (rc != LBM_OK) { lbm_destroy(c); return rc; }
+    *out = c;
+    return LBM_OK;
+}
+
+int lbm_destroy(lbm_ctx* c) {
+    if (!c) return LBM_OK;
+    cudaSetDevice(c->p.device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    cudaFree(c->s.f);
+    cudaFree(c->d_stage);
+    cudaFree(c->d_red);
+    cudaFree(c->d_uf);
+    cudaFree(c->d_rho);
+    cudaFree(c->d_max);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return LBM_OK;
+}
+
+int lbm_device_bytes(const lbm_ctx* c, size_t* bytes) {
+    if (check_ctx(c) || !bytes) return fail(LBM_ERR_INVALID_ARG, "null argument");
+    *bytes = (size_t)Q * c->s.pstride * elem_size(c->s.prec) + c->stage_elems * 8 + c->red_elems * 8 +
+             (c->d_uf ? 3 * c->s.N * 8 : 0) + (c->d_rho ? c->s.N * 8 : 0);
+    return LBM_OK;
+}
+
+int lbm_upload_f(lbm_ctx* c, const double* f) {
+    if (check_ctx(c) || !f) return fail(LBM_ERR_INVALID_ARG, "null argument");
+    if (int rc = set_device(c)) return rc;
+    const int k = chunk_planes(c, Q);
+    const size_t per_plane = plane_nodes(c->p) * Q;
+    for (int z0 = 0; z0 < c->p.nz; z0 += k) {
+        const int nzc = std::min(k, c->p.nz - z0);
+        CK(cudaMemcpyAsync(c->d_stage, f + (size_t)z0 * per_plane, (size_t)nzc * per_plane * 8,
+                           cudaMemcpyHostToDevice, c->stream));
+        CK(launch_aos_to_store(c->s, c->d_stage, z0, nzc, c->stream));
+    }
+    c->parity = 0;
+    c->nsteps = 0;
+    return sync(c);
+}
+
+int lbm_download_f(lbm_ctx* c, double* f) {
+    if (check_ctx(c) || !f) return fail(LBM_ERR_INVALID_ARG, "null argument");
+    if (int rc = set_device(c)) return rc;
+    const int k = chunk_planes(c, Q);
+    const size_t per_plane = plane_nodes(c->p) * Q;
+    for (int z0 = 0; z0 < c->p.nz; z0 += k) {
+        const int nzc = std::min(k, c->p.nz - z0);
+        CK(launch_store_to_aos(c->s, c->parity, c->d_stage, z0, nzc, c->stream));
+        CK(cudaMemcpyAsync(f + (size_t)z0 * per_plane, c->d_stage, (size_t)nzc * per_plane * 8,
+                           cudaMemcpyDeviceToHost, c->stream));
+    }
+    return sync(c);
+}
+
+int lbm_initpop(lbm_ctx* c, const double* ux, const double* uy, const double* uz) {
+    if (check_ctx(c) || !ux || !uy || !uz) return fail(LBM_ERR_INVALID_ARG, "null argument");
+    if (int rc = set_device(c)) return rc;
+    const int k = chunk_planes(c, 3);
+    const size_t pp = plane_nodes(c->p);
+    for (int z0 = 0; z0 < c->p.nz; z0 += k) {
+        const int nzc = std::min(k, c->p.nz - z0);
+        const size_t n = (size_t)nzc * pp;
+        double* du = c->d_stage;
+        double* dv = du + n;
+        double* dw = dv + n;
+        CK(cudaMemcpyAsync(du, ux + (size_t)z0 * pp, n * 8, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(dv, uy + (size_t)z0 * pp, n * 8, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(dw, uz + (size_t)z0 * pp, n * 8, cudaMemcpyHostToDevice, c->stream));
+        CK(launch_initpop(c->s, du, dv, dw, z0, nzc, c->stream));
+    }
+    c->parity = 0;
+    c->nsteps = 0;
+    return sync(c);
+}
+
+int lbm_init_channel(lbm_ctx* c, double uc, double amp, uint64_t seed) {
+    if (check_ctx(c)) return LBM_ERR_INVALID_ARG;
+    if (!std::isfinite(uc) || !std::isfinite(amp)) return fail(LBM_ERR_INVALID_ARG, "non-finite argument");
+    if (int rc = set_device(c)) return rc;
+    CK(launch_init_channel(c->s, uc, amp, seed, c->stream));
+    c->parity = 0;
+    c->nsteps = 0;
+    return sync(c);
+}
+
+int lbm_channel_velocity(int32_t nx, int32_t ny, int32_t nz, double uc, double amp, uint64_t seed,
+                         double* ux, double* uy, double* uz) {
+    if (nx < 1 || ny < 1 || nz < 1 || !ux || !uy || !uz) return fail(LBM_ERR_INVALID_ARG, "bad argument");
+    channel_velocity_host(nx, ny, nz, uc, amp, seed, ux, uy, uz);
+    return LBM_OK;
+}
+
+int lbm_step_async(lbm_ctx* c, int32_t nsteps) {
+    if (check_ctx(c)) return LBM_ERR_INVALID_ARG;
+    if (nsteps < 0) return fail(LBM_ERR_INVALID_ARG, "negative step count");
+    for (int32_t k = 0; k < nsteps; ++k) {
+        CK(launch_step(c->s, c->parity, c->stream));
+        c->parity ^= 1;
+        ++c->nsteps;
+    }
+    return LBM_OK;
+}
+
+int lbm_step(lbm_ctx* c, int32_t nsteps) {
+    if (check_ctx(c)) return LBM_ERR_INVALID_ARG;
+    if (int rc = set_device(c)) return rc;
+    if (int rc = lbm_step_async(c, nsteps)) return rc;
+    return sync(c);
+}
+
+int lbm_synchronize(lbm_ctx* c) {
+    if (check_ctx(c)) return LBM_ERR_INVALID_ARG;
+    return sync(c);
+}
+
+int lbm_stream(lbm_ctx* c, void** stream) {
+    if (check_ctx(c) || !stream) return fail(LBM_ERR_INVALID_ARG, "null argument");
+    *stream = (void*)c->stream;
+    return LBM_OK;
+}
+
+int lbm_step_count(const lbm_ctx* c, int64_t* n) {
+    if (check_ctx(c) || !n) return fail(LBM_ERR_INVALID_ARG, "null argument");
+    *n = c->nsteps;
+    return LBM_OK;
+}
+
+int lbm_prerelax(lbm_ctx* c, const double* ux, const double* uy, const double* uz, double eps,
+                 int32_t maxit, int32_t* iters, double* err) {
+    if (check_ctx(c) || !ux || !uy || !uz) return fail(LBM_ERR_INVALID_ARG, "null argument");
+    if (!(eps >= 0.0) || maxit < 0) return fail(LBM_ERR_INVALID_ARG, "bad eps or maxit");
+    if (int rc = set_device(c)) return rc;
+    const size_t N = c->s.N;
+    if (!c->d_uf) CK(cudaMalloc(&c->d_uf, 3 * N * sizeof(double)));
+    if (!c->d_rho) CK(cudaMalloc(&c->d_rho, N * sizeof(double)));
+    if (!c->d_max) CK(cudaMalloc(&c->d_max, sizeof(unsigned long long)));
+    const int k = chunk_planes(c, 3);
+    const size_t pp = plane_nodes(c->p);
+    for (int z0 = 0; z0 < c->p.nz; z0 += k) {
+        const int nzc = std::min(k, c->p.nz - z0);
+        const size_t n = (size_t)nzc * pp;
+        double* du = c->d_stage;
+        CK(cudaMemcpyAsync(du, ux + (size_t)z0 * pp, n * 8, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(du + n, uy + (size_t)z0 * pp, n * 8, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(du + 2 * n, uz + (size_t)z0 * pp, n * 8, cudaMemcpyHostToDevice, c->stream));
+        CK(launch_ref_to_gpu_vec(c->s, du, du + n, du + 2 * n, c->d_uf, z0, nzc, c->stream));
+    }
+    // initpop leaves rho = 0 (initial.f90:32); main.f90:71 copies it to rhop
+    CK(cudaMemsetAsync(c->d_rho, 0, N * sizeof(double), c->stream));
+    int32_t istep = 0;
+    double rhoerr = 0.0;
+    for (;;) {
+        CK(cudaMemsetAsync(c->d_max, 0, sizeof(unsigned long long), c->stream));
+        CK(launch_prerelax(c->s, c->parity, c->d_uf, c->d_rho, c->d_max, c->stream));
+        c->parity ^= 1;
+        unsigned long long bits = 0;
+        CK(cudaMemcpyAsync(&bits, c->d_max, sizeof(bits), cudaMemcpyDeviceToHost, c->stream));
+        if (int rc = sync(c)) return rc;
+        std::memcpy(&rhoerr, &bits, sizeof(double));
+        if (!(rhoerr == rhoerr)) return fail(LBM_ERR_NONFINITE, "NaN density during pre-relaxation");
+        if (rhoerr <= eps || istep > maxit) break;   // main.f90:85
+        ++istep;
+    }
+    if (iters) *iters = istep;
+    if (err) *err = rhoerr;
+    c->nsteps = 0;
+    if (rhoerr > eps) return fail(LBM_ERR_NOT_CONVERGED, "pre-relaxation exceeded maxit");
+    return LBM_OK;
+}
+
+int lbm_macrovar(lbm_ctx* c, double* rho, double* ux, double* uy, double* uz) {
+    if (check_ctx(c)) return LBM_ERR_INVALID_ARG;
+    if (int rc = set_device(c)) return rc;
+    const int k = chunk_planes(c, 4);
+    const size_t pp = plane_nodes(c->p);
+    double* outs[4] = {rho, ux, uy, uz};
+    for (int z0 = 0; z0 < c->p.nz; z0 += k) {
+        const int nzc = std::min(k, c->p.nz - z0);
+        const size_t n = (size_t)nzc * pp;
+        double* d[4];
+        for (int a = 0; a < 4; ++a) d[a] = outs[a] ? c->d_stage + a * n : nullptr;
+        CK(launch_macro(c->s, c->parity, d[0], d[1], d[2], d[3], z0, nzc, c->stream));
+        for (int a = 0; a < 4; ++a)
+            if (outs[a])
+                CK(cudaMemcpyAsync(outs[a] + (size_t)z0 * pp, d[a], n * 8, cudaMemcpyDeviceToHost, c->stream));
+    }
+    return sync(c);
+}
+
+int lbm_profiles(lbm_ctx* c, double* out) {
+    if (check_ctx(c) || !out) return fail(LBM_ERR_INVALID_ARG, "null argument");
+    if (int rc = set_device(c)) return rc;
+    const int nb = profile_blocks(c->s);
+    const size_t need = (size_t)c->s.g.NZ * nb * LBM_PROFILE_COLS;
+    if (int rc = ensure_red(c, need)) return rc;
+    CK(launch_profiles(c->s, c->parity, c->d_red, nb, c->stream));
+    std::vector<double> h(need);
+    CK(cudaMemcpyAsync(h.data(), c->d_red, need * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (int rc = sync(c)) return rc;
+    for (int z = 0; z < c->s.g.NZ; ++z)
+        for (int k = 0; k < LBM_PROFILE_COLS; ++k) {
+            double acc = 0.0;
+            for (int b = 0; b < nb; ++b) acc += h[((size_t)z * nb + b) * LBM_PROFILE_COLS + k];
+            out[k + (size_t)LBM_PROFILE_COLS * z] = acc;
+        }
+    return LBM_OK;
+}
+
+int lbm_diag(lbm_ctx* c, lbm_stats* st) {
+    if (check_ctx(c) || !st) return fail(LBM_ERR_INVALID_ARG, "null argument");
+    std::vector<double> prof((size_t)LBM_PROFILE_COLS * c->p.nx);
+    if (int rc = lbm_profiles(c, prof.data())) return rc;
+    std::memset(st, 0, sizeof(*st));
+    double n = 0.0;
+    for (int ix = 0; ix < c->p.nx; ++ix) {
+        const double* r = &prof[(size_t)LBM_PROFILE_COLS * ix];
+        st->mom_sum[0] += r[0]; st->mom_sum[1] += r[1]; st->mom_sum[2] += r[2];
+        st->usq_sum[0] += r[6]; st->usq_sum[1] += r[7]; st->usq_sum[2] += r[8];
+        st->rho_sum += r[9];
+        n += r[11];
+    }
+    const size_t need = (size_t)kExtremaBlocks * 5;
+    if (int rc = ensure_red(c, need)) return rc;
+    CK(launch_extrema(c->s, c->parity, c->d_red, c->stream));
+    std::vector<double> h(need);
+    CK(cudaMemcpyAsync(h.data(), c->d_red, need * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (int rc = sync(c)) return rc;
+    double rmax = -INFINITY, rmin = INFINITY, vmax = -1.0, vidx = 0.0, nonf = 0.0;
+    for (int b = 0; b < kExtremaBlocks; ++b) {
+        const double* r = &h[(size_t)b * 5];
+        rmax = std::max(rmax, r[0]);
+        rmin = std::min(rmin, r[1]);
+        if (r[2] > vmax || (r[2] == vmax && r[3] < vidx)) { vmax = r[2]; vidx = r[3]; }
+        nonf += r[4];
+    }
+    st->nfluid = (int64_t)(n + 0.5);
+    st->rho_max = rmax;
+    st->rho_min = rmin;
+    st->vmax = vmax;
+    const int64_t li = (int64_t)vidx;
+    st->vmax_at[0] = (int32_t)(li % c->p.nx) + 1;
+    st->vmax_at[1] = (int32_t)((li / c->p.nx) % c->p.ny) + 1;
+    st->vmax_at[2] = (int32_t)(li / ((int64_t)c->p.nx * c->p.ny)) + 1;
+    st->nonfinite = (int32_t)nonf;
+    return st->nonfinite ? fail(LBM_ERR_NONFINITE, "non-finite populations present") : LBM_OK;
+}
+
+int lbm_avedensity(lbm_ctx* c, double* mean) {
+    if (check_ctx(c)) return LBM_ERR_INVALID_ARG;
+    std::vector<double> prof((size_t)LBM_PROFILE_COLS * c->p.nx);
+    if (int rc = lbm_profiles(c, prof.data())) return rc;
+    double s = 0.0, n = 0.0;
+    for (int ix = 0; ix < c->p.nx; ++ix) {
+        s += prof[(size_t)LBM_PROFILE_COLS * ix + 9];
+        n += prof[(size_t)LBM_PROFILE_COLS * ix + 11];
+    }
+    const double m = n > 0 ? s / n : 0.0;
+    if (mean) *mean = m;
+    CK(launch_add_rest(c->s, c->parity, -m, c->stream));
+    return sync(c);
+}
+
+int lbm_save_flow(lbm_ctx* c, const char* path, int32_t kind, const int32_t* ints) {
+    if (check_ctx(c) || !path || !ints) return fail(LBM_ERR_INVALID_ARG, "null argument");
+    if (kind != 0 && kind != 1) return fail(LBM_ERR_INVALID_ARG, "kind must be 0 or 1");
+    if (int rc = set_device(c)) return rc;
+    FILE* fp = std::fopen(path, "wb");
+    if (!fp) return fail(LBM_ERR_IO, std::string("cannot open ") + path);
+    const int nints = kind == 0 ? 1 : 3;
+    {
+        RecordWriter w(fp, 4 * nints);
+        w.put(ints, 4 * nints);
+        if (!w.ok) { std::fclose(fp); return fail(LBM_ERR_IO, "write failed"); }
+    }
+    const size_t per_plane = plane_nodes(c->p) * Q;
+    RecordWriter w(fp, (int64_t)(nodes(c->p) * Q * 8));
+    const int k = chunk_planes(c, Q);
+    std::vector<double> h((size_t)k * per_plane);
+    for (int z0 = 0; z0 < c->p.nz && w.ok; z0 += k) {
+        const int nzc = std::min(k, c->p.nz - z0);
+        cudaError_t e = launch_store_to_aos(c->s, c->parity, c->d_stage, z0, nzc, c->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(h.data(), c->d_stage, (size_t)nzc * per_plane * 8, cudaMemcpyDeviceToHost,
+                                c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) { std::fclose(fp); return cuda_fail(e, "checkpoint download"); }
+        w.put(h.data(), (int64_t)nzc * per_plane * 8);
+    }
+    const bool ok = w.ok && w.done == w.total;
+    if (std::fclose(fp) != 0 || !ok) return fail(LBM_ERR_IO, "write failed");
+    return LBM_OK;
+}
+
+int lbm_load_flow(lbm_ctx* c, const char* path, int32_t kind, int32_t* ints) {
+    if (check_ctx(c) || !path) return fail(LBM_ERR_INVALID_ARG, "null argument");
+    if (kind != 0 && kind != 1) return fail(LBM_ERR_INVALID_ARG, "kind must be 0 or 1");
+    if (int rc = set_device(c)) return rc;
+    FILE* fp = std::fopen(path, "rb");
+    if (!fp) return fail(LBM_ERR_IO, std::string("cannot open ") + path);
+    const int nints = kind == 0 ? 1 : 3;
+    int32_t hdr[3] = {0, 0, 0};
+    {
+        RecordReader r(fp);
+        if (!r.ok || !r.get(hdr, 4 * nints) || !r.finish()) {
+            std::fclose(fp);
+            return fail(LBM_ERR_IO, "bad header record (expected " + std::to_string(nints) + " integers)");
+        }
+    }
+    RecordReader r(fp);
+    const size_t per_plane = plane_nodes(c->p) * Q;
+    const int k = chunk_planes(c, Q);
+    std::vector<double> h((size_t)k * per_plane);
+    for (int z0 = 0; z0 < c->p.nz; z0 += k) {
+        const int nzc = std::min(k, c->p.nz - z0);
+        if (!r.get(h.data(), (int64_t)nzc * per_plane * 8)) {
+            std::fclose(fp);
+            return fail(LBM_ERR_IO, "population record too short for this lattice");
+        }
+        cudaError_t e = cudaMemcpyAsync(c->d_stage, h.data(), (size_t)nzc * per_plane * 8,
+                                        cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = launch_aos_to_store(c->s, c->d_stage, z0, nzc, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) { std::fclose(fp); return cuda_fail(e, "checkpoint upload"); }
+    }
+    const bool exact = r.finish();
+    std::fclose(fp);
+    if (!exact) return fail(LBM_ERR_IO, "population record size does not match this lattice");
+    if (ints) for (int i = 0; i < nints; ++i) ints[i] = hdr[i];
+    c->parity = 0;
+    c->nsteps = 0;
+    return LBM_OK;
+}
+
+}  // extern "C"

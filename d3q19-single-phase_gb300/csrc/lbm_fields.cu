@@ -1,0 +1,383 @@
+// Non-hot kernels: layout conversion between the reference's AoS FP64 array
+// f(0:18,nx,ny,nz) and the device SoA storage, equilibrium initialisation,
+// macroscopic fields and FP64 reductions for the diagnostics.
+#include "lbm_internal.h"
+
+namespace lbm {
+
+// Channel initial velocity: Poiseuille profile along ref y (the steady laminar
+// solution of saveload.f90:924-926 with ustar -> uc) plus uniform noise of
+// +-amp*uc per component from the counter-based generator; the host copy
+// channel_velocity_host gives identical bits.
+__host__ __device__ inline void channel_velocity_node(int nx, int ny, int ix, int iy, int iz,
+                                                      double uc, double amp, uint64_t seed,
+                                                      double& u, double& v, double& w) {
+    // ix, iy, iz are 0-based reference indices; the profile is the steady
+    // laminar solution 4 uc ((nx/2)^2 - xx0^2) / nx^2, xx0 = |ix+1-0.5-nx/2|
+    const double half = 0.5 * (double)nx;
+    double xx0 = (double)ix + 0.5 - half;
+    xx0 = xx0 < 0 ? -xx0 : xx0;
+#ifdef __CUDA_ARCH__
+    const double prof = __ddiv_rn(__dmul_rn(4.0 * uc, __dsub_rn(__dmul_rn(half, half), __dmul_rn(xx0, xx0))),
+                                  __dmul_rn((double)nx, (double)nx));
+#else
+    const double prof = (4.0 * uc) * (half * half - xx0 * xx0) / ((double)nx * (double)nx);
+#endif
+    const uint64_t lin = (uint64_t)ix + (uint64_t)nx * ((uint64_t)iy + (uint64_t)ny * (uint64_t)iz);
+    const double a = amp * uc;
+#ifdef __CUDA_ARCH__
+    u = __dmul_rn(a, uniform_pm1(seed, 3 * lin + 0));
+    v = __dadd_rn(prof, __dmul_rn(a, uniform_pm1(seed, 3 * lin + 1)));
+    w = __dmul_rn(a, uniform_pm1(seed, 3 * lin + 2));
+#else
+    u = a * uniform_pm1(seed, 3 * lin + 0);
+    v = prof + a * uniform_pm1(seed, 3 * lin + 1);
+    w = a * uniform_pm1(seed, 3 * lin + 2);
+#endif
+}
+
+namespace {
+
+template <typename T>
+__device__ __forceinline__ T* pop_plane(const DeviceState& s, int i) {
+    return static_cast<T*>(s.f) + (size_t)i * s.pstride;
+}
+
+// Natural (post-stream) populations of GPU node (x,y,z), true units, FP64.
+// parity 0: slot i at n.  parity 1 (after an even AA step): f_i(x) sits in
+// slot opp(i) at x - c_i, or in slot i at x when x - c_i is beyond a wall.
+template <typename T>
+__device__ void gather_natural(const DeviceState& s, int parity, int x, int y, int z,
+                               double f[Q]) {
+    const Geometry& g = s.g;
+    const double invS = s.cd.invS;
+    const uint32_t n = x + g.NX * (y + g.NY * (uint32_t)z);
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        uint32_t m = n;
+        int slot = i;
+        if (parity) {
+            const int zs = z - DZg(i);
+            if (zs >= 0 && zs < g.NZ) {
+                int xs = x - DXg(i); xs = xs < 0 ? xs + g.NX : (xs >= g.NX ? xs - g.NX : xs);
+                int ys = y - DYg(i); ys = ys < 0 ? ys + g.NY : (ys >= g.NY ? ys - g.NY : ys);
+                m = xs + g.NX * (ys + g.NY * (uint32_t)zs);
+                slot = OPPf(i);
+            }
+        }
+        f[i] = (double)ld_pop(pop_plane<T>(s, slot) + m) * invS;
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void put(const DeviceState& s, int i, uint32_t n, double v_true) {
+    const double S = s.cd.S;
+    if constexpr (sizeof(T) == 8) pop_plane<T>(s, i)[n] = v_true * S;
+    else st_pop(pop_plane<T>(s, i) + n, (float)(v_true * S));
+}
+
+// Thread mapping for reference-layout chunks: threadIdx.x/blockIdx.x -> ref y
+// (GPU X, contiguous in the SoA planes), blockIdx.y -> ref x, blockIdx.z -> ref
+// z inside the chunk.
+struct RefNode { int ix, iy, iz; bool ok; };
+__device__ __forceinline__ RefNode ref_node(const Geometry& g, int z0) {
+    RefNode r;
+    r.iy = blockIdx.x * blockDim.x + threadIdx.x;
+    r.ix = blockIdx.y;
+    r.iz = z0 + blockIdx.z;
+    r.ok = r.iy < g.NX;
+    return r;
+}
+// 0-based reference-layout linear node index (x fastest)
+__device__ __forceinline__ size_t ref_lin(const Geometry& g, int ix, int iy, int iz) {
+    return (size_t)ix + (size_t)g.NZ * ((size_t)iy + (size_t)g.NX * iz);
+}
+__device__ __forceinline__ uint32_t gpu_lin(const Geometry& g, int ix, int iy, int iz) {
+    return (uint32_t)iy + g.NX * ((uint32_t)iz + g.NY * (uint32_t)ix);
+}
+
+template <typename T>
+__global__ void k_aos_to_store(DeviceState s, const double* __restrict__ aos, int z0) {
+    const RefNode r = ref_node(s.g, z0);
+    if (!r.ok) return;
+    const size_t src = 19 * ref_lin(s.g, r.ix, r.iy, r.iz - z0);
+    const uint32_t n = gpu_lin(s.g, r.ix, r.iy, r.iz);
+#pragma unroll
+    for (int i = 0; i < Q; ++i) put<T>(s, i, n, aos[src + i]);
+}
+
+template <typename T>
+__global__ void k_store_to_aos(DeviceState s, int parity, double* __restrict__ aos, int z0) {
+    const RefNode r = ref_node(s.g, z0);
+    if (!r.ok) return;
+    double f[Q];
+    gather_natural<T>(s, parity, r.iy, r.iz, r.ix, f);
+    const size_t dst = 19 * ref_lin(s.g, r.ix, r.iy, r.iz - z0);
+#pragma unroll
+    for (int i = 0; i < Q; ++i) aos[dst + i] = f[i];
+}
+
+// initpop (initial.f90:19-46) at delta-rho = 0; explicit round-to-nearest
+// operations (no FMA contraction) so that host code gets identical bits.
+__device__ __forceinline__ void equilibrium_rn(double ux, double uy, double uz, double f[Q]) {
+    const double usqr = __dmul_rn(1.5, __dadd_rn(__dadd_rn(__dmul_rn(ux, ux), __dmul_rn(uy, uy)),
+                                                 __dmul_rn(uz, uz)));
+    f[0] = __dmul_rn(W0, __dsub_rn(0.0, usqr));
+#pragma unroll
+    for (int i = 1; i < Q; ++i) {
+        const double G = __dadd_rn(__dadd_rn(__dmul_rn((double)CXf(i), ux), __dmul_rn((double)CYf(i), uy)),
+                                   __dmul_rn((double)CZf(i), uz));
+        const double t = __dsub_rn(__dadd_rn(__dadd_rn(0.0, __dmul_rn(3.0, G)),
+                                             __dmul_rn(__dmul_rn(4.5, G), G)), usqr);
+        f[i] = __dmul_rn(weight(i), t);
+    }
+}
+
+template <typename T>
+__global__ void k_initpop(DeviceState s, const double* __restrict__ ux, const double* __restrict__ uy,
+                          const double* __restrict__ uz, int z0) {
+    const RefNode r = ref_node(s.g, z0);
+    if (!r.ok) return;
+    const size_t src = ref_lin(s.g, r.ix, r.iy, r.iz - z0);
+    double f[Q];
+    equilibrium_rn(ux[src], uy[src], uz[src], f);
+    const uint32_t n = gpu_lin(s.g, r.ix, r.iy, r.iz);
+#pragma unroll
+    for (int i = 0; i < Q; ++i) put<T>(s, i, n, f[i]);
+}
+
+template <typename T>
+__global__ void k_init_channel(DeviceState s, double uc, double amp, uint64_t seed) {
+    const RefNode r = ref_node(s.g, 0);
+    if (!r.ok) return;
+    double u, v, w;
+    channel_velocity_node(s.g.NZ, s.g.NX, r.ix, r.iy, r.iz, uc, amp, seed, u, v, w);
+    double f[Q];
+    equilibrium_rn(u, v, w, f);
+    const uint32_t n = gpu_lin(s.g, r.ix, r.iy, r.iz);
+#pragma unroll
+    for (int i = 0; i < Q; ++i) put<T>(s, i, n, f[i]);
+}
+
+// macrovar (collision.f90:394-418) for fluid nodes
+__device__ __forceinline__ void macro_of(const double f[Q], const double F[3], double& rho,
+                                         double& ux, double& uy, double& uz) {
+    double r = 0.0, a = 0.0, b = 0.0, c = 0.0;
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        r += f[i];
+        if (CXf(i)) a += CXf(i) * f[i];
+        if (CYf(i)) b += CYf(i) * f[i];
+        if (CZf(i)) c += CZf(i) * f[i];
+    }
+    rho = r; ux = a + 0.5 * F[0]; uy = b + 0.5 * F[1]; uz = c + 0.5 * F[2];
+}
+
+template <typename T>
+__global__ void k_macro(DeviceState s, int parity, double* rho, double* ux, double* uy,
+                        double* uz, int z0) {
+    const RefNode r = ref_node(s.g, z0);
+    if (!r.ok) return;
+    double f[Q];
+    gather_natural<T>(s, parity, r.iy, r.iz, r.ix, f);
+    const double F[3] = {(double)s.cd.Fx, (double)s.cd.Fy, (double)s.cd.Fz};
+    double d, a, b, c;
+    macro_of(f, F, d, a, b, c);
+    const size_t o = ref_lin(s.g, r.ix, r.iy, r.iz - z0);
+    if (rho) rho[o] = d;
+    if (ux) ux[o] = a;
+    if (uy) uy[o] = b;
+    if (uz) uz[o] = c;
+}
+
+__global__ void k_ref_to_gpu_vec(Geometry g, size_t N, const double* __restrict__ ux,
+                                 const double* __restrict__ uy, const double* __restrict__ uz,
+                                 double* __restrict__ uf, int z0) {
+    const RefNode r = ref_node(g, z0);
+    if (!r.ok) return;
+    const size_t src = ref_lin(g, r.ix, r.iy, r.iz - z0);
+    const uint32_t n = gpu_lin(g, r.ix, r.iy, r.iz);
+    uf[n] = ux[src]; uf[N + n] = uy[src]; uf[2 * N + n] = uz[src];
+}
+
+constexpr int kRedThreads = 256;
+
+// Plane sums for statistc2: block (b, Z) covers part of plane Z (ref x = Z+1).
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads)
+k_profiles(DeviceState s, int parity, double* __restrict__ partial) {
+    const Geometry& g = s.g;
+    const int z = blockIdx.y;
+    const double F[3] = {(double)s.cd.Fx, (double)s.cd.Fy, (double)s.cd.Fz};
+    double acc[LBM_PROFILE_COLS];
+#pragma unroll
+    for (int k = 0; k < LBM_PROFILE_COLS; ++k) acc[k] = 0.0;
+    const uint32_t plane = g.NXY;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < plane; t += gridDim.x * blockDim.x) {
+        const int x = t % g.NX, y = t / g.NX;
+        double f[Q];
+        gather_natural<T>(s, parity, x, y, z, f);
+        double rho, ux, uy, uz;
+        macro_of(f, F, rho, ux, uy, uz);
+        acc[0] += ux; acc[1] += uy; acc[2] += uz;
+        acc[3] += ux * uz; acc[4] += ux * uy; acc[5] += uy * uz;
+        acc[6] += ux * ux; acc[7] += uy * uy; acc[8] += uz * uz;
+        acc[9] += rho; acc[10] += rho * rho; acc[11] += 1.0;
+    }
+    __shared__ double sh[LBM_PROFILE_COLS][kRedThreads / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < LBM_PROFILE_COLS; ++k) {
+        double v = acc[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) sh[k][wid] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < LBM_PROFILE_COLS) {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x / 32); ++w) v += sh[threadIdx.x][w];
+        partial[((size_t)z * gridDim.x + blockIdx.x) * LBM_PROFILE_COLS + threadIdx.x] = v;
+    }
+}
+
+// Per-block extrema: {rho_max, rho_min, vmax, vmax_refidx, nonfinite}
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads)
+k_extrema(DeviceState s, int parity, double* __restrict__ partial) {
+    const Geometry& g = s.g;
+    const double F[3] = {(double)s.cd.Fx, (double)s.cd.Fy, (double)s.cd.Fz};
+    double rmax = -INFINITY, rmin = INFINITY, vmax = -1.0, vidx = 0.0, nonf = 0.0;
+    const size_t N = s.N;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < N;
+         t += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(t % g.NX);
+        const int y = (int)((t / g.NX) % g.NY);
+        const int z = (int)(t / g.NXY);
+        double f[Q];
+        gather_natural<T>(s, parity, x, y, z, f);
+        bool finite = true;
+#pragma unroll
+        for (int i = 0; i < Q; ++i) finite &= isfinite(f[i]);
+        if (!finite) { nonf += 1.0; continue; }
+        double rho, ux, uy, uz;
+        macro_of(f, F, rho, ux, uy, uz);
+        rmax = fmax(rmax, rho); rmin = fmin(rmin, rho);
+        const double v = sqrt(ux * ux + uy * uy + uz * uz);
+        const double ri = (double)ref_lin(g, z, x, y);
+        if (v > vmax || (v == vmax && ri < vidx)) { vmax = v; vidx = ri; }
+    }
+    __shared__ double sh[5][kRedThreads];
+    sh[0][threadIdx.x] = rmax; sh[1][threadIdx.x] = rmin; sh[2][threadIdx.x] = vmax;
+    sh[3][threadIdx.x] = vidx; sh[4][threadIdx.x] = nonf;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) {
+            const int o = threadIdx.x + h;
+            sh[0][threadIdx.x] = fmax(sh[0][threadIdx.x], sh[0][o]);
+            sh[1][threadIdx.x] = fmin(sh[1][threadIdx.x], sh[1][o]);
+            const double va = sh[2][threadIdx.x], vb = sh[2][o];
+            if (vb > va || (vb == va && sh[3][o] < sh[3][threadIdx.x])) {
+                sh[2][threadIdx.x] = vb; sh[3][threadIdx.x] = sh[3][o];
+            }
+            sh[4][threadIdx.x] += sh[4][o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x < 5) partial[(size_t)blockIdx.x * 5 + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+// Subtract w_i*delta from every population.  The weights are symmetric
+// (w_i = w_opp(i)) and every (population, node) value occupies exactly one
+// slot in either AA orientation, so the slot's own weight is the right one.
+template <typename T>
+__global__ void k_add_rest(DeviceState s, double delta) {
+    const size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= s.N) return;
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        T* p = pop_plane<T>(s, i) + n;
+        const double v = (double)ld_pop(p) + weight(i) * delta * s.cd.S;
+        if constexpr (sizeof(T) == 8) *p = v; else st_pop(p, (float)v);
+    }
+}
+
+dim3 ref_grid(const Geometry& g, int nzc, int bx) {
+    return dim3((g.NX + bx - 1) / bx, g.NZ, nzc);
+}
+constexpr int kBx = 128;
+
+}  // namespace
+
+void channel_velocity_host(int nx, int ny, int nz, double uc, double amp, uint64_t seed,
+                           double* ux, double* uy, double* uz) {
+    for (int iz = 0; iz < nz; ++iz)
+        for (int iy = 0; iy < ny; ++iy)
+            for (int ix = 0; ix < nx; ++ix) {
+                const size_t o = (size_t)ix + (size_t)nx * ((size_t)iy + (size_t)ny * iz);
+                channel_velocity_node(nx, ny, ix, iy, iz, uc, amp, seed, ux[o], uy[o], uz[o]);
+            }
+}
+
+#define LBM_DISPATCH(PREC_EXPR, CALL)                                   \
+    switch (PREC_EXPR) {                                                \
+        case LBM_PREC_FP64: { using T = double; CALL; } break;          \
+        case LBM_PREC_FP32: { using T = float; CALL; } break;           \
+        case LBM_PREC_FP16: { using T = __half; CALL; } break;          \
+        default: return cudaErrorInvalidValue;                          \
+    }                                                                   \
+    return cudaGetLastError();
+
+cudaError_t launch_aos_to_store(const DeviceState& s, const double* aos, int z0, int nzc,
+                                cudaStream_t st) {
+    LBM_DISPATCH(s.prec, (k_aos_to_store<T><<<ref_grid(s.g, nzc, kBx), kBx, 0, st>>>(s, aos, z0)))
+}
+
+cudaError_t launch_store_to_aos(const DeviceState& s, int parity, double* aos, int z0, int nzc,
+                                cudaStream_t st) {
+    LBM_DISPATCH(s.prec, (k_store_to_aos<T><<<ref_grid(s.g, nzc, kBx), kBx, 0, st>>>(s, parity, aos, z0)))
+}
+
+cudaError_t launch_initpop(const DeviceState& s, const double* ux, const double* uy,
+                           const double* uz, int z0, int nzc, cudaStream_t st) {
+    LBM_DISPATCH(s.prec, (k_initpop<T><<<ref_grid(s.g, nzc, kBx), kBx, 0, st>>>(s, ux, uy, uz, z0)))
+}
+
+cudaError_t launch_init_channel(const DeviceState& s, double uc, double amp, uint64_t seed,
+                                cudaStream_t st) {
+    LBM_DISPATCH(s.prec, (k_init_channel<T><<<ref_grid(s.g, s.g.NY, kBx), kBx, 0, st>>>(s, uc, amp, seed)))
+}
+
+cudaError_t launch_macro(const DeviceState& s, int parity, double* rho, double* ux, double* uy,
+                         double* uz, int z0, int nzc, cudaStream_t st) {
+    LBM_DISPATCH(s.prec, (k_macro<T><<<ref_grid(s.g, nzc, kBx), kBx, 0, st>>>(s, parity, rho, ux, uy, uz, z0)))
+}
+
+cudaError_t launch_ref_to_gpu_vec(const DeviceState& s, const double* ux, const double* uy,
+                                  const double* uz, double* uf, int z0, int nzc, cudaStream_t st) {
+    k_ref_to_gpu_vec<<<ref_grid(s.g, nzc, kBx), kBx, 0, st>>>(s.g, s.N, ux, uy, uz, uf, z0);
+    return cudaGetLastError();
+}
+
+int profile_blocks(const DeviceState& s) {
+    const uint32_t plane = s.g.NXY;
+    int nb = (int)((plane + kRedThreads * 8 - 1) / (kRedThreads * 8));
+    return nb < 1 ? 1 : (nb > 64 ? 64 : nb);
+}
+
+cudaError_t launch_profiles(const DeviceState& s, int parity, double* partial, int nblk,
+                            cudaStream_t st) {
+    LBM_DISPATCH(s.prec, (k_profiles<T><<<dim3(nblk, s.g.NZ), kRedThreads, 0, st>>>(s, parity, partial)))
+}
+
+cudaError_t launch_extrema(const DeviceState& s, int parity, double* partial,
+                           cudaStream_t st) {
+    LBM_DISPATCH(s.prec, (k_extrema<T><<<kExtremaBlocks, kRedThreads, 0, st>>>(s, parity, partial)))
+}
+
+cudaError_t launch_add_rest(const DeviceState& s, int parity, double delta, cudaStream_t st) {
+    (void)parity;
+    const unsigned nb = (unsigned)((s.N + 255) / 256);
+    LBM_DISPATCH(s.prec, (k_add_rest<T><<<nb, 256, 0, st>>>(s, delta)))
+}
+
+}  // namespace lbm

@@ -1,0 +1,103 @@
+// Internal declarations shared by the CUDA translation units and the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <stddef.h>
+#include <stdint.h>
+#include <string>
+
+#include "../../include/lbm_gb300.h"
+#include "lbm_lattice.h"
+#include "lbm_collide.cuh"
+
+namespace lbm {
+
+// Storage type of each precision and its arithmetic type.
+template <int PREC> struct Prec;
+template <> struct Prec<LBM_PREC_FP64> { using T = double; using R = double; };
+template <> struct Prec<LBM_PREC_FP32> { using T = float;  using R = float; };
+template <> struct Prec<LBM_PREC_FP16> { using T = __half; using R = float; };
+
+__device__ __forceinline__ double ld_pop(const double* p) { return __ldg(p); }
+__device__ __forceinline__ float  ld_pop(const float* p)  { return __ldg(p); }
+__device__ __forceinline__ float  ld_pop(const __half* p) { return __half2float(__ldg(p)); }
+__device__ __forceinline__ void st_pop(double* p, double v) { *p = v; }
+__device__ __forceinline__ void st_pop(float* p, float v)   { *p = v; }
+__device__ __forceinline__ void st_pop(__half* p, float v)  { *p = __float2half_rn(v); }
+
+// One base pointer per population plane, passed by value so that every
+// address is a single IMAD.WIDE from the constant bank.
+template <typename T>
+struct PopPtrs { T* p[Q]; };
+
+struct Geometry {
+    int NX, NY, NZ;      // GPU axes (X = ref y, Y = ref z, Z = ref x)
+    uint32_t NXY;        // NX*NY
+};
+
+// Everything a step needs; built once per context.
+struct DeviceState {
+    int prec;
+    Geometry g;
+    size_t N;            // nodes
+    size_t pstride;      // elements between population planes
+    void* f;             // 19 * pstride elements of the storage type
+    CollideConsts<double> cd;
+    CollideConsts<float> cf;
+};
+
+// launchers (lbm_step.cu)
+cudaError_t launch_step(const DeviceState& s, int parity, cudaStream_t st);
+cudaError_t launch_prerelax(const DeviceState& s, int parity, const double* uf,
+                            double* rho_prev_and_new, unsigned long long* maxabs,
+                            cudaStream_t st);
+
+// field kernels (lbm_fields.cu)
+// AoS FP64 chunk (reference layout, ref z planes [z0, z0+nzc)) <-> storage.
+cudaError_t launch_aos_to_store(const DeviceState& s, const double* aos, int z0,
+                                int nzc, cudaStream_t st);
+cudaError_t launch_store_to_aos(const DeviceState& s, int parity, double* aos,
+                                int z0, int nzc, cudaStream_t st);
+// equilibrium from velocity arrays in reference layout (chunk of ref z planes)
+cudaError_t launch_initpop(const DeviceState& s, const double* ux,
+                           const double* uy, const double* uz, int z0, int nzc,
+                           cudaStream_t st);
+cudaError_t launch_init_channel(const DeviceState& s, double uc, double amp,
+                                uint64_t seed, cudaStream_t st);
+// macrovar for ref z planes [z0, z0+nzc) into reference-layout FP64 arrays
+cudaError_t launch_macro(const DeviceState& s, int parity, double* rho,
+                         double* ux, double* uy, double* uz, int z0, int nzc,
+                         cudaStream_t st);
+// velocity (nx*ny*nz*3 doubles, reference layout chunk) to GPU-layout frozen u
+cudaError_t launch_ref_to_gpu_vec(const DeviceState& s, const double* ux,
+                                  const double* uy, const double* uz,
+                                  double* uf, int z0, int nzc, cudaStream_t st);
+// plane sums (LBM_PROFILE_COLS per wall-normal plane) into partials
+// [NZ][nblk][COLS]; nblk returned through the call.
+cudaError_t launch_profiles(const DeviceState& s, int parity, double* partial,
+                            int nblk, cudaStream_t st);
+int profile_blocks(const DeviceState& s);
+// per-block extrema for diag: partial[kExtremaBlocks][5] =
+// {rho_max, rho_min, vmax, reference linear index of vmax, nonfinite count}
+constexpr int kExtremaBlocks = 1024;
+cudaError_t launch_extrema(const DeviceState& s, int parity, double* partial,
+                           cudaStream_t st);
+cudaError_t launch_add_rest(const DeviceState& s, int parity, double delta,
+                            cudaStream_t st);
+
+// splitmix64-based uniform in [-1, 1): identical on host and device
+__host__ __device__ inline uint64_t splitmix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+__host__ __device__ inline double uniform_pm1(uint64_t seed, uint64_t key) {
+    const uint64_t z = splitmix64(seed * 0xD1B54A32D192ED03ull + key);
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+}
+
+void channel_velocity_host(int nx, int ny, int nz, double uc, double amp,
+                           uint64_t seed, double* ux, double* uy, double* uz);
+
+}  // namespace lbm

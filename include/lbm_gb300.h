@@ -1,0 +1,210 @@
+/*
+ * lbm_gb300.h - C ABI of the GB300 (sm_103a) D3Q19 channel-flow time step.
+ *
+ * The reference (UDel-CFD/D3Q19-Single-Phase, Fortran 90 + MPI) exposes its
+ * hot path as argument-less subroutines working on module globals
+ * (Channel-Flow/var_inc.f90:84-150).  This header replaces them with explicit
+ * calls on an opaque context that owns all device state:
+ *
+ *   reference subroutine                         replaced by
+ *   ------------------------------------------   -------------------------------
+ *   para (rates, lattice, para.f90:106-214)      lbm_params_init / lbm_create
+ *   FORCING (collision.f90:515-527)              lbm_params.force[3]
+ *   initpop (initial.f90:19-46)                  lbm_initpop
+ *   initvel + initpop for the channel configs    lbm_init_channel (device IC)
+ *   collision_MRT + collisionExchnge + macrovar  lbm_step
+ *     (collision.f90:24-273, 281-372, 378-463;
+ *      call order main.f90:157-161)
+ *   rhoupdat + pre-relaxation loop               lbm_prerelax
+ *     (collision.f90:469-480, main.f90:69-90)
+ *   macrovar results rho, ux, uy, uz             lbm_macrovar
+ *   f(0:18,lx,ly,lz) in memory                   lbm_upload_f / lbm_download_f
+ *   avedensity (collision.f90:487-513)           lbm_avedensity
+ *   diag / statistc / statistc2 sums             lbm_diag / lbm_profiles
+ *     (saveload.f90:1202-1676)
+ *   saveinitflow / savecntdflow /                lbm_save_flow / lbm_load_flow
+ *   loadinitflow / loadcntdflow
+ *     (saveload.f90:102-231, 296-332)
+ *
+ * Conventions
+ *  - Every call returns 0 (LBM_OK) or a negative LBM_ERR_* code; nothing
+ *    exits or throws across the ABI.  lbm_strerror() gives a message and
+ *    lbm_last_error() the detail of the most recent failure on this thread.
+ *  - Host arrays use the reference layout and axes: f(0:18,nx,ny,nz) in
+ *    Fortran (column-major) order, i.e. flat index
+ *    ip + 19*((ix-1) + nx*((iy-1) + ny*(iz-1))); macroscopic arrays are
+ *    (nx,ny,nz).  x is wall-normal (half-way bounce-back walls at x=1/2 and
+ *    x=nx+1/2), y is streamwise and z spanwise, both periodic.  Population
+ *    order is d'Humieres et al. (2002) as in para.f90:176-214.
+ *  - Populations are deviations from the rest state (f_i - w_i rho0), the
+ *    reference's own stored variable (initial.f90:26-44).  All host arrays are
+ *    double precision, the reference's -r8 REAL.
+ *  - Host pointers are borrowed only for the duration of a call.  Calls are
+ *    synchronous at the ABI edge unless named *_async.  One host thread per
+ *    context; one GPU and one CUDA stream per context.
+ */
+#ifndef LBM_GB300_H
+#define LBM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+    LBM_OK = 0,
+    LBM_ERR_INVALID_ARG = -1,   /* bad pointer, size or parameter            */
+    LBM_ERR_CUDA = -2,          /* a CUDA runtime call failed                */
+    LBM_ERR_OOM = -3,           /* device or pinned host allocation failed   */
+    LBM_ERR_STATE = -4,         /* call not valid in the context's state     */
+    LBM_ERR_NOT_CONVERGED = -5, /* pre-relaxation hit its iteration limit    */
+    LBM_ERR_IO = -6,            /* checkpoint file missing/short/corrupt     */
+    LBM_ERR_NONFINITE = -7,     /* NaN/Inf detected in the populations       */
+    LBM_ERR_UNSUPPORTED = -8    /* feature not available in this build/GPU   */
+};
+
+/* ---- storage precision of the populations -------------------------------- */
+enum {
+    LBM_PREC_FP64 = 0,  /* FP64 storage, FP64 arithmetic (parity path)           */
+    LBM_PREC_FP32 = 1,  /* FP32 storage, FP32 arithmetic                         */
+    LBM_PREC_FP16 = 2   /* FP16 storage of scale*(f_i - w_i), FP32 arithmetic    */
+};
+
+/* MRT rate sets of para.f90:110-141 */
+enum { LBM_MRT_STABLE = 1, LBM_MRT_LBGK = 2, LBM_MRT_LOWDISS = 3 };
+
+/*
+ * Run parameters.  Mirrors the scalar globals that para.f90 computes and
+ * collision_MRT reads (var_inc.f90:85-93).  Fill it with lbm_params_init()
+ * and override fields, or copy them from an existing para.f90 run.
+ */
+typedef struct lbm_params {
+    int32_t nx, ny, nz;       /* lattice size, reference axes (var_inc.f90:51) */
+    int32_t precision;        /* LBM_PREC_*                                    */
+    double  s1, s2, s4, s9, s10, s13, s16;  /* MRT relaxation rates            */
+    double  omegepsl, omegepslj, omegxx;    /* equilibrium coefficients        */
+    double  force[3];         /* uniform body force (force_realx/y/z)          */
+    double  fp16_scale;       /* fixed FP16 storage scale (0 -> 32768)         */
+    int32_t device;           /* CUDA device ordinal                           */
+    int32_t reserved;
+} lbm_params;
+
+/* Global diagnostics over fluid nodes (diag, saveload.f90:1507-1676, plus the
+ * mass and momentum sums of avedensity, collision.f90:487-513).  Velocities
+ * are the macrovar ones (momentum including F/2), reference axes. */
+typedef struct lbm_stats {
+    int64_t nfluid;           /* fluid node count                              */
+    double  rho_sum;          /* sum of delta-rho (mass drift monitor)         */
+    double  mom_sum[3];       /* sum of ux, uy, uz                             */
+    double  usq_sum[3];       /* sum of ux^2, uy^2, uz^2                       */
+    double  rho_max, rho_min; /* extreme delta-rho                             */
+    double  vmax;             /* max |u|                                       */
+    int32_t vmax_at[3];       /* 1-based (ix,iy,iz) of vmax                    */
+    int32_t nonfinite;        /* number of nodes with a NaN/Inf population     */
+} lbm_stats;
+
+/* Number of columns lbm_profiles writes per wall-normal plane; the order is
+ * sum over the plane of: ux, uy, uz, ux*uz, ux*uy, uy*uz, ux^2, uy^2, uz^2,
+ * rho, rho^2, fluid count (the sums of statistc2, saveload.f90:1392-1423). */
+#define LBM_PROFILE_COLS 12
+
+typedef struct lbm_ctx lbm_ctx;
+
+const char* lbm_strerror(int code);
+const char* lbm_last_error(void);
+int lbm_version(void);
+
+/* Fill p with the para.f90 values for the given lattice, MRT type
+ * (para.f90:106-141: s9 = s13 = 1/(3 visc + 0.5)) and streamwise body force
+ * (applied along reference y, FORCING collision.f90:522-524). */
+int lbm_params_init(lbm_params* p, int32_t nx, int32_t ny, int32_t nz,
+                    int32_t mrt_type, double visc, double force_y,
+                    int32_t precision);
+
+/* Allocate device state for p (populations in HBM, SoA, in-place).  Replaces
+ * allocarray (para.f90:418-447) for the fluid arrays. */
+int lbm_create(const lbm_params* p, lbm_ctx** out);
+int lbm_destroy(lbm_ctx* ctx);
+
+/* Device bytes held by the context. */
+int lbm_device_bytes(const lbm_ctx* ctx, size_t* bytes);
+
+/* Populations in the reference layout f(0:18,nx,ny,nz), natural
+ * (post-streaming) orientation, FP64.  Upload resets the step parity. */
+int lbm_upload_f(lbm_ctx* ctx, const double* f);
+int lbm_download_f(lbm_ctx* ctx, double* f);
+
+/* initpop (initial.f90:19-46): f = equilibrium at delta-rho = 0 for the given
+ * velocity arrays (nx,ny,nz). */
+int lbm_initpop(lbm_ctx* ctx, const double* ux, const double* uy,
+                const double* uz);
+
+/* Device-side initial condition for the channel configurations: laminar
+ * Poiseuille profile along y with centreline velocity uc (the analytic
+ * steady solution of saveload.f90:926) plus uniform random perturbations of
+ * +-amp*uc in all three components drawn from a counter-based generator
+ * (splitmix64 of seed and node index), then initpop.  Host code can
+ * reproduce the same field exactly; see lbm_channel_velocity. */
+int lbm_init_channel(lbm_ctx* ctx, double uc, double amp, uint64_t seed);
+
+/* Host-side copy of the velocity field lbm_init_channel builds (arrays of
+ * nx*ny*nz doubles, reference layout). Needs no context or GPU. */
+int lbm_channel_velocity(int32_t nx, int32_t ny, int32_t nz, double uc,
+                         double amp, uint64_t seed, double* ux, double* uy,
+                         double* uz);
+
+/* nsteps x (collision_MRT + periodic exchange + macrovar); synchronous. */
+int lbm_step(lbm_ctx* ctx, int32_t nsteps);
+/* Same, enqueued on the context's stream without waiting. */
+int lbm_step_async(lbm_ctx* ctx, int32_t nsteps);
+int lbm_synchronize(lbm_ctx* ctx);
+/* The context's cudaStream_t, for event timing by the caller. */
+int lbm_stream(lbm_ctx* ctx, void** stream);
+/* Steps taken since the last upload / init. */
+int lbm_step_count(const lbm_ctx* ctx, int64_t* nsteps);
+
+/* Density pre-relaxation of main.f90:69-90 with the velocity frozen at
+ * (ux,uy,uz) (arrays (nx,ny,nz)): repeat {rho = sum f (rhoupdat);
+ * collision with the frozen velocity} until max|rho - rho_prev| <= eps or the
+ * iteration counter exceeds maxit.  iters/err receive the final counter and
+ * residual.  Returns LBM_ERR_NOT_CONVERGED only if maxit was exceeded. */
+int lbm_prerelax(lbm_ctx* ctx, const double* ux, const double* uy,
+                 const double* uz, double eps, int32_t maxit, int32_t* iters,
+                 double* err);
+
+/* macrovar (collision.f90:378-418): rho = sum f, u = sum c f + F/2, written to
+ * host arrays (nx,ny,nz); any pointer may be NULL to skip it. */
+int lbm_macrovar(lbm_ctx* ctx, double* rho, double* ux, double* uy,
+                 double* uz);
+
+/* Global fluid-node diagnostics (diag) computed on the device in FP64. */
+int lbm_diag(lbm_ctx* ctx, lbm_stats* st);
+
+/* Plane sums for statistc/statistc2: out[LBM_PROFILE_COLS*nx], column-major
+ * (column c of plane ix at out[c + LBM_PROFILE_COLS*(ix-1)]). FP64. */
+int lbm_profiles(lbm_ctx* ctx, double* out);
+
+/* avedensity (collision.f90:487-513): subtract the fluid-mean delta-rho from
+ * every node; here applied to the rest population so that rho = sum f moves
+ * by the mean.  mean (may be NULL) receives the value removed. */
+int lbm_avedensity(lbm_ctx* ctx, double* mean);
+
+/* Checkpoints in the reference's Fortran unformatted sequential format (4-byte
+ * record markers, gfortran sub-records above 2 GiB):
+ *   kind 0: finit.NNN   = {istat}{f}             (saveinitflow, :102-124)
+ *   kind 1: endrunflow  = {istep,istat,imovie}{f} (savecntdflow, :196-231)
+ * f is FP64, natural orientation, reference layout.  ints[] carries the
+ * integer header (1 or 3 values). */
+int lbm_save_flow(lbm_ctx* ctx, const char* path, int32_t kind,
+                  const int32_t* ints);
+int lbm_load_flow(lbm_ctx* ctx, const char* path, int32_t kind,
+                  int32_t* ints);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LBM_GB300_H */

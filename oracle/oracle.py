@@ -1,0 +1,223 @@
+"""ctypes binding of the FP64 CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg
+use this module, and only as the checker.  The product library and package
+never import it.  Parity status: see ``lbm_oracle.h`` (pinned by the
+reference's analytic Poiseuille series and by swap == push self-consistency;
+no executed-reference vectors exist because the Fortran reference cannot be
+built here).
+"""
+from __future__ import annotations
+
+import ctypes
+import shutil
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "liblbm_oracle.so"
+CFLAGS = ["-O2", "-std=c11", "-ffp-contract=off", "-fopenmp", "-fPIC", "-Wall", "-Wextra"]
+
+Q = 19
+CX = np.array([0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0])
+CY = np.array([0, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1, 0, 0, 0, 0, 1, -1, 1, -1])
+CZ = np.array([0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1])
+OPP = np.array([0, 2, 1, 4, 3, 6, 5, 10, 9, 8, 7, 14, 13, 12, 11, 18, 17, 16, 15])
+W = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
+
+
+def build(force: bool = False) -> Path:
+    src = [HERE / "lbm_oracle.c", HERE / "lbm_oracle.h"]
+    if force or not LIB.exists() or any(s.stat().st_mtime > LIB.stat().st_mtime for s in src):
+        LIB.parent.mkdir(exist_ok=True)
+        cc = shutil.which("gcc") or "gcc"
+        tmp = LIB.with_suffix(".tmp")
+        subprocess.run([cc, *CFLAGS, "-shared", "-o", str(tmp), str(HERE / "lbm_oracle.c"), "-lm"], check=True)
+        tmp.replace(LIB)
+    return LIB
+
+
+class OrcParams(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in ("s1", "s2", "s4", "s9", "s10", "s13", "s16",
+                                               "omegepsl", "omegepslj", "omegxx")] + \
+               [("force", ctypes.c_double * 3)]
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(str(LIB))
+        dp = ctypes.POINTER(ctypes.c_double)
+        pp = ctypes.POINTER(OrcParams)
+        i = ctypes.c_int
+        sig = {
+            "orc_collide_node": (None, [pp, dp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_double, dp]),
+            "orc_force_moments": (None, [pp, ctypes.c_double, ctypes.c_double, ctypes.c_double, dp]),
+            "orc_moment_row": (None, [i, ctypes.POINTER(ctypes.c_int), dp]),
+            "orc_macrovar": (None, [pp, dp, i, i, i, dp, dp, dp, dp]),
+            "orc_initpop": (None, [i, i, i, dp, dp, dp, dp]),
+            "orc_rhoupdat": (None, [dp, i, i, i, dp]),
+            "orc_step_swap": (i, [pp, dp, i, i, i, dp, dp, dp, dp]),
+            "orc_step_push": (None, [pp, dp, dp, i, i, i, dp, dp, dp, dp]),
+            "orc_run": (i, [pp, dp, i, i, i, i, i, dp, dp, dp, dp]),
+            "orc_prerelax": (i, [pp, dp, i, i, i, dp, dp, dp, ctypes.c_double, i, ctypes.POINTER(i), dp]),
+            "orc_run_omp": (i, [pp, dp, i, i, i, i, i]),
+            "orc_max_threads": (i, []),
+            "orc_profiles": (None, [dp, dp, dp, dp, i, i, i, dp]),
+            "orc_channel_velocity": (None, [i, i, i, ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
+                                            dp, dp, dp]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def params(rates: dict, force=(0.0, 0.0, 0.0)) -> OrcParams:
+    p = OrcParams()
+    for k in ("s1", "s2", "s4", "s9", "s10", "s13", "s16", "omegepsl", "omegepslj", "omegxx"):
+        setattr(p, k, rates[k])
+    p.force[:] = list(force)
+    return p
+
+
+def params_from(run) -> OrcParams:
+    """Oracle parameters from a package RunParams."""
+    return params(run.rates(), (0.0, run.force_y, 0.0))
+
+
+def fields(shape):
+    return [np.zeros(shape, dtype=np.float64, order="F") for _ in range(4)]
+
+
+def collide_node(p: OrcParams, f, rho, ux, uy, uz) -> np.ndarray:
+    f = np.ascontiguousarray(f, dtype=np.float64)
+    out = np.empty(Q)
+    lib().orc_collide_node(ctypes.byref(p), _p(f), rho, ux, uy, uz, _p(out))
+    return out
+
+
+def force_moments(p: OrcParams, ux, uy, uz) -> np.ndarray:
+    out = np.empty(Q)
+    lib().orc_force_moments(ctypes.byref(p), ux, uy, uz, _p(out))
+    return out
+
+
+def moment_matrix() -> tuple[np.ndarray, np.ndarray]:
+    M = np.zeros((Q, Q), dtype=np.int64)
+    d = np.zeros(Q)
+    row = (ctypes.c_int * Q)()
+    n2 = ctypes.c_double()
+    for k in range(Q):
+        lib().orc_moment_row(k, row, ctypes.byref(n2))
+        M[k] = list(row)
+        d[k] = n2.value
+    return M, d
+
+
+def macrovar(p: OrcParams, f: np.ndarray):
+    _, nx, ny, nz = f.shape
+    out = fields((nx, ny, nz))
+    lib().orc_macrovar(ctypes.byref(p), _p(f), nx, ny, nz, *map(_p, out))
+    return tuple(out)
+
+
+def initpop(ux, uy, uz) -> np.ndarray:
+    nx, ny, nz = ux.shape
+    f = np.empty((Q, nx, ny, nz), dtype=np.float64, order="F")
+    a, b, c = (np.asfortranarray(v, dtype=np.float64) for v in (ux, uy, uz))
+    lib().orc_initpop(nx, ny, nz, _p(a), _p(b), _p(c), _p(f))
+    return f
+
+
+def run(p: OrcParams, f: np.ndarray, nsteps: int, mode: int = 0):
+    """main.f90:136-161 on a copy of f; returns (f, rho, ux, uy, uz)."""
+    f = np.array(f, dtype=np.float64, order="F", copy=True)
+    _, nx, ny, nz = f.shape
+    out = fields((nx, ny, nz))
+    rc = lib().orc_run(ctypes.byref(p), _p(f), nx, ny, nz, nsteps, mode, *map(_p, out))
+    if rc != 0:
+        raise RuntimeError("oracle run failed")
+    return (f, *out)
+
+
+def step_swap(p: OrcParams, f: np.ndarray, rho, ux, uy, uz) -> np.ndarray:
+    f = np.array(f, dtype=np.float64, order="F", copy=True)
+    _, nx, ny, nz = f.shape
+    m = [np.asfortranarray(v, dtype=np.float64) for v in (rho, ux, uy, uz)]
+    if lib().orc_step_swap(ctypes.byref(p), _p(f), nx, ny, nz, *map(_p, m)) != 0:
+        raise RuntimeError("oracle swap failed")
+    return f
+
+
+def step_push(p: OrcParams, f: np.ndarray, rho, ux, uy, uz) -> np.ndarray:
+    f = np.asfortranarray(f, dtype=np.float64)
+    _, nx, ny, nz = f.shape
+    g = np.empty_like(f, order="F")
+    m = [np.asfortranarray(v, dtype=np.float64) for v in (rho, ux, uy, uz)]
+    lib().orc_step_push(ctypes.byref(p), _p(f), _p(g), nx, ny, nz, *map(_p, m))
+    return g
+
+
+def prerelax(p: OrcParams, f: np.ndarray, ux, uy, uz, eps=1e-5, maxit=15000):
+    f = np.array(f, dtype=np.float64, order="F", copy=True)
+    _, nx, ny, nz = f.shape
+    it = ctypes.c_int()
+    err = ctypes.c_double()
+    a, b, c = (np.asfortranarray(v, dtype=np.float64) for v in (ux, uy, uz))
+    rc = lib().orc_prerelax(ctypes.byref(p), _p(f), nx, ny, nz, _p(a), _p(b), _p(c), eps, maxit,
+                            ctypes.byref(it), ctypes.byref(err))
+    if rc < 0:
+        raise RuntimeError("oracle prerelax failed")
+    return f, it.value, err.value, rc
+
+
+def run_omp(p: OrcParams, f: np.ndarray, nsteps: int, nthreads: int) -> np.ndarray:
+    _, nx, ny, nz = f.shape
+    if lib().orc_run_omp(ctypes.byref(p), _p(f), nx, ny, nz, nsteps, nthreads) != 0:
+        raise RuntimeError("oracle omp run failed")
+    return f
+
+
+def max_threads() -> int:
+    return lib().orc_max_threads()
+
+
+def profiles(rho, ux, uy, uz) -> np.ndarray:
+    nx, ny, nz = rho.shape
+    out = np.empty((nx, 12))
+    m = [np.asfortranarray(v, dtype=np.float64) for v in (rho, ux, uy, uz)]
+    lib().orc_profiles(*map(_p, m), nx, ny, nz, _p(out))
+    return out
+
+
+def channel_velocity(nx, ny, nz, uc, amp, seed):
+    out = [np.empty((nx, ny, nz), dtype=np.float64, order="F") for _ in range(3)]
+    lib().orc_channel_velocity(nx, ny, nz, uc, amp, ctypes.c_uint64(seed), *map(_p, out))
+    return tuple(out)
+
+
+def poiseuille_transient(nx: int, ustar: float, visc: float, istep: int, nterms: int = 26) -> np.ndarray:
+    """Analytic laminar start-up profile u(x)/ustar at the nodes of the lower
+    half, the series outputuy writes (saveload.f90:921-933)."""
+    time1 = istep * visc / (nx / 2.0) ** 2
+    i = np.arange(1, nx // 2 + 1)
+    xx0 = np.abs(i - 0.5 - nx / 2.0)
+    s = np.zeros_like(xx0)
+    for n in range(nterms):
+        s += (4 * (-1) ** n) / (np.pi * (n + 0.5)) ** 3 * np.exp(-((n + 0.5) ** 2) * np.pi**2 * time1) * \
+            np.cos((n + 0.5) * np.pi * (xx0 / (nx / 2.0)))
+    return (1 - (xx0 / (nx / 2.0)) ** 2) - s

@@ -1,0 +1,93 @@
+"""CPU checks of the C ABI library: it loads, exports every symbol the header
+declares, and its host-only entry points (parameter setup, initial-condition
+generator, argument validation) behave like the reference's para.f90 and the
+oracle.  No call here launches GPU work."""
+from __future__ import annotations
+
+import ctypes
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+HEADER = Path(__file__).resolve().parents[1] / "include" / "lbm_gb300.h"
+
+
+def declared_functions() -> list[str]:
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(lbm_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(lib, pkg):
+    names = declared_functions()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(lib, n), n
+    assert sorted(pkg.EXPORTS) == names
+
+
+def test_library_is_built_for_sm103a(pkg):
+    data = pkg.library_path().read_bytes()
+    assert b"sm_103a" in data
+
+
+def test_params_init_matches_para(lib, pkg):
+    for mrt in (1, 2, 3):
+        run = pkg.RunParams(nx=64, ny=128, nz=64, visc=0.0012, force_y=3.8e-7, mrt_type=mrt)
+        c = run.to_c()
+        r = run.rates()
+        for k, v in r.items():
+            assert getattr(c, k) == pytest.approx(v, rel=1e-15), (mrt, k)
+        assert list(c.force) == [0.0, 3.8e-7, 0.0]
+        assert c.fp16_scale == 32768.0
+
+
+def test_params_init_rejects_bad_arguments(lib, pkg):
+    p = pkg.LBMParams()
+    assert lib.lbm_params_init(ctypes.byref(p), 0, 4, 4, 1, 0.01, 0.0, 0) == -1
+    assert lib.lbm_params_init(ctypes.byref(p), 4, 4, 4, 7, 0.01, 0.0, 0) == -1
+    assert lib.lbm_params_init(ctypes.byref(p), 4, 4, 4, 1, -1.0, 0.0, 0) == -1
+    assert lib.lbm_params_init(ctypes.byref(p), 4, 4, 4, 1, 0.01, 0.0, 5) == -1
+    assert b"MRT" in lib.lbm_last_error() or b"precision" in lib.lbm_last_error()
+    assert lib.lbm_params_init(None, 4, 4, 4, 1, 0.01, 0.0, 0) == -1
+
+
+def test_create_rejects_bad_params_before_touching_a_device(lib, pkg):
+    p = pkg.LBMParams()
+    assert lib.lbm_params_init(ctypes.byref(p), 4, 4, 4, 1, 0.01, 0.0, 0) == 0
+    ctx = ctypes.c_void_p()
+    p.nx = -3
+    assert lib.lbm_create(ctypes.byref(p), ctypes.byref(ctx)) == -1
+    assert not ctx.value
+    p.nx = 4
+    p.s9 = float("nan")
+    assert lib.lbm_create(ctypes.byref(p), ctypes.byref(ctx)) == -1
+    assert lib.lbm_create(None, ctypes.byref(ctx)) == -1
+    assert lib.lbm_destroy(None) == 0
+    assert lib.lbm_step(None, 1) == -1
+
+
+def test_strerror_covers_codes(lib):
+    for code in range(0, -9, -1):
+        assert lib.lbm_strerror(code)
+    assert lib.lbm_strerror(-99) == b"unknown error"
+
+
+def test_channel_velocity_host_copy_matches_oracle(pkg, orc):
+    for shape, seed in (((6, 5, 4), 1), ((16, 8, 4), 20240611)):
+        a = pkg.channel_velocity(*shape, 0.05, 0.05, seed)
+        b = orc.channel_velocity(*shape, 0.05, 0.05, seed)
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)
+
+
+def test_channel_configs(pkg):
+    c0 = pkg.CHANNEL_CONFIGS["c0"]
+    assert (c0.wall, c0.stream, c0.span) == (64, 128, 64)
+    assert c0.force == pytest.approx(0.0035**2 / 32)
+    p = c0.params()
+    assert (p.nx, p.ny, p.nz) == (64, 128, 64)
+    c4 = pkg.CHANNEL_CONFIGS["c4"]
+    assert c4.nodes == 1024 * 512 * 512 and c4.precision == "fp16"

@@ -1,0 +1,275 @@
+"""GPU parity: the sm_103a kernels, called through the C ABI, against the FP64
+oracle and the committed golden fixtures.
+
+Tolerances
+  FP64 storage + arithmetic: relative L-infinity <= 1e-10 in f, rho and u after
+    100 steps (the spec bar); the kernels reorder the same FP64
+    arithmetic, so the observed gap is ~1e-14.
+  FP32 and FP16 storage (FP32 arithmetic): checked against FP64 through the
+    mean profile and bounded population errors, see test_precision_*.
+"""
+from __future__ import annotations
+
+import os
+import tempfile
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = Path(__file__).resolve().parent / "golden" / "channel_6x10x4.npz"
+
+
+def rel_linf(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def stable_run(pkg, shape, force_y=3.8e-7, precision="fp64", visc=0.0012, mrt=1):
+    nx, ny, nz = shape
+    return pkg.RunParams(nx=nx, ny=ny, nz=nz, visc=visc, force_y=force_y, mrt_type=mrt,
+                         precision=pkg.PRECISIONS[precision])
+
+
+def random_state(orc, shape, seed, amp=1e-4):
+    u = orc.channel_velocity(*shape, 0.05, 0.05, seed)
+    f = orc.initpop(*u)
+    rng = np.random.default_rng(seed)
+    return np.asfortranarray(f + amp * rng.standard_normal(f.shape))
+
+
+def test_upload_download_roundtrip(pkg, orc):
+    shape = (6, 33, 5)
+    f = random_state(orc, shape, 1)
+    for prec, tol in (("fp64", 0.0), ("fp32", 6e-8), ("fp16", 5e-4)):
+        with pkg.Lattice(stable_run(pkg, shape, precision=prec)) as lat:
+            lat.upload_f(f)
+            g = lat.download_f()
+            err = np.abs(g - f)
+            assert (err <= tol * np.abs(f) + 1e-12 * (prec == "fp16")).all(), prec
+
+
+def test_device_initial_condition_is_bitwise_oracle_initpop(pkg, orc):
+    shape = (8, 40, 6)
+    with pkg.Lattice(stable_run(pkg, shape)) as lat:
+        lat.init_channel(0.05, 0.05, 77)
+        g = lat.download_f()
+        u = orc.channel_velocity(*shape, 0.05, 0.05, 77)
+        assert np.array_equal(g, orc.initpop(*u))
+        # host-array initpop gives the same bits too
+        lat.initpop(*u)
+        assert np.array_equal(lat.download_f(), g)
+
+
+@pytest.mark.parametrize("nsteps", [1, 2, 3, 8])
+def test_steps_match_oracle_fp64(pkg, orc, nsteps):
+    shape = (6, 12, 5)
+    run = stable_run(pkg, shape, force_y=2e-5)
+    f = random_state(orc, shape, 10 + nsteps)
+    fo, rho, ux, uy, uz = orc.run(orc.params_from(run), f, nsteps, mode=0)
+    with pkg.Lattice(run) as lat:
+        lat.upload_f(f)
+        lat.step(nsteps)
+        g = lat.download_f()
+        m = lat.macrovar()
+    assert rel_linf(g, fo) < 1e-13
+    for a, b in zip(m, (rho, ux, uy, uz)):
+        assert rel_linf(a, b) < 1e-12
+
+
+@pytest.mark.parametrize("shape", [(1, 4, 3), (2, 5, 1), (3, 1, 2), (7, 9, 11)])
+def test_odd_shapes_match_oracle(pkg, orc, shape):
+    run = stable_run(pkg, shape, force_y=1e-5)
+    f = random_state(orc, shape, 3)
+    fo = orc.run(orc.params_from(run), f, 5, mode=0)[0]
+    with pkg.Lattice(run) as lat:
+        lat.upload_f(f)
+        lat.step(5)
+        assert rel_linf(lat.download_f(), fo) < 1e-13
+
+
+def test_golden_fixture(pkg):
+    g = np.load(GOLDEN)
+    nx, ny, nz = (int(v) for v in g["shape"])
+    run = pkg.RunParams(nx=nx, ny=ny, nz=nz, visc=float(g["visc"]), force_y=float(g["force"][1]), mrt_type=1)
+    with pkg.Lattice(run) as lat:
+        lat.upload_f(g["f0"])
+        done = 0
+        for n in g["steps"]:
+            lat.step(int(n) - done)
+            done = int(n)
+            assert rel_linf(lat.download_f(), g[f"f{n}"]) < 1e-13
+            m = np.stack(lat.macrovar())
+            assert rel_linf(m, g[f"macro{n}"]) < 1e-12
+
+
+def test_config0_fp64_parity_100_steps(pkg, orc):
+    """Plain turbulent channel 128 x 64 x 64 (c0), seeded Poiseuille + 5 %
+    noise, 100 steps: relative L-inf <= 1e-10 in f, rho and u."""
+    c0 = pkg.CHANNEL_CONFIGS["c0"]
+    run = c0.params("fp64")
+    shape = (run.nx, run.ny, run.nz)
+    u = orc.channel_velocity(*shape, c0.uc, c0.amp, c0.seed)
+    f0 = orc.initpop(*u)
+    p = orc.params_from(run)
+    fo = orc.run_omp(p, np.array(f0, order="F", copy=True), 100, orc.max_threads())
+    rho, ux, uy, uz = orc.macrovar(p, fo)
+    with pkg.Lattice(run) as lat:
+        lat.init_channel(c0.uc, c0.amp, c0.seed)
+        assert np.array_equal(lat.download_f(), f0)
+        lat.step(100)
+        g = lat.download_f()
+        m = lat.macrovar()
+        prof = lat.profiles()
+    errs = [rel_linf(g, fo)] + [rel_linf(a, b) for a, b in zip(m, (rho, ux, uy, uz))]
+    assert max(errs) <= 1e-10, errs
+    np.testing.assert_allclose(prof, orc.profiles(rho, ux, uy, uz), rtol=1e-9, atol=1e-13)
+
+
+def test_prerelax_matches_oracle(pkg, orc):
+    shape = (8, 16, 6)
+    run = stable_run(pkg, shape)
+    u = orc.channel_velocity(*shape, 0.05, 0.05, 5)
+    f = orc.initpop(*u)
+    f[0] += 1e-3 * np.random.default_rng(2).standard_normal(f.shape[1:])
+    fo, it, err, rc = orc.prerelax(orc.params_from(run), f, *u, eps=1e-6, maxit=5000)
+    with pkg.Lattice(run) as lat:
+        lat.upload_f(f)
+        it2, err2 = lat.prerelax(*u, eps=1e-6, maxit=5000)
+        assert it2 == it
+        assert err2 == pytest.approx(err, rel=1e-6, abs=1e-15)
+        assert rel_linf(lat.download_f(), fo) < 1e-12
+
+
+def test_prerelax_limit_reports_not_converged(pkg, orc):
+    shape = (4, 8, 4)
+    run = stable_run(pkg, shape)
+    u = orc.channel_velocity(*shape, 0.05, 0.05, 5)
+    f = orc.initpop(*u)
+    f[0] += 1e-2
+    with pkg.Lattice(run) as lat:
+        lat.upload_f(f)
+        with pytest.raises(pkg.LBMError) as e:
+            lat.prerelax(*u, eps=1e-14, maxit=3)
+        assert e.value.code == -5
+
+
+def test_poiseuille_startup_on_gpu(pkg, orc):
+    nx = 20
+    run = pkg.para(nx, 4, 4, laminar=True)
+    z = np.zeros((nx, 4, 4), order="F")
+    with pkg.Lattice(run) as lat:
+        lat.initpop(z, z, z)
+        lat.step(120)
+        rho, ux, uy, uz = lat.macrovar()
+    ana = orc.poiseuille_transient(nx, run.ustar, run.visc, 120)
+    assert np.abs(uy[: nx // 2, 1, 1] / run.ustar - ana).max() < 5e-3
+
+
+def test_diag_and_mass_conservation(pkg, orc):
+    c0 = pkg.CHANNEL_CONFIGS["c0"]
+    run = c0.params("fp64")
+    with pkg.Lattice(run) as lat:
+        lat.init_channel(c0.uc, c0.amp, c0.seed)
+        st0 = lat.diag()
+        lat.step(200)
+        st = lat.diag()
+        rho, ux, uy, uz = lat.macrovar()
+    assert st.nfluid == c0.nodes and st.nonfinite == 0
+    assert abs(st.rho_sum - st0.rho_sum) < 1e-9
+    assert st.rho_max == pytest.approx(rho.max(), rel=1e-12)
+    assert st.rho_min == pytest.approx(rho.min(), rel=1e-12)
+    v = np.sqrt(ux**2 + uy**2 + uz**2)
+    assert st.vmax == pytest.approx(v.max(), rel=1e-12)
+    ix, iy, iz = np.unravel_index(np.argmax(v, axis=None), v.shape, order="F")
+    assert tuple(st.vmax_at) == (ix + 1, iy + 1, iz + 1)
+    assert st.mom_sum[1] == pytest.approx(uy.sum(), rel=1e-10)
+
+
+def read_fortran_records(path):
+    """Parse a gfortran-style unformatted sequential file into records."""
+    data = Path(path).read_bytes()
+    recs, pos = [], 0
+    while pos < len(data):
+        chunks = []
+        while True:
+            n = int(np.frombuffer(data, np.int32, 1, pos)[0])
+            pos += 4
+            chunks.append(data[pos:pos + abs(n)])
+            pos += abs(n)
+            pos += 4
+            if n >= 0:
+                break
+        recs.append(b"".join(chunks))
+    return recs
+
+
+def test_checkpoint_files_in_reference_format(pkg, orc):
+    shape = (6, 12, 5)
+    run = stable_run(pkg, shape)
+    f = random_state(orc, shape, 9)
+    with tempfile.TemporaryDirectory() as d, pkg.Lattice(run) as lat:
+        lat.upload_f(f)
+        lat.step(3)                                  # odd step count: swapped AA state
+        want = lat.download_f()
+        p0 = os.path.join(d, "finit.000")
+        p1 = os.path.join(d, "endrunflow2D16x8.0000003.000")
+        lat.save_flow(p0, 0, [7])
+        lat.save_flow(p1, 1, [3, 1, 0])
+        r0 = read_fortran_records(p0)
+        assert len(r0) == 2 and np.frombuffer(r0[0], np.int32).tolist() == [7]
+        assert np.array_equal(np.frombuffer(r0[1], np.float64), want.ravel(order="F"))
+        r1 = read_fortran_records(p1)
+        assert np.frombuffer(r1[0], np.int32).tolist() == [3, 1, 0]
+        lat.step(2)
+        assert lat.load_flow(p1, 1) == [3, 1, 0]
+        assert np.array_equal(lat.download_f(), want)
+        # continuing from the file equals continuing without it
+        lat.step(4)
+        a = lat.download_f()
+        lat.upload_f(want)
+        lat.step(4)
+        assert np.array_equal(lat.download_f(), a)
+        # corrupt / wrong-size files are rejected with LBM_ERR_IO
+        bad = os.path.join(d, "bad")
+        Path(bad).write_bytes(Path(p0).read_bytes()[:-100])
+        with pytest.raises(pkg.LBMError) as e:
+            lat.load_flow(bad, 0)
+        assert e.value.code == -6
+        with pytest.raises(pkg.LBMError):
+            lat.load_flow(os.path.join(d, "missing"), 0)
+        with pytest.raises(pkg.LBMError):
+            lat.load_flow(p1, 0)                     # header holds 3 integers, not 1
+
+
+def test_precision_variants_against_fp64(pkg):
+    """FP32 and FP16-storage runs of the c0 channel against FP64 after 300
+    steps: mean streamwise profile within 1 % and bounded population error."""
+    c0 = pkg.CHANNEL_CONFIGS["c0"]
+    res = {}
+    for prec in ("fp64", "fp32", "fp16"):
+        with pkg.Lattice(c0.params(prec)) as lat:
+            lat.init_channel(c0.uc, c0.amp, c0.seed)
+            lat.step(300)
+            res[prec] = (lat.profiles(), lat.download_f(), lat.diag())
+    ref = pkg.statistics(res["fp64"][0], c0.ustar)
+    for prec, tol_f in (("fp32", 1e-5), ("fp16", 2e-2)):
+        st = pkg.statistics(res[prec][0], c0.ustar)
+        err_mean = np.abs(st["mean"][:, 1] - ref["mean"][:, 1]).max() / np.abs(ref["mean"][:, 1]).max()
+        assert err_mean < 1e-2, (prec, err_mean)
+        assert rel_linf(res[prec][1], res["fp64"][1]) < tol_f, prec
+        assert res[prec][2].nonfinite == 0
+
+
+def test_avedensity_removes_mean(pkg, orc):
+    shape = (6, 12, 5)
+    run = stable_run(pkg, shape)
+    f = random_state(orc, shape, 4)
+    f[0] += 3e-4
+    with pkg.Lattice(run) as lat:
+        lat.upload_f(f)
+        lat.step(1)
+        m = lat.avedensity()
+        assert m == pytest.approx(3e-4, rel=0.2)
+        assert abs(lat.diag().rho_sum) < 1e-12
