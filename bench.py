@@ -406,12 +406,21 @@ def main():
     ap.add_argument("--precision", choices=tuple(BYTES), default=None)
     ap.add_argument("--accuracy-steps", type=int, default=100)
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU work for the CPU baseline")
+    ap.add_argument("--grid", type=int, nargs=3, metavar=("STREAM", "SPAN", "WALL"), default=None,
+                    help="override the lattice (streamwise spanwise wall-normal), e.g. for a small ncu capture")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
     world, rank, local = dist_setup()
+    if args.grid:
+        import dataclasses
+        pkg = importlib.import_module(PKG)
+        c = pkg.CHANNEL_CONFIGS[args.config]
+        pkg.CHANNEL_CONFIGS[args.config] = dataclasses.replace(
+            c, stream=args.grid[0], span=args.grid[1], wall=args.grid[2], h=args.grid[2] / 2,
+            name=f"{c.name}@{args.grid[0]}x{args.grid[1]}x{args.grid[2]}")
     if args.impl == "reference":
         run_reference(args, world, rank)
     else:

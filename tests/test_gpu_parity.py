@@ -182,7 +182,7 @@ def test_diag_and_mass_conservation(pkg, orc):
     assert st.rho_min == pytest.approx(rho.min(), rel=1e-12)
     v = np.sqrt(ux**2 + uy**2 + uz**2)
     assert st.vmax == pytest.approx(v.max(), rel=1e-12)
-    ix, iy, iz = np.unravel_index(np.argmax(v, axis=None), v.shape, order="F")
+    ix, iy, iz = np.unravel_index(np.argmax(v.ravel(order="F")), v.shape, order="F")
     assert tuple(st.vmax_at) == (ix + 1, iy + 1, iz + 1)
     assert st.mom_sum[1] == pytest.approx(uy.sum(), rel=1e-10)
 
