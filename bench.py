@@ -253,7 +253,7 @@ def run_gpu(args, world, rank, local):
     prec = args.precision or cfg.precision
     N = cfg.nodes
     bpn = 38 * BYTES[prec]
-    run = cfg.params(prec, device=local)
+    run = cfg.params(prec, device=local, flags=pkg.FLAG_SIMPLE_STEP if args.simple else 0)
     torch.cuda.set_device(local)
     lat = pkg.Lattice(run)
     lat.init_channel(cfg.uc, cfg.amp, cfg.seed)
@@ -408,6 +408,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU work for the CPU baseline")
     ap.add_argument("--grid", type=int, nargs=3, metavar=("STREAM", "SPAN", "WALL"), default=None,
                     help="override the lattice (streamwise spanwise wall-normal), e.g. for a small ncu capture")
+    ap.add_argument("--simple", action="store_true", help="one-node-per-thread step kernels (A/B reference)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

@@ -37,6 +37,7 @@ PREC_FP64, PREC_FP32, PREC_FP16 = 0, 1, 2
 PRECISIONS = {"fp64": PREC_FP64, "fp32": PREC_FP32, "fp16": PREC_FP16}
 MRT_STABLE, MRT_LBGK, MRT_LOWDISS = 1, 2, 3
 PROFILE_COLS = 12
+FLAG_SIMPLE_STEP = 1
 PROFILE_NAMES = ("ux", "uy", "uz", "uxuz", "uxuy", "uyuz", "uxux", "uyuy", "uzuz", "rho", "rhorho", "count")
 
 # Every symbol include/lbm_gb300.h declares.
@@ -67,7 +68,7 @@ class LBMParams(ctypes.Structure):
         ("omegepsl", ctypes.c_double), ("omegepslj", ctypes.c_double), ("omegxx", ctypes.c_double),
         ("force", ctypes.c_double * 3),
         ("fp16_scale", ctypes.c_double),
-        ("device", ctypes.c_int32), ("reserved", ctypes.c_int32),
+        ("device", ctypes.c_int32), ("flags", ctypes.c_int32),
     ]
 
 
@@ -166,6 +167,7 @@ class RunParams:
     precision: int = PREC_FP64
     fp16_scale: float = 32768.0
     device: int = 0
+    flags: int = 0
     extra: dict = field(default_factory=dict)
 
     def to_c(self) -> LBMParams:
@@ -175,6 +177,7 @@ class RunParams:
                                         self.visc, self.force_y, self.precision), "lbm_params_init")
         p.fp16_scale = self.fp16_scale
         p.device = self.device
+        p.flags = self.flags
         return p
 
     def rates(self) -> dict:

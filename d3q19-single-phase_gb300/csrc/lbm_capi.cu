@@ -28,6 +28,7 @@ struct lbm_ctx {
     double* d_uf = nullptr;    // frozen velocity for pre-relaxation (GPU layout)
     double* d_rho = nullptr;   // pre-relaxation density
     unsigned long long* d_max = nullptr;
+    int* d_err = nullptr;      // set by a kernel whose bounded wait gave up
 };
 
 namespace {
@@ -120,6 +121,14 @@ int ensure_red(lbm_ctx* c, size_t elems) {
 
 int sync(lbm_ctx* c) {
     CK(cudaStreamSynchronize(c->stream));
+    if (c->d_err) {
+        int flag = 0;
+        CK(cudaMemcpy(&flag, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+        if (flag) {
+            cudaMemset(c->d_err, 0, sizeof(int));
+            return fail(LBM_ERR_CUDA, "a step kernel's bulk-copy wait timed out; populations are invalid");
+        }
+    }
     return LBM_OK;
 }
 
@@ -310,6 +319,12 @@ int lbm_create(const lbm_params* p, lbm_ctx** out) {
     }
     s.cd = make_consts<double>(c->p, S);
     s.cf = make_consts<float>(c->p, S);
+    cudaDeviceGetAttribute(&s.sm_count, cudaDevAttrMultiProcessorCount, p->device);
+    s.use_rows = !(p->flags & LBM_FLAG_SIMPLE_STEP) && rows_supported(s);
+    if (s.use_rows && prepare_step_rows() != cudaSuccess) s.use_rows = 0;
+    e = cudaMalloc(&c->d_err, sizeof(int));
+    if (e != cudaSuccess) { lbm_destroy(c); return cuda_fail(e, "cudaMalloc(error flag)"); }
+    cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
     // staging: up to 256 MB, at least one reference z plane of AoS populations
     const size_t want = std::max<size_t>(plane_nodes(*p) * Q, (size_t)32 << 20);
     const size_t stage = std::min<size_t>(want, std::max<size_t>(plane_nodes(*p) * Q, s.N * Q));
@@ -332,6 +347,7 @@ int lbm_destroy(lbm_ctx* c) {
     cudaFree(c->d_uf);
     cudaFree(c->d_rho);
     cudaFree(c->d_max);
+    cudaFree(c->d_err);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return LBM_OK;
@@ -416,7 +432,8 @@ int lbm_step_async(lbm_ctx* c, int32_t nsteps) {
     if (check_ctx(c)) return LBM_ERR_INVALID_ARG;
     if (nsteps < 0) return fail(LBM_ERR_INVALID_ARG, "negative step count");
     for (int32_t k = 0; k < nsteps; ++k) {
-        CK(launch_step(c->s, c->parity, c->stream));
+        if (c->s.use_rows) CK(launch_step_rows(c->s, c->parity, c->d_err, c->stream));
+        else CK(launch_step(c->s, c->parity, c->stream));
         c->parity ^= 1;
         ++c->nsteps;
     }

@@ -44,6 +44,8 @@ struct DeviceState {
     void* f;             // 19 * pstride elements of the storage type
     CollideConsts<double> cd;
     CollideConsts<float> cf;
+    int sm_count;        // SMs of the device (persistent grids)
+    int use_rows;        // 1: row-pipelined bulk-copy kernels for the step
 };
 
 // launchers (lbm_step.cu)
@@ -51,6 +53,11 @@ cudaError_t launch_step(const DeviceState& s, int parity, cudaStream_t st);
 cudaError_t launch_prerelax(const DeviceState& s, int parity, const double* uf,
                             double* rho_prev_and_new, unsigned long long* maxabs,
                             cudaStream_t st);
+
+// row-pipelined bulk-copy step (lbm_step_tma.cu), FP32/FP16 storage
+bool rows_supported(const DeviceState& s);
+cudaError_t prepare_step_rows();
+cudaError_t launch_step_rows(const DeviceState& s, int parity, int* err, cudaStream_t st);
 
 // field kernels (lbm_fields.cu)
 // AoS FP64 chunk (reference layout, ref z planes [z0, z0+nzc)) <-> storage.

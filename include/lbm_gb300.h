@@ -89,8 +89,12 @@ typedef struct lbm_params {
     double  force[3];         /* uniform body force (force_realx/y/z)          */
     double  fp16_scale;       /* fixed FP16 storage scale (0 -> 32768)         */
     int32_t device;           /* CUDA device ordinal                           */
-    int32_t reserved;
+    int32_t flags;            /* LBM_FLAG_* bits                               */
 } lbm_params;
+
+/* lbm_params.flags: use the one-node-per-thread step kernels even where the
+ * row-pipelined bulk-copy kernels apply (FP32/FP16 storage, 16-byte rows). */
+#define LBM_FLAG_SIMPLE_STEP 1
 
 /* Global diagnostics over fluid nodes (diag, saveload.f90:1507-1676, plus the
  * mass and momentum sums of avedensity, collision.f90:487-513).  Velocities

@@ -273,3 +273,51 @@ def test_avedensity_removes_mean(pkg, orc):
         m = lat.avedensity()
         assert m == pytest.approx(3e-4, rel=0.2)
         assert abs(lat.diag().rho_sum) < 1e-12
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp16"])
+@pytest.mark.parametrize("shape", [(5, 16, 3), (8, 64, 7), (3, 24, 1), (6, 32, 9)])
+def test_row_pipelined_kernels_match_simple_kernels(pkg, orc, prec, shape):
+    """The bulk-copy row kernels (FP32/FP16 storage, rows of 16-byte multiples)
+    against the one-node-per-thread kernels: same arithmetic per node, so the
+    populations agree to rounding of the storage type."""
+    f = random_state(orc, shape, 21)
+    out = {}
+    for flags in (0, pkg.FLAG_SIMPLE_STEP):
+        run = stable_run(pkg, shape, force_y=2e-5, precision=prec)
+        run.flags = flags
+        with pkg.Lattice(run) as lat:
+            lat.upload_f(f)
+            res = []
+            for n in (1, 1, 5):
+                lat.step(n)
+                res.append(lat.download_f())
+            out[flags] = res
+    ulp = 2.0**-23 if prec == "fp32" else 2.0**-10
+    for a, b in zip(out[0], out[pkg.FLAG_SIMPLE_STEP]):
+        assert np.abs(a - b).max() <= 4 * ulp * np.abs(b).max()
+    # and both follow the FP64 oracle within the storage precision
+    fo = orc.run(orc.params_from(stable_run(pkg, shape, force_y=2e-5)), f, 7, mode=0)[0]
+    assert rel_linf(out[0][-1], fo) < (1e-5 if prec == "fp32" else 5e-3)
+
+
+def test_row_kernels_full_size_config4_properties(pkg):
+    """1024 x 512 x 512 FP16 store (the large channel): no NaN, mass drift and
+    mean profile against the one-node-per-thread kernels after 20 steps."""
+    c4 = pkg.CHANNEL_CONFIGS["c4"]
+    res = {}
+    for flags in (0, pkg.FLAG_SIMPLE_STEP):
+        run = c4.params("fp16")
+        run.flags = flags
+        with pkg.Lattice(run) as lat:
+            lat.init_channel(c4.uc, c4.amp, c4.seed)
+            d0 = lat.diag()
+            lat.step(20)
+            d1 = lat.diag()
+            res[flags] = (lat.profiles(), d1, d1.rho_sum - d0.rho_sum)
+    a, b = res[0], res[pkg.FLAG_SIMPLE_STEP]
+    assert a[1].nonfinite == 0 and b[1].nonfinite == 0
+    ma = pkg.statistics(a[0], c4.ustar)["mean"][:, 1]
+    mb = pkg.statistics(b[0], c4.ustar)["mean"][:, 1]
+    assert np.abs(ma - mb).max() < 1e-4 * np.abs(mb).max()
+    assert abs(a[2]) < 1e-5 * c4.nodes and abs(b[2]) < 1e-5 * c4.nodes
