@@ -72,6 +72,8 @@ CollideConsts<R> make_consts(const lbm_params& p, double S) {
     c.kpi = (R)(p.s10 / 72.0);
     c.kxy = (R)(p.s13 / 4.0);
     c.km = (R)(p.s16 / 8.0);
+    c.kw = (R)(p.s9 / 12.0);
+    c.kwi = (R)(p.s10 / 24.0);
     c.oeps = (R)p.omegepsl; c.oepsj = (R)p.omegepslj; c.oxx = (R)p.omegxx;
     return c;
 }

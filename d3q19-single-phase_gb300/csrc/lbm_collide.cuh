@@ -34,6 +34,7 @@ struct CollideConsts {
     R fqx, fqy, fqz;        // -(2/3) S F / 40: forcing part of the q increment
     R thFx, thFy, thFz;     // S F / 3: turns j into the q-equilibrium offset
     R ke, keps, kq, kp, kpi, kxy, km;  // s_k / |row_k|^2
+    R kw, kwi;              // s9/12 and s10/24 (p_ww, pi_ww rows)
     R oeps, oepsj, oxx;     // omegepsl, omegepslj, omegxx
 };
 
@@ -113,8 +114,8 @@ __device__ __forceinline__ void collide(R f[Q], const CollideConsts<R>& c,
     const R a_qz = c.fqz - c.kq * (qz + R(2.0 / 3.0) * jz - c.thFz);
     const R a_p  = P * R(2.0 / 36.0) - c.kp * (p3 + P - eqp);
     const R a_pi = P * R(-1.0 / 72.0) - c.kpi * (pi3 - R(0.5) * P - c.oxx * eqp);
-    const R a_w  = Wf * R(2.0 / 12.0) - c.kp * R(3) * (pw + Wf - eqw);      // s9/12 = 3 s9/36
-    const R a_wi = Wf * R(-1.0 / 24.0) - c.kpi * R(3) * (piw - R(0.5) * Wf - c.oxx * eqw);  // s10/24 = 3 s10/72
+    const R a_w  = Wf * R(2.0 / 12.0) - c.kw * (pw + Wf - eqw);
+    const R a_wi = Wf * R(-1.0 / 24.0) - c.kwi * (piw - R(0.5) * Wf - c.oxx * eqw);
     const R a_xy = Qxy * R(0.25) - c.kxy * (pxy + R(0.5) * Qxy - jx * uy);
     const R a_yz = Qyz * R(0.25) - c.kxy * (pyz + R(0.5) * Qyz - jy * uz);
     const R a_xz = Qxz * R(0.25) - c.kxy * (pxz + R(0.5) * Qxz - jx * uz);
@@ -150,29 +151,27 @@ __device__ __forceinline__ void collide(R f[Q], const CollideConsts<R>& c,
     const R Eyy = bd - R(2) * ppi;
     const R gx = ajx + a_qx, gy = ajy + a_qy, gz = ajz + a_qz;
 
-    {   // 7 (+1,+1,0) / 10
-        const R E = Exy + a_xy, O = (gx + gy) + (a_mx - a_my);
-        f[7] += E + O;  f[10] += E - O;
+    // odd parts of the diagonal pairs share g +- a_m combinations
+    const R uxm = gx + a_mx, uxp = gx - a_mx;
+    const R uyp = gy - a_my, uym = gy + a_my;
+    const R uzm = gz + a_mz, uzp = gz - a_mz;
+    {   // 7 (+1,+1,0) / 10 and 8 (-1,+1,0) / 9
+        const R E7 = Exy + a_xy, O7 = uxm + uyp;
+        const R E8 = Exy - a_xy, O8 = uyp - uxm;
+        f[7] += E7 + O7;  f[10] += E7 - O7;
+        f[8] += E8 + O8;  f[9] += E8 - O8;
     }
-    {   // 8 (-1,+1,0) / 9
-        const R E = Exy - a_xy, O = (gy - gx) - (a_mx + a_my);
-        f[8] += E + O;  f[9] += E - O;
+    {   // 11 (+1,0,+1) / 14 and 12 (-1,0,+1) / 13
+        const R E11 = Exz + a_xz, O11 = uxp + uzm;
+        const R E12 = Exz - a_xz, O12 = uzm - uxp;
+        f[11] += E11 + O11; f[14] += E11 - O11;
+        f[12] += E12 + O12; f[13] += E12 - O12;
     }
-    {   // 11 (+1,0,+1) / 14
-        const R E = Exz + a_xz, O = (gx + gz) + (a_mz - a_mx);
-        f[11] += E + O; f[14] += E - O;
-    }
-    {   // 12 (-1,0,+1) / 13
-        const R E = Exz - a_xz, O = (gz - gx) + (a_mx + a_mz);
-        f[12] += E + O; f[13] += E - O;
-    }
-    {   // 15 (0,+1,+1) / 18
-        const R E = Eyy + a_yz, O = (gy + gz) + (a_my - a_mz);
-        f[15] += E + O; f[18] += E - O;
-    }
-    {   // 16 (0,-1,+1) / 17
-        const R E = Eyy - a_yz, O = (gz - gy) - (a_my + a_mz);
-        f[16] += E + O; f[17] += E - O;
+    {   // 15 (0,+1,+1) / 18 and 16 (0,-1,+1) / 17
+        const R E15 = Eyy + a_yz, O15 = uym + uzp;
+        const R E16 = Eyy - a_yz, O16 = uzp - uym;
+        f[15] += E15 + O15; f[18] += E15 - O15;
+        f[16] += E16 + O16; f[17] += E16 - O16;
     }
 }
 
