@@ -10,17 +10,19 @@
 // periodic x-shift of the odd step a modular index inside shared memory.
 //
 // Each persistent CTA owns one SM and a ring of NSTAGE stage buffers of 19
-// rows.  Thread 0 issues the 19 cp.async.bulk loads of an item into a stage
-// with one mbarrier (expect_tx = 19 rows); all threads wait on it (bounded)
-// and compute two adjacent nodes each.  Results go either
-//   SOUT = true : into one of two shared-memory output buffers (x-shift and
-//                 periodic wrap applied there) that thread 0 writes back with
-//                 19 bulk stores at the start of the next item, or
-//   SOUT = false: straight to HBM (aligned pairs as one 32/64-bit store,
-//                 x-shifted populations element-wise) when shared memory is
-//                 too small for output buffers (FP32 rows of 1024).
-// NSTAGE-1 items are always in flight, so the bytes in flight per SM are set
-// by shared memory, not by registers.
+// rows, each with an mbarrier that completes when its 19 bulk copies have
+// landed (expect_tx = 19 rows).  There is no CTA-wide barrier in the steady
+// state: every warp computes its share of an item (two adjacent nodes per
+// thread, results stored straight to HBM: aligned pairs as one 32/64-bit
+// store, x-shifted populations element-wise), then counts itself done on the
+// stage's counter; the last warp to finish a stage refills it with the item
+// NSTAGE ahead (lane i copies population i).  Warps therefore drift freely up
+// to NSTAGE-1 items apart, and NSTAGE-1 items are in flight per SM, so the
+// bytes in flight are set by shared memory, not by registers.
+//
+// Every mbarrier wait is bounded; a wait that gives up sets the error flag
+// and the warp carries on with whatever the buffer holds, so the kernel always
+// terminates and the host reports the step as failed.
 #include <algorithm>
 
 #include "lbm_internal.h"
@@ -45,16 +47,6 @@ __device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_
         "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
         "l"(src), "r"(bytes), "r"(bar)
         : "memory");
-}
-__device__ __forceinline__ void bulk_store(void* dst, uint32_t src, uint32_t bytes) {
-    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(src), "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
-__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
-__device__ __forceinline__ void fence_proxy_async_smem() {
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
     uint32_t ok;
@@ -91,6 +83,33 @@ __device__ __forceinline__ void st_pair(float* p, float a, float b) {
 __device__ __forceinline__ void st_one(__half* p, float a) { *p = __float2half_rn(a); }
 __device__ __forceinline__ void st_one(float* p, float a) { *p = a; }
 
+// Lattice lookups with a runtime population index (one lane per population
+// when issuing bulk copies): values packed into 64-bit words at compile time.
+constexpr uint64_t pack2(int (*f)(int)) {
+    uint64_t w = 0;
+    for (int i = 0; i < Q; ++i) w |= (uint64_t)(f(i) + 1) << (2 * i);
+    return w;
+}
+constexpr int dy_c(int i) { return DYg(i); }
+constexpr int dz_c(int i) { return DZg(i); }
+constexpr uint64_t kDY = pack2(dy_c), kDZ = pack2(dz_c);
+constexpr uint64_t pack_opp_lo() {
+    uint64_t w = 0;
+    for (int i = 0; i < 12; ++i) w |= (uint64_t)OPPf(i) << (5 * i);
+    return w;
+}
+constexpr uint64_t pack_opp_hi() {
+    uint64_t w = 0;
+    for (int i = 12; i < Q; ++i) w |= (uint64_t)OPPf(i) << (5 * (i - 12));
+    return w;
+}
+constexpr uint64_t kOPPlo = pack_opp_lo(), kOPPhi = pack_opp_hi();
+__device__ __forceinline__ int dy_rt(int i) { return (int)((kDY >> (2 * i)) & 3u) - 1; }
+__device__ __forceinline__ int dz_rt(int i) { return (int)((kDZ >> (2 * i)) & 3u) - 1; }
+__device__ __forceinline__ int opp_rt(int i) {
+    return i < 12 ? (int)((kOPPlo >> (5 * i)) & 31u) : (int)((kOPPhi >> (5 * (i - 12))) & 31u);
+}
+
 struct Item {
     int y, z;
     uint32_t row;                  // NX*(y + NY*z)
@@ -116,48 +135,32 @@ __device__ __forceinline__ bool push_bb(int wall, int i) {
     return (DZg(i) == 1 && (wall & 2)) || (DZg(i) == -1 && (wall & 1));
 }
 
-// Source row of population i's staged input for an item.
+// Source row of population i for an item (runtime i).
 template <typename T, bool ODD>
 __device__ __forceinline__ const T* src_row(const PopPtrs<T>& P, const Geometry& g, const Item& I, int wall, int i) {
-    if (!ODD || pull_bb(wall, i)) return P.p[i] + I.row;
-    return P.p[OPPf(i)] + row_at(g, I.y - DYg(i), I.z - DZg(i));
+    const int dz = dz_rt(i);
+    const bool bb = (dz == 1 && (wall & 1)) || (dz == -1 && (wall & 2));
+    if (!ODD || bb) return P.p[i] + I.row;
+    return P.p[opp_rt(i)] + row_at(g, I.y - dy_rt(i), I.z - dz);
 }
-
-// Destination row of population i's result for an item.
+// Issued by one warp: lane i moves population i's row.  The mbarrier learns the
+// byte count from lane 0 before any copy is issued.
 template <typename T, bool ODD>
-__device__ __forceinline__ T* dst_row(const PopPtrs<T>& P, const Geometry& g, const Item& I, int wall, int i) {
-    if (!ODD || push_bb(wall, i)) return P.p[OPPf(i)] + I.row;
-    return P.p[i] + row_at(g, I.y + DYg(i), I.z + DZg(i));
+__device__ __forceinline__ void issue_item(const PopPtrs<T>& P, const Geometry& g, uint32_t it, uint32_t stage_smem,
+                                           uint32_t bar, uint32_t row_bytes, int lane) {
+    if (lane == 0) mbar_expect_tx(bar, (uint32_t)Q * row_bytes);
+    __syncwarp();
+    if (lane < Q) {
+        const Item I = item_of(g, it);
+        bulk_load(stage_smem + (uint32_t)lane * row_bytes, src_row<T, ODD>(P, g, I, wall_of(g, I.z), lane),
+                  row_bytes, bar);
+    }
 }
 
-template <typename T, bool ODD>
-__device__ void store_item(const PopPtrs<T>& P, const Geometry& g, uint32_t it, uint32_t out_smem,
-                           uint32_t row_bytes) {
-    const Item I = item_of(g, it);
-    const int wall = wall_of(g, I.z);
-#pragma unroll
-    for (int i = 0; i < Q; ++i)
-        bulk_store(dst_row<T, ODD>(P, g, I, wall, i), out_smem + (uint32_t)i * row_bytes, row_bytes);
-    bulk_commit();
-}
-
-template <typename T, bool ODD>
-__device__ void issue_item(const PopPtrs<T>& P, const Geometry& g, uint32_t it, uint32_t stage_smem,
-                           uint32_t bar, uint32_t row_bytes) {
-    const Item I = item_of(g, it);
-    const int wall = wall_of(g, I.z);
-    mbar_expect_tx(bar, (uint32_t)Q * row_bytes);
-#pragma unroll
-    for (int i = 0; i < Q; ++i)
-        bulk_load(stage_smem + (uint32_t)i * row_bytes, src_row<T, ODD>(P, g, I, wall, i), row_bytes, bar);
-}
-
-// Two adjacent nodes (x, x+1), x even, of one item.  out == nullptr: write
-// straight to HBM; otherwise into the item's shared-memory output rows
-// (population i's result row at out + i*NX, in destination x order).
-template <typename T, bool ODD, int WALL, bool SOUT>
+// Two adjacent nodes (x, x+1), x even, of one item.
+template <typename T, bool ODD, int WALL>
 __device__ __forceinline__ void pair_update(const PopPtrs<T>& P, const CollideConsts<float>& C,
-                                            const Geometry& g, const Item& I, const T* stage, T* out, int x) {
+                                            const Geometry& g, const Item& I, const T* stage, int x) {
     const int NX = g.NX;
     const int xm1 = (x == 0) ? NX - 1 : x - 1;
     const int xp2 = (x + 2 == NX) ? 0 : x + 2;
@@ -181,9 +184,7 @@ __device__ __forceinline__ void pair_update(const PopPtrs<T>& P, const CollideCo
     for (int i = 0; i < Q; ++i) {
         const bool local = !ODD || push_bb(WALL, i);
         const int sh = local ? 0 : DXg(i);
-        T* d;
-        if (SOUT) d = out + i * NX;
-        else d = local ? P.p[OPPf(i)] + I.row : P.p[i] + row_at(g, I.y + DYg(i), I.z + DZg(i));
+        T* d = local ? P.p[OPPf(i)] + I.row : P.p[i] + row_at(g, I.y + DYg(i), I.z + DZg(i));
         if (sh == 0) {
             st_pair(d + x, fa[i], fb[i]);
         } else if (sh == 1) {
@@ -194,89 +195,71 @@ __device__ __forceinline__ void pair_update(const PopPtrs<T>& P, const CollideCo
     }
 }
 
-template <typename T, bool ODD, bool SOUT>
+constexpr int kMaxStages = 5;
+
+template <typename T, bool ODD>
 __global__ void __launch_bounds__(512, 1)
 k_step_rows(PopPtrs<T> P, CollideConsts<float> C, Geometry g, int nstage, int* err) {
     extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ unsigned int done_count[kMaxStages];
     const uint32_t row_bytes = (uint32_t)g.NX * sizeof(T);
     const uint32_t stage_bytes = (uint32_t)Q * row_bytes;
     const uint32_t bars = smem_addr(smem);                 // nstage mbarriers (8 B each)
     const uint32_t data = bars + 128;                       // stage buffers, 16-B aligned
-    const uint32_t outs = data + (uint32_t)nstage * stage_bytes;   // 2 output buffers (SOUT)
-    T* const stage_ptr0 = reinterpret_cast<T*>(smem + 128);
-    T* const out_ptr0 = stage_ptr0 + (size_t)nstage * Q * g.NX;
+    const T* const stage_ptr0 = reinterpret_cast<const T*>(smem + 128);
     const uint32_t total = (uint32_t)g.NY * (uint32_t)g.NZ;
     const uint32_t G = gridDim.x;
     const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    const unsigned nwarps = blockDim.x >> 5;
 
     if (tid == 0) {
-        for (int s = 0; s < nstage; ++s) mbar_init(bars + 8 * s, 1);
+        for (int s = 0; s < nstage; ++s) {
+            mbar_init(bars + 8 * s, 1);
+            done_count[s] = 0;
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    if (tid == 0) {
+    if (tid < 32) {
         for (int s = 0; s < nstage; ++s) {
             const uint32_t it = blockIdx.x + (uint32_t)s * G;
-            if (it < total) issue_item<T, ODD>(P, g, it, data + s * stage_bytes, bars + 8 * s, row_bytes);
+            if (it < total) issue_item<T, ODD>(P, g, it, data + s * stage_bytes, bars + 8 * s, row_bytes, lane);
         }
     }
     const int npairs = g.NX >> 1;
-    uint32_t k = 0;
-    for (;; ++k) {
+    bool failed = false;
+    for (uint32_t k = 0;; ++k) {
         const uint32_t it = blockIdx.x + k * G;
         if (it >= total) break;
         const int s = (int)(k % (uint32_t)nstage);
-        const uint32_t phase = (k / (uint32_t)nstage) & 1u;
-        const bool ok = mbar_wait(bars + 8 * s, phase);
-        if (__syncthreads_or(!ok)) {
-            // a bulk copy did not complete: flag it, drain what is in flight, leave
-            if (tid == 0) {
-                atomicExch(err, 1);
-                // issued so far: items up to k+nstage-2 (k >= 1) or nstage-1 (k == 0)
-                const uint32_t last = k == 0 ? (uint32_t)nstage - 1 : k + (uint32_t)nstage - 2;
-                for (uint32_t j = k; j <= last; ++j) {
-                    if (blockIdx.x + j * G >= total) break;
-                    mbar_wait(bars + 8 * (j % nstage), (j / nstage) & 1u);
-                }
-                if (SOUT) bulk_wait_all();
-            }
-            return;
-        }
-        // every thread is past item k-1: its outputs can be written back and its
-        // stage refilled
-        if (tid == 0 && k >= 1) {
-            if (SOUT) store_item<T, ODD>(P, g, it - G, outs + ((k - 1) & 1u) * stage_bytes, row_bytes);
-            const uint32_t kk = k - 1 + (uint32_t)nstage;
-            const uint32_t nit = blockIdx.x + kk * G;
-            const int ps = (int)((k - 1) % (uint32_t)nstage);
-            if (nit < total) issue_item<T, ODD>(P, g, nit, data + ps * stage_bytes, bars + 8 * ps, row_bytes);
-        }
+        if (!mbar_wait(bars + 8 * s, (k / (uint32_t)nstage) & 1u)) failed = true;
         const Item I = item_of(g, it);
         const int wall = wall_of(g, I.z);
         const T* stage = stage_ptr0 + (size_t)s * Q * g.NX;
-        T* out = SOUT ? out_ptr0 + (size_t)(k & 1u) * Q * g.NX : nullptr;
         for (int p = tid; p < npairs; p += blockDim.x) {
             const int x = 2 * p;
-            if (wall == 0)      pair_update<T, ODD, 0, SOUT>(P, C, g, I, stage, out, x);
-            else if (wall == 1) pair_update<T, ODD, 1, SOUT>(P, C, g, I, stage, out, x);
-            else if (wall == 2) pair_update<T, ODD, 2, SOUT>(P, C, g, I, stage, out, x);
-            else                pair_update<T, ODD, 3, SOUT>(P, C, g, I, stage, out, x);
+            if (wall == 0)      pair_update<T, ODD, 0>(P, C, g, I, stage, x);
+            else if (wall == 1) pair_update<T, ODD, 1>(P, C, g, I, stage, x);
+            else if (wall == 2) pair_update<T, ODD, 2>(P, C, g, I, stage, x);
+            else                pair_update<T, ODD, 3>(P, C, g, I, stage, x);
         }
-        if (SOUT) {
-            // generic-proxy writes to the output buffer must be visible to the
-            // bulk store; the buffer written next (item k+1) was read by the
-            // store of item k-1, which has to be finished before the barrier
-            fence_proxy_async_smem();
-            if (tid == 0) bulk_wait_read_all();
+        // this warp has finished reading stage s; the last warp refills it
+        __syncwarp();
+        unsigned last = 0;
+        if (lane == 0) {
+            __threadfence_block();
+            last = atomicAdd(&done_count[s], 1u) == nwarps - 1;
+            if (last) done_count[s] = 0;
+        }
+        last = __shfl_sync(0xffffffffu, last, 0);
+        if (last) {
+            __threadfence_block();
+            const uint32_t nit = blockIdx.x + (k + (uint32_t)nstage) * G;
+            if (nit < total) issue_item<T, ODD>(P, g, nit, data + s * stage_bytes, bars + 8 * s, row_bytes, lane);
         }
     }
-    if (SOUT) {
-        __syncthreads();
-        if (tid == 0 && k >= 1) {
-            store_item<T, ODD>(P, g, blockIdx.x + (k - 1) * G, outs + ((k - 1) & 1u) * stage_bytes, row_bytes);
-            bulk_wait_all();
-        }
-    }
+    if (failed) atomicExch(err, 1);
 }
 
 template <typename T>
@@ -289,40 +272,32 @@ PopPtrs<T> pop_ptrs(const DeviceState& s) {
 
 constexpr size_t kSmemBudget = 200 * 1024;
 
-// Stage buffers (and output buffers when they fit) for a row of NX elements.
 template <typename T>
-void plan_for(const Geometry& g, int& nstage, bool& sout) {
+int stages_for(const Geometry& g) {
     const size_t stage = (size_t)Q * g.NX * sizeof(T);
-    const int with_out = (int)((kSmemBudget - 128) / stage) - 2;   // 2 output buffers
-    if (with_out >= 3) {
-        nstage = with_out > 4 ? 4 : with_out;
-        sout = true;
-        return;
-    }
     const int ns = (int)((kSmemBudget - 128) / stage);
-    nstage = ns > 4 ? 4 : ns;
-    sout = false;
+    return ns > kMaxStages ? kMaxStages : ns;
 }
 
 template <typename T>
 cudaError_t rows_impl(const DeviceState& s, int parity, int* err, cudaStream_t st) {
-    int ns;
-    bool sout;
-    plan_for<T>(s.g, ns, sout);
-    const size_t stage = (size_t)Q * s.g.NX * sizeof(T);
-    const size_t smem = 128 + (size_t)(ns + (sout ? 2 : 0)) * stage;
+    const int ns = stages_for<T>(s.g);
+    const size_t smem = 128 + (size_t)ns * Q * s.g.NX * sizeof(T);
     const int threads = std::min(512, std::max(32, ((s.g.NX / 2 + 31) / 32) * 32));
     const PopPtrs<T> P = pop_ptrs<T>(s);
     const uint32_t total = (uint32_t)s.g.NY * (uint32_t)s.g.NZ;
     const unsigned grid = (unsigned)std::min<uint32_t>(total, (uint32_t)s.sm_count);
-    if (sout) {
-        if (parity == 0) k_step_rows<T, false, true><<<grid, threads, smem, st>>>(P, s.cf, s.g, ns, err);
-        else             k_step_rows<T, true, true><<<grid, threads, smem, st>>>(P, s.cf, s.g, ns, err);
-    } else {
-        if (parity == 0) k_step_rows<T, false, false><<<grid, threads, smem, st>>>(P, s.cf, s.g, ns, err);
-        else             k_step_rows<T, true, false><<<grid, threads, smem, st>>>(P, s.cf, s.g, ns, err);
-    }
+    if (parity == 0) k_step_rows<T, false><<<grid, threads, smem, st>>>(P, s.cf, s.g, ns, err);
+    else             k_step_rows<T, true><<<grid, threads, smem, st>>>(P, s.cf, s.g, ns, err);
     return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t set_smem_attr() {
+    const int b = (int)kSmemBudget;
+    cudaError_t e = cudaFuncSetAttribute(k_step_rows<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_step_rows<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    return e;
 }
 
 }  // namespace
@@ -332,21 +307,8 @@ bool rows_supported(const DeviceState& s) {
     const size_t es = s.prec == LBM_PREC_FP32 ? 4 : 2;
     if ((s.g.NX * es) % 16 != 0 || s.g.NX < 16) return false;          // 16-B bulk copies
     if ((s.pstride * es) % 16 != 0) return false;
-    int ns;
-    bool sout;
-    if (s.prec == LBM_PREC_FP32) plan_for<float>(s.g, ns, sout);
-    else plan_for<__half>(s.g, ns, sout);
+    const int ns = s.prec == LBM_PREC_FP32 ? stages_for<float>(s.g) : stages_for<__half>(s.g);
     return ns >= 2 && s.sm_count > 0;
-}
-
-template <typename T>
-cudaError_t set_smem_attr() {
-    const int b = (int)kSmemBudget;
-    cudaError_t e = cudaFuncSetAttribute(k_step_rows<T, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_step_rows<T, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_step_rows<T, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_step_rows<T, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-    return e;
 }
 
 cudaError_t prepare_step_rows() {
