@@ -46,7 +46,7 @@ EXPORTS = (
     "lbm_device_bytes", "lbm_upload_f", "lbm_download_f", "lbm_initpop", "lbm_init_channel",
     "lbm_channel_velocity", "lbm_step", "lbm_step_async", "lbm_synchronize", "lbm_stream",
     "lbm_step_count", "lbm_prerelax", "lbm_macrovar", "lbm_diag", "lbm_profiles", "lbm_avedensity",
-    "lbm_save_flow", "lbm_load_flow",
+    "lbm_save_flow", "lbm_load_flow", "lbm_profiles_noalloc",
 )
 
 
@@ -125,6 +125,7 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
         "lbm_macrovar": (ctypes.c_int, [ctx, dp, dp, dp, dp]),
         "lbm_diag": (ctypes.c_int, [ctx, ctypes.POINTER(LBMStats)]),
         "lbm_profiles": (ctypes.c_int, [ctx, dp]),
+        "lbm_profiles_noalloc": (ctypes.c_int, [ctx, dp]),
         "lbm_avedensity": (ctypes.c_int, [ctx, dp]),
         "lbm_save_flow": (ctypes.c_int, [ctx, ctypes.c_char_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]),
         "lbm_load_flow": (ctypes.c_int, [ctx, ctypes.c_char_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]),

@@ -223,6 +223,17 @@ struct RecordReader {
 
 }  // namespace
 
+namespace lbm {
+// Context internals for entry points defined in other translation units.
+const DeviceState* ctx_state(lbm_ctx* c, int* parity, cudaStream_t* stream, int* device) {
+    *parity = c->parity;
+    *stream = c->stream;
+    *device = c->p.device;
+    return &c->s;
+}
+int set_error(int code, const char* msg) { return fail(code, msg); }
+}  // namespace lbm
+
 extern "C" {
 
 const char* lbm_strerror(int code) {

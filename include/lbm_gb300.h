@@ -191,6 +191,24 @@ int lbm_diag(lbm_ctx* ctx, lbm_stats* st);
  * (column c of plane ix at out[c + LBM_PROFILE_COLS*(ix-1)]). FP64. */
 int lbm_profiles(lbm_ctx* ctx, double* out);
 
+/* The plane sums of lbm_profiles, computed without allocating anything.
+ * No counterpart in the reference: it exists for callers that cannot call
+ * cudaMalloc when they want the statistics -- a monitor sampling profiles
+ * while the solver owns a fixed memory budget, code running between the
+ * captures of a CUDA graph, or a host whose allocator is not the CUDA
+ * runtime's.  (lbm_profiles may allocate its reduction buffer on first use.)
+ * The partial sums live in a device array compiled into the library, sized
+ * for at most LBM_NOALLOC_MAX_PLANES wall-normal planes (about 2 MB, held on
+ * every GPU that loads the library until the process exits); a context with
+ * nx above that is rejected with LBM_ERR_INVALID_ARG.  The first call on a
+ * device looks up that array's device address, so make the first call before
+ * any stream capture.  All calls share the array: calls that overlap on the
+ * GPU race with each other.  Each call overwrites every entry it reads, so
+ * results never depend on a previous call.  On success no host memory is
+ * allocated either.  out: LBM_PROFILE_COLS*nx doubles, as lbm_profiles. */
+#define LBM_NOALLOC_MAX_PLANES 4096
+int lbm_profiles_noalloc(lbm_ctx* ctx, double* out);
+
 /* avedensity (collision.f90:487-513): subtract the fluid-mean delta-rho from
  * every node; here applied to the rest population so that rho = sum f moves
  * by the mean.  mean (may be NULL) receives the value removed. */
