@@ -41,8 +41,11 @@ struct CollideConsts {
 // Relax the populations f[0..18] of one node in place.
 //   FROZEN = false : rho = sum f, j = sum c f + S F/2 (the normal step)
 //   FROZEN = true  : rho = sum f, j = S * uf (velocity frozen, pre-relaxation)
+//   YF = true      : the force has only a streamwise (reference y) component,
+//                    as FORCING sets it (collision.f90:522-524); the terms with
+//                    Fx or Fz are dropped instead of multiplied by zero
 // rho_out / j_out receive the macroscopic values used (scaled units).
-template <typename R, bool FROZEN>
+template <typename R, bool FROZEN, bool YF = false>
 __device__ __forceinline__ void collide(R f[Q], const CollideConsts<R>& c,
                                         R ufx, R ufy, R ufz,
                                         R& rho_out, R& jx_out, R& jy_out, R& jz_out)
@@ -72,6 +75,7 @@ __device__ __forceinline__ void collide(R f[Q], const CollideConsts<R>& c,
 
     R jx, jy, jz;
     if (FROZEN) { jx = c.S * ufx; jy = c.S * ufy; jz = c.S * ufz; }
+    else if (YF) { jx = jfx; jy = jfy + c.hFy; jz = jfz; }
     else        { jx = jfx + c.hFx; jy = jfy + c.hFy; jz = jfz + c.hFz; }
     rho_out = rho; jx_out = jx; jy_out = jy; jz_out = jz;
 
@@ -80,12 +84,22 @@ __device__ __forceinline__ void collide(R f[Q], const CollideConsts<R>& c,
     const R ju = jxux + jyuy + jzuz;                                 // S |u|^2
 
     // moment-space forcing MF = M Fbar (scaled)
-    const R A = jx * c.Fx + jy * c.Fy + jz * c.Fz;                  // S u.F
-    const R P = R(2) * (jx * c.Fx) - jy * c.Fy - jz * c.Fz;         // MF_3pxx / 2
-    const R Wf = jy * c.Fy - jz * c.Fz;                              // MF_pww / 2
-    const R Qxy = jx * c.Fy + jy * c.Fx;
-    const R Qyz = jy * c.Fz + jz * c.Fy;
-    const R Qxz = jx * c.Fz + jz * c.Fx;
+    R A, P, Wf, Qxy, Qyz, Qxz;
+    if (YF) {
+        A = jy * c.Fy;                    // S u.F
+        P = -A;                           // MF_3pxx / 2
+        Wf = A;                           // MF_pww / 2
+        Qxy = jx * c.Fy;
+        Qyz = jz * c.Fy;
+        Qxz = R(0);
+    } else {
+        A = jx * c.Fx + jy * c.Fy + jz * c.Fz;
+        P = R(2) * (jx * c.Fx) - jy * c.Fy - jz * c.Fz;
+        Wf = jy * c.Fy - jz * c.Fz;
+        Qxy = jx * c.Fy + jy * c.Fx;
+        Qyz = jy * c.Fz + jz * c.Fy;
+        Qxz = jx * c.Fz + jz * c.Fx;
+    }
 
     // raw moments of f (non-conserved)
     const R e   = R(-30) * f[0] + R(-11) * sa + R(8) * sd;
@@ -109,16 +123,22 @@ __device__ __forceinline__ void collide(R f[Q], const CollideConsts<R>& c,
     // increments a_k = (MF_k - s_k (m_k + MF_k/2 - meq_k)) / d_k
     const R a_e   = A * R(38.0 / 2394.0) - c.ke * (e + R(19) * A + R(11) * rho - R(19) * ju);
     const R a_eps = A * R(-11.0 / 252.0) - c.keps * (eps - R(5.5) * A - c.oeps * rho - c.oepsj * ju);
-    const R a_qx = c.fqx - c.kq * (qx + R(2.0 / 3.0) * jx - c.thFx);
+    R a_qx, a_qz;
+    if (YF) {
+        a_qx = -c.kq * (qx + R(2.0 / 3.0) * jx);
+        a_qz = -c.kq * (qz + R(2.0 / 3.0) * jz);
+    } else {
+        a_qx = c.fqx - c.kq * (qx + R(2.0 / 3.0) * jx - c.thFx);
+        a_qz = c.fqz - c.kq * (qz + R(2.0 / 3.0) * jz - c.thFz);
+    }
     const R a_qy = c.fqy - c.kq * (qy + R(2.0 / 3.0) * jy - c.thFy);
-    const R a_qz = c.fqz - c.kq * (qz + R(2.0 / 3.0) * jz - c.thFz);
     const R a_p  = P * R(2.0 / 36.0) - c.kp * (p3 + P - eqp);
     const R a_pi = P * R(-1.0 / 72.0) - c.kpi * (pi3 - R(0.5) * P - c.oxx * eqp);
     const R a_w  = Wf * R(2.0 / 12.0) - c.kw * (pw + Wf - eqw);
     const R a_wi = Wf * R(-1.0 / 24.0) - c.kwi * (piw - R(0.5) * Wf - c.oxx * eqw);
     const R a_xy = Qxy * R(0.25) - c.kxy * (pxy + R(0.5) * Qxy - jx * uy);
     const R a_yz = Qyz * R(0.25) - c.kxy * (pyz + R(0.5) * Qyz - jy * uz);
-    const R a_xz = Qxz * R(0.25) - c.kxy * (pxz + R(0.5) * Qxz - jx * uz);
+    const R a_xz = YF ? -c.kxy * (pxz - jx * uz) : Qxz * R(0.25) - c.kxy * (pxz + R(0.5) * Qxz - jx * uz);
     const R a_mx = -c.km * mx, a_my = -c.km * my, a_mz = -c.km * mz;
 
     R ajx, ajy, ajz;
@@ -130,6 +150,11 @@ __device__ __forceinline__ void collide(R f[Q], const CollideConsts<R>& c,
     } else {
         ajx = c.ajx; ajy = c.ajy; ajz = c.ajz;
     }
+    // with a streamwise-only force the x and z momentum increments vanish
+    const R Ox = YF && !FROZEN ? R(-4) * a_qx : ajx - R(4) * a_qx;
+    const R Oz = YF && !FROZEN ? R(-4) * a_qz : ajz - R(4) * a_qz;
+    const R gx = YF && !FROZEN ? a_qx : ajx + a_qx;
+    const R gz = YF && !FROZEN ? a_qz : ajz + a_qz;
 
     // back-transform f* = f + M^T a
     f[0] += R(-30) * a_e + R(12) * a_eps;
@@ -139,7 +164,7 @@ __device__ __forceinline__ void collide(R f[Q], const CollideConsts<R>& c,
     const R Eyz = ba - a_p + R(2) * a_pi;
     const R tw = a_w - R(2) * a_wi;
     const R Ey = Eyz + tw, Ez = Eyz - tw;
-    const R Ox = ajx - R(4) * a_qx, Oy = ajy - R(4) * a_qy, Oz = ajz - R(4) * a_qz;
+    const R Oy = ajy - R(4) * a_qy;
     f[1] += Ex + Ox;  f[2] += Ex - Ox;
     f[3] += Ey + Oy;  f[4] += Ey - Oy;
     f[5] += Ez + Oz;  f[6] += Ez - Oz;
@@ -149,7 +174,7 @@ __device__ __forceinline__ void collide(R f[Q], const CollideConsts<R>& c,
     const R Exy = bd + ppi + wwi;
     const R Exz = bd + ppi - wwi;
     const R Eyy = bd - R(2) * ppi;
-    const R gx = ajx + a_qx, gy = ajy + a_qy, gz = ajz + a_qz;
+    const R gy = ajy + a_qy;
 
     // odd parts of the diagonal pairs share g +- a_m combinations
     const R uxm = gx + a_mx, uxp = gx - a_mx;

@@ -64,7 +64,7 @@ __device__ __forceinline__ bool push_bounces(int i) {
     return (DZg(i) == 1 && (WALL & 2)) || (DZg(i) == -1 && (WALL & 1));
 }
 
-template <typename T, typename R, int WALL, bool FROZEN>
+template <typename T, typename R, int WALL, bool FROZEN, bool YF = false>
 __device__ __forceinline__ void odd_node(const PopPtrs<T>& P, const CollideConsts<R>& C,
                                          const NodeIdx& I, uint32_t n,
                                          R ufx, R ufy, R ufz, R& rho, R& jx, R& jy, R& jz)
@@ -75,7 +75,7 @@ __device__ __forceinline__ void odd_node(const PopPtrs<T>& P, const CollideConst
         if (pull_bounces<WALL>(i)) f[i] = ld_pop(P.p[i] + n);
         else f[i] = ld_pop(P.p[OPPf(i)] + I.at(-DXg(i), -DYg(i), -DZg(i)));
     }
-    collide<R, FROZEN>(f, C, ufx, ufy, ufz, rho, jx, jy, jz);
+    collide<R, FROZEN, YF>(f, C, ufx, ufy, ufz, rho, jx, jy, jz);
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
         if (push_bounces<WALL>(i)) st_pop(P.p[OPPf(i)] + n, f[i]);
@@ -83,7 +83,7 @@ __device__ __forceinline__ void odd_node(const PopPtrs<T>& P, const CollideConst
     }
 }
 
-template <typename T, typename R>
+template <typename T, typename R, bool YF>
 __global__ void __launch_bounds__(kBlockX)
 k_step_even(PopPtrs<T> P, CollideConsts<R> C, Geometry g)
 {
@@ -94,12 +94,12 @@ k_step_even(PopPtrs<T> P, CollideConsts<R> C, Geometry g)
 #pragma unroll
     for (int i = 0; i < Q; ++i) f[i] = ld_pop(P.p[i] + n);
     R rho, jx, jy, jz;
-    collide<R, false>(f, C, R(0), R(0), R(0), rho, jx, jy, jz);
+    collide<R, false, YF>(f, C, R(0), R(0), R(0), rho, jx, jy, jz);
 #pragma unroll
     for (int i = 0; i < Q; ++i) st_pop(P.p[OPPf(i)] + n, f[i]);
 }
 
-template <typename T, typename R>
+template <typename T, typename R, bool YF>
 __global__ void __launch_bounds__(kBlockX)
 k_step_odd(PopPtrs<T> P, CollideConsts<R> C, Geometry g)
 {
@@ -110,10 +110,10 @@ k_step_odd(PopPtrs<T> P, CollideConsts<R> C, Geometry g)
     const uint32_t n = I.at(0, 0, 0);
     R rho, jx, jy, jz;
     const int wall = (z == 0 ? 1 : 0) | (z == g.NZ - 1 ? 2 : 0);
-    if (wall == 0)      odd_node<T, R, 0, false>(P, C, I, n, R(0), R(0), R(0), rho, jx, jy, jz);
-    else if (wall == 1) odd_node<T, R, 1, false>(P, C, I, n, R(0), R(0), R(0), rho, jx, jy, jz);
-    else if (wall == 2) odd_node<T, R, 2, false>(P, C, I, n, R(0), R(0), R(0), rho, jx, jy, jz);
-    else                odd_node<T, R, 3, false>(P, C, I, n, R(0), R(0), R(0), rho, jx, jy, jz);
+    if (wall == 0)      odd_node<T, R, 0, false, YF>(P, C, I, n, R(0), R(0), R(0), rho, jx, jy, jz);
+    else if (wall == 1) odd_node<T, R, 1, false, YF>(P, C, I, n, R(0), R(0), R(0), rho, jx, jy, jz);
+    else if (wall == 2) odd_node<T, R, 2, false, YF>(P, C, I, n, R(0), R(0), R(0), rho, jx, jy, jz);
+    else                odd_node<T, R, 3, false, YF>(P, C, I, n, R(0), R(0), R(0), rho, jx, jy, jz);
 }
 
 // Pre-relaxation step (main.f90:69-90): velocity frozen at uf (GPU layout,
@@ -186,8 +186,14 @@ cudaError_t step_impl(const DeviceState& s, int parity, cudaStream_t st) {
     const dim3 grid = step_grid(s.g, bx);
     const CollideConsts<R>* C;
     if constexpr (sizeof(R) == 8) C = &s.cd; else C = &s.cf;
-    if (parity == 0) k_step_even<T, R><<<grid, bx, 0, st>>>(P, *C, s.g);
-    else             k_step_odd<T, R><<<grid, bx, 0, st>>>(P, *C, s.g);
+    const bool yf = C->Fx == R(0) && C->Fz == R(0);
+    if (yf) {
+        if (parity == 0) k_step_even<T, R, true><<<grid, bx, 0, st>>>(P, *C, s.g);
+        else             k_step_odd<T, R, true><<<grid, bx, 0, st>>>(P, *C, s.g);
+    } else {
+        if (parity == 0) k_step_even<T, R, false><<<grid, bx, 0, st>>>(P, *C, s.g);
+        else             k_step_odd<T, R, false><<<grid, bx, 0, st>>>(P, *C, s.g);
+    }
     return cudaGetLastError();
 }
 

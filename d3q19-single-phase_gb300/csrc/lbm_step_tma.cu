@@ -158,7 +158,7 @@ __device__ __forceinline__ void issue_item(const PopPtrs<T>& P, const Geometry& 
 }
 
 // Two adjacent nodes (x, x+1), x even, of one item.
-template <typename T, bool ODD, int WALL>
+template <typename T, bool ODD, int WALL, bool YF>
 __device__ __forceinline__ void pair_update(const PopPtrs<T>& P, const CollideConsts<float>& C,
                                             const Geometry& g, const Item& I, const T* stage, int x) {
     const int NX = g.NX;
@@ -178,8 +178,8 @@ __device__ __forceinline__ void pair_update(const PopPtrs<T>& P, const CollideCo
         }
     }
     float rho, jx, jy, jz;
-    collide<float, false>(fa, C, 0.f, 0.f, 0.f, rho, jx, jy, jz);
-    collide<float, false>(fb, C, 0.f, 0.f, 0.f, rho, jx, jy, jz);
+    collide<float, false, YF>(fa, C, 0.f, 0.f, 0.f, rho, jx, jy, jz);
+    collide<float, false, YF>(fb, C, 0.f, 0.f, 0.f, rho, jx, jy, jz);
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
         const bool local = !ODD || push_bb(WALL, i);
@@ -195,10 +195,19 @@ __device__ __forceinline__ void pair_update(const PopPtrs<T>& P, const CollideCo
     }
 }
 
+// All pairs of an item handled by this thread; the wall case is fixed for
+// the whole loop so that row offsets can be hoisted out of it.
+template <typename T, bool ODD, int WALL, bool YF>
+__device__ __forceinline__ void item_pairs(const PopPtrs<T>& P, const CollideConsts<float>& C, const Geometry& g,
+                                           const Item& I, const T* stage, int tid, int nthreads) {
+    const int npairs = g.NX >> 1;
+    for (int p = tid; p < npairs; p += nthreads) pair_update<T, ODD, WALL, YF>(P, C, g, I, stage, 2 * p);
+}
+
 constexpr int kMaxStages = 5;
 
-template <typename T, bool ODD>
-__global__ void __launch_bounds__(512, 1)
+template <typename T, bool ODD, bool YF, int NT>
+__global__ void __launch_bounds__(NT, 512 / NT)
 k_step_rows(PopPtrs<T> P, CollideConsts<float> C, Geometry g, int nstage, int* err) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ unsigned int done_count[kMaxStages];
@@ -211,7 +220,7 @@ k_step_rows(PopPtrs<T> P, CollideConsts<float> C, Geometry g, int nstage, int* e
     const uint32_t G = gridDim.x;
     const int tid = threadIdx.x;
     const int lane = tid & 31;
-    const unsigned nwarps = blockDim.x >> 5;
+    const unsigned nwarps = NT / 32;
 
     if (tid == 0) {
         for (int s = 0; s < nstage; ++s) {
@@ -227,7 +236,6 @@ k_step_rows(PopPtrs<T> P, CollideConsts<float> C, Geometry g, int nstage, int* e
             if (it < total) issue_item<T, ODD>(P, g, it, data + s * stage_bytes, bars + 8 * s, row_bytes, lane);
         }
     }
-    const int npairs = g.NX >> 1;
     bool failed = false;
     for (uint32_t k = 0;; ++k) {
         const uint32_t it = blockIdx.x + k * G;
@@ -237,13 +245,10 @@ k_step_rows(PopPtrs<T> P, CollideConsts<float> C, Geometry g, int nstage, int* e
         const Item I = item_of(g, it);
         const int wall = wall_of(g, I.z);
         const T* stage = stage_ptr0 + (size_t)s * Q * g.NX;
-        for (int p = tid; p < npairs; p += blockDim.x) {
-            const int x = 2 * p;
-            if (wall == 0)      pair_update<T, ODD, 0>(P, C, g, I, stage, x);
-            else if (wall == 1) pair_update<T, ODD, 1>(P, C, g, I, stage, x);
-            else if (wall == 2) pair_update<T, ODD, 2>(P, C, g, I, stage, x);
-            else                pair_update<T, ODD, 3>(P, C, g, I, stage, x);
-        }
+        if (wall == 0)      item_pairs<T, ODD, 0, YF>(P, C, g, I, stage, tid, NT);
+        else if (wall == 1) item_pairs<T, ODD, 1, YF>(P, C, g, I, stage, tid, NT);
+        else if (wall == 2) item_pairs<T, ODD, 2, YF>(P, C, g, I, stage, tid, NT);
+        else                item_pairs<T, ODD, 3, YF>(P, C, g, I, stage, tid, NT);
         // this warp has finished reading stage s; the last warp refills it
         __syncwarp();
         unsigned last = 0;
@@ -270,33 +275,69 @@ PopPtrs<T> pop_ptrs(const DeviceState& s) {
     return P;
 }
 
-constexpr size_t kSmemBudget = 200 * 1024;
+constexpr size_t kSmemPerSM = 224 * 1024;    // dynamic shared memory planned per SM
+
+// Launch shape of the row kernels for a row of NX elements of T:
+// 512 threads (one CTA per SM), or 256 threads with two CTAs per SM when each
+// thread then handles at least two pairs per item and two stages still fit.
+struct RowPlan { int threads, ctas_per_sm, nstage; size_t smem; };
 
 template <typename T>
-int stages_for(const Geometry& g) {
+RowPlan plan_rows(const Geometry& g) {
     const size_t stage = (size_t)Q * g.NX * sizeof(T);
-    const int ns = (int)((kSmemBudget - 128) / stage);
-    return ns > kMaxStages ? kMaxStages : ns;
+    RowPlan r;
+    const int pairs = g.NX / 2;
+    if (pairs >= 512 && 2 * (128 + 2 * stage) <= kSmemPerSM) {
+        r.threads = 256;
+        r.ctas_per_sm = 2;
+    } else {
+        r.threads = 512;
+        r.ctas_per_sm = 1;
+    }
+    int ns = (int)((kSmemPerSM / r.ctas_per_sm - 128) / stage);
+    r.nstage = ns > kMaxStages ? kMaxStages : ns;
+    r.smem = 128 + (size_t)r.nstage * stage;
+    return r;
+}
+
+template <typename T, bool YF, int NT>
+void launch_rows_nt(const DeviceState& s, const PopPtrs<T>& P, int parity, int* err, const RowPlan& r,
+                    unsigned grid, cudaStream_t st) {
+    if (parity == 0) k_step_rows<T, false, YF, NT><<<grid, NT, r.smem, st>>>(P, s.cf, s.g, r.nstage, err);
+    else             k_step_rows<T, true, YF, NT><<<grid, NT, r.smem, st>>>(P, s.cf, s.g, r.nstage, err);
 }
 
 template <typename T>
 cudaError_t rows_impl(const DeviceState& s, int parity, int* err, cudaStream_t st) {
-    const int ns = stages_for<T>(s.g);
-    const size_t smem = 128 + (size_t)ns * Q * s.g.NX * sizeof(T);
-    const int threads = std::min(512, std::max(32, ((s.g.NX / 2 + 31) / 32) * 32));
+    const RowPlan r = plan_rows<T>(s.g);
     const PopPtrs<T> P = pop_ptrs<T>(s);
     const uint32_t total = (uint32_t)s.g.NY * (uint32_t)s.g.NZ;
-    const unsigned grid = (unsigned)std::min<uint32_t>(total, (uint32_t)s.sm_count);
-    if (parity == 0) k_step_rows<T, false><<<grid, threads, smem, st>>>(P, s.cf, s.g, ns, err);
-    else             k_step_rows<T, true><<<grid, threads, smem, st>>>(P, s.cf, s.g, ns, err);
+    const unsigned grid = (unsigned)std::min<uint32_t>(total, (uint32_t)(s.sm_count * r.ctas_per_sm));
+    const bool yf = s.cf.Fx == 0.0f && s.cf.Fz == 0.0f;
+    if (r.threads == 256) {
+        if (yf) launch_rows_nt<T, true, 256>(s, P, parity, err, r, grid, st);
+        else    launch_rows_nt<T, false, 256>(s, P, parity, err, r, grid, st);
+    } else {
+        if (yf) launch_rows_nt<T, true, 512>(s, P, parity, err, r, grid, st);
+        else    launch_rows_nt<T, false, 512>(s, P, parity, err, r, grid, st);
+    }
     return cudaGetLastError();
+}
+
+template <typename T, bool YF, int NT>
+cudaError_t set_attr_nt() {
+    const int b = (int)(kSmemPerSM / (512 / NT));
+    cudaError_t e = cudaFuncSetAttribute(k_step_rows<T, false, YF, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_step_rows<T, true, YF, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    return e;
 }
 
 template <typename T>
 cudaError_t set_smem_attr() {
-    const int b = (int)kSmemBudget;
-    cudaError_t e = cudaFuncSetAttribute(k_step_rows<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_step_rows<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaError_t e = set_attr_nt<T, false, 512>();
+    if (e == cudaSuccess) e = set_attr_nt<T, true, 512>();
+    if (e == cudaSuccess) e = set_attr_nt<T, false, 256>();
+    if (e == cudaSuccess) e = set_attr_nt<T, true, 256>();
     return e;
 }
 
@@ -307,8 +348,8 @@ bool rows_supported(const DeviceState& s) {
     const size_t es = s.prec == LBM_PREC_FP32 ? 4 : 2;
     if ((s.g.NX * es) % 16 != 0 || s.g.NX < 16) return false;          // 16-B bulk copies
     if ((s.pstride * es) % 16 != 0) return false;
-    const int ns = s.prec == LBM_PREC_FP32 ? stages_for<float>(s.g) : stages_for<__half>(s.g);
-    return ns >= 2 && s.sm_count > 0;
+    const RowPlan r = s.prec == LBM_PREC_FP32 ? plan_rows<float>(s.g) : plan_rows<__half>(s.g);
+    return r.nstage >= 2 && s.sm_count > 0;
 }
 
 cudaError_t prepare_step_rows() {
