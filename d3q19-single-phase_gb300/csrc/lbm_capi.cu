@@ -577,7 +577,7 @@ int lbm_diag(lbm_ctx* c, lbm_stats* st) {
     std::vector<double> h(need);
     CK(cudaMemcpyAsync(h.data(), c->d_red, need * 8, cudaMemcpyDeviceToHost, c->stream));
     if (int rc = sync(c)) return rc;
-    double rmax = -INFINITY, rmin = INFINITY, vmax = -1.0, vidx = 0.0, nonf = 0.0;
+    double rmax = -INFINITY, rmin = INFINITY, vmax = -1.0, vidx = 1e300, nonf = 0.0;
     for (int b = 0; b < kExtremaBlocks; ++b) {
         const double* r = &h[(size_t)b * 5];
         rmax = std::max(rmax, r[0]);

@@ -69,6 +69,32 @@ __device__ void gather_natural(const DeviceState& s, int parity, int x, int y, i
     }
 }
 
+// Same, in the arithmetic type R of the diagnostics (FP32 for FP32/FP16
+// storage, FP64 for FP64 storage).
+template <typename T, typename R>
+__device__ void gather_natural_r(const DeviceState& s, int parity, int x, int y, int z, R f[Q]) {
+    const Geometry& g = s.g;
+    const R invS = (R)s.cd.invS;
+    const uint32_t n = x + g.NX * (y + g.NY * (uint32_t)z);
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        uint32_t m = n;
+        int slot = i;
+        if (parity) {
+            const int zs = z - DZg(i);
+            if (zs >= 0 && zs < g.NZ) {
+                int xs = x - DXg(i); xs = xs < 0 ? xs + g.NX : (xs >= g.NX ? xs - g.NX : xs);
+                int ys = y - DYg(i); ys = ys < 0 ? ys + g.NY : (ys >= g.NY ? ys - g.NY : ys);
+                m = xs + g.NX * (ys + g.NY * (uint32_t)zs);
+                slot = OPPf(i);
+            }
+        }
+        f[i] = (R)ld_pop(pop_plane<T>(s, slot) + m) * invS;
+    }
+}
+template <typename T> struct DiagR { using type = float; };
+template <> struct DiagR<double> { using type = double; };
+
 template <typename T>
 __device__ __forceinline__ void put(const DeviceState& s, int i, uint32_t n, double v_true) {
     const double S = s.cd.S;
@@ -160,9 +186,9 @@ __global__ void k_init_channel(DeviceState s, double uc, double amp, uint64_t se
 }
 
 // macrovar (collision.f90:394-418) for fluid nodes
-__device__ __forceinline__ void macro_of(const double f[Q], const double F[3], double& rho,
-                                         double& ux, double& uy, double& uz) {
-    double r = 0.0, a = 0.0, b = 0.0, c = 0.0;
+template <typename R>
+__device__ __forceinline__ void macro_of(const R f[Q], const R F[3], R& rho, R& ux, R& uy, R& uz) {
+    R r = 0, a = 0, b = 0, c = 0;
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
         r += f[i];
@@ -170,7 +196,7 @@ __device__ __forceinline__ void macro_of(const double f[Q], const double F[3], d
         if (CYf(i)) b += CYf(i) * f[i];
         if (CZf(i)) c += CZf(i) * f[i];
     }
-    rho = r; ux = a + 0.5 * F[0]; uy = b + 0.5 * F[1]; uz = c + 0.5 * F[2];
+    rho = r; ux = a + R(0.5) * F[0]; uy = b + R(0.5) * F[1]; uz = c + R(0.5) * F[2];
 }
 
 template <typename T>
@@ -182,7 +208,7 @@ __global__ void k_macro(DeviceState s, int parity, double* rho, double* ux, doub
     gather_natural<T>(s, parity, r.iy, r.iz, r.ix, f);
     const double F[3] = {(double)s.cd.Fx, (double)s.cd.Fy, (double)s.cd.Fz};
     double d, a, b, c;
-    macro_of(f, F, d, a, b, c);
+    macro_of<double>(f, F, d, a, b, c);
     const size_t o = ref_lin(s.g, r.ix, r.iy, r.iz - z0);
     if (rho) rho[o] = d;
     if (ux) ux[o] = a;
@@ -203,26 +229,29 @@ __global__ void k_ref_to_gpu_vec(Geometry g, size_t N, const double* __restrict_
 constexpr int kRedThreads = 256;
 
 // Plane sums for statistc2: block (b, Z) covers part of plane Z (ref x = Z+1).
+// Per-node values in the diagnostics type R, sums in FP64.
 template <typename T>
 __global__ void __launch_bounds__(kRedThreads)
 k_profiles(DeviceState s, int parity, double* __restrict__ partial) {
+    using R = typename DiagR<T>::type;
     const Geometry& g = s.g;
     const int z = blockIdx.y;
-    const double F[3] = {(double)s.cd.Fx, (double)s.cd.Fy, (double)s.cd.Fz};
+    const R F[3] = {(R)s.cd.Fx, (R)s.cd.Fy, (R)s.cd.Fz};
     double acc[LBM_PROFILE_COLS];
 #pragma unroll
     for (int k = 0; k < LBM_PROFILE_COLS; ++k) acc[k] = 0.0;
     const uint32_t plane = g.NXY;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < plane; t += gridDim.x * blockDim.x) {
         const int x = t % g.NX, y = t / g.NX;
-        double f[Q];
-        gather_natural<T>(s, parity, x, y, z, f);
-        double rho, ux, uy, uz;
+        R f[Q];
+        gather_natural_r<T, R>(s, parity, x, y, z, f);
+        R rho, ux, uy, uz;
         macro_of(f, F, rho, ux, uy, uz);
-        acc[0] += ux; acc[1] += uy; acc[2] += uz;
-        acc[3] += ux * uz; acc[4] += ux * uy; acc[5] += uy * uz;
-        acc[6] += ux * ux; acc[7] += uy * uy; acc[8] += uz * uz;
-        acc[9] += rho; acc[10] += rho * rho; acc[11] += 1.0;
+        const double dux = ux, duy = uy, duz = uz, drho = rho;
+        acc[0] += dux; acc[1] += duy; acc[2] += duz;
+        acc[3] += dux * duz; acc[4] += dux * duy; acc[5] += duy * duz;
+        acc[6] += dux * dux; acc[7] += duy * duy; acc[8] += duz * duz;
+        acc[9] += drho; acc[10] += drho * drho; acc[11] += 1.0;
     }
     __shared__ double sh[LBM_PROFILE_COLS][kRedThreads / 32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -240,35 +269,40 @@ k_profiles(DeviceState s, int parity, double* __restrict__ partial) {
     }
 }
 
-// Per-block extrema: {rho_max, rho_min, vmax, vmax_refidx, nonfinite}
+// Per-block extrema: {rho_max, rho_min, vmax, vmax_refidx, nonfinite}.
+// Blocks walk whole streamwise rows (32-bit row arithmetic); per-node values in
+// the diagnostics type R.
 template <typename T>
 __global__ void __launch_bounds__(kRedThreads)
 k_extrema(DeviceState s, int parity, double* __restrict__ partial) {
+    using R = typename DiagR<T>::type;
     const Geometry& g = s.g;
-    const double F[3] = {(double)s.cd.Fx, (double)s.cd.Fy, (double)s.cd.Fz};
-    double rmax = -INFINITY, rmin = INFINITY, vmax = -1.0, vidx = 0.0, nonf = 0.0;
-    const size_t N = s.N;
-    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < N;
-         t += (size_t)gridDim.x * blockDim.x) {
-        const int x = (int)(t % g.NX);
-        const int y = (int)((t / g.NX) % g.NY);
-        const int z = (int)(t / g.NXY);
-        double f[Q];
-        gather_natural<T>(s, parity, x, y, z, f);
-        bool finite = true;
+    const R F[3] = {(R)s.cd.Fx, (R)s.cd.Fy, (R)s.cd.Fz};
+    R rmax = -INFINITY, rmin = INFINITY, vmax = -1;
+    uint32_t vidx = 0xffffffffu;
+    unsigned nonf = 0;
+    const uint32_t rows = (uint32_t)g.NY * (uint32_t)g.NZ;
+    for (uint32_t r = blockIdx.x; r < rows; r += gridDim.x) {
+        const int y = (int)(r % (uint32_t)g.NY), z = (int)(r / (uint32_t)g.NY);
+        for (int x = threadIdx.x; x < g.NX; x += blockDim.x) {
+            R f[Q];
+            gather_natural_r<T, R>(s, parity, x, y, z, f);
+            bool finite = true;
 #pragma unroll
-        for (int i = 0; i < Q; ++i) finite &= isfinite(f[i]);
-        if (!finite) { nonf += 1.0; continue; }
-        double rho, ux, uy, uz;
-        macro_of(f, F, rho, ux, uy, uz);
-        rmax = fmax(rmax, rho); rmin = fmin(rmin, rho);
-        const double v = sqrt(ux * ux + uy * uy + uz * uz);
-        const double ri = (double)ref_lin(g, z, x, y);
-        if (v > vmax || (v == vmax && ri < vidx)) { vmax = v; vidx = ri; }
+            for (int i = 0; i < Q; ++i) finite &= isfinite(f[i]);
+            if (!finite) { ++nonf; continue; }
+            R rho, ux, uy, uz;
+            macro_of(f, F, rho, ux, uy, uz);
+            rmax = rho > rmax ? rho : rmax;
+            rmin = rho < rmin ? rho : rmin;
+            const R v = sqrt(ux * ux + uy * uy + uz * uz);
+            const uint32_t ri = (uint32_t)z + (uint32_t)g.NZ * ((uint32_t)x + (uint32_t)g.NX * (uint32_t)y);
+            if (v > vmax || (v == vmax && ri < vidx)) { vmax = v; vidx = ri; }
+        }
     }
     __shared__ double sh[5][kRedThreads];
     sh[0][threadIdx.x] = rmax; sh[1][threadIdx.x] = rmin; sh[2][threadIdx.x] = vmax;
-    sh[3][threadIdx.x] = vidx; sh[4][threadIdx.x] = nonf;
+    sh[3][threadIdx.x] = vidx == 0xffffffffu ? 1e300 : (double)vidx; sh[4][threadIdx.x] = nonf;
     __syncthreads();
     for (int h = blockDim.x / 2; h > 0; h >>= 1) {
         if (threadIdx.x < h) {
