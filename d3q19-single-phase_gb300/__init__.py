@@ -46,7 +46,8 @@ EXPORTS = (
     "lbm_device_bytes", "lbm_upload_f", "lbm_download_f", "lbm_initpop", "lbm_init_channel",
     "lbm_channel_velocity", "lbm_step", "lbm_step_async", "lbm_synchronize", "lbm_stream",
     "lbm_step_count", "lbm_prerelax", "lbm_macrovar", "lbm_diag", "lbm_profiles", "lbm_avedensity",
-    "lbm_save_flow", "lbm_load_flow", "lbm_profiles_noalloc",
+    "lbm_save_flow", "lbm_load_flow", "lbm_profiles_noalloc", "lbm_particle_params_init",
+    "lbm_particles_place", "lbm_particles_set", "lbm_particles_get", "lbm_particle_counts",
 )
 
 
@@ -79,6 +80,12 @@ class LBMStats(ctypes.Structure):
         ("rho_max", ctypes.c_double), ("rho_min", ctypes.c_double), ("vmax", ctypes.c_double),
         ("vmax_at", ctypes.c_int32 * 3), ("nonfinite", ctypes.c_int32),
     ]
+
+
+class LBMParticleParams(ctypes.Structure):
+    _fields_ = [("npart", ctypes.c_int32), ("flags", ctypes.c_int32), ("radius", ctypes.c_double),
+                ("rho_ratio", ctypes.c_double), ("stf0", ctypes.c_double), ("stf1", ctypes.c_double),
+                ("stf0_w", ctypes.c_double), ("stf1_w", ctypes.c_double), ("zeta", ctypes.c_double)]
 
 
 _lib = None
@@ -129,6 +136,15 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
         "lbm_avedensity": (ctypes.c_int, [ctx, dp]),
         "lbm_save_flow": (ctypes.c_int, [ctx, ctypes.c_char_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]),
         "lbm_load_flow": (ctypes.c_int, [ctx, ctypes.c_char_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]),
+        "lbm_particle_params_init": (ctypes.c_int, [ctypes.POINTER(LBMParticleParams), ctypes.c_int32,
+                                                    ctypes.c_double, ctypes.c_double]),
+        "lbm_particles_place": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                               ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
+                                               dp]),
+        "lbm_particles_set": (ctypes.c_int, [ctx, ctypes.POINTER(LBMParticleParams), dp, dp, dp]),
+        "lbm_particles_get": (ctypes.c_int, [ctx, dp, dp, dp, dp, dp]),
+        "lbm_particle_counts": (ctypes.c_int, [ctx, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
+                                               ctypes.POINTER(ctypes.c_int64)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -391,6 +407,31 @@ class Lattice:
         self._call("lbm_avedensity", ctypes.byref(m))
         return m.value
 
+    # moving spheres -----------------------------------------------------------
+    def set_particles(self, pos, radius: float, rho_ratio: float = 2.0, vel=None, omg=None, **overrides) -> None:
+        """Attach spheres (positions (n,3), reference axes, node ix at ix-1/2)."""
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        pp = LBMParticleParams()
+        _check(self.lib, self.lib.lbm_particle_params_init(ctypes.byref(pp), len(pos), radius, rho_ratio),
+               "lbm_particle_params_init")
+        for k, v in overrides.items():
+            setattr(pp, k, v)
+        v = None if vel is None else np.ascontiguousarray(vel, dtype=np.float64).reshape(-1, 3)
+        o = None if omg is None else np.ascontiguousarray(omg, dtype=np.float64).reshape(-1, 3)
+        self._npart = len(pos)
+        self._call("lbm_particles_set", ctypes.byref(pp), _dptr(pos), _dptr(v), _dptr(o))
+
+    def particles(self) -> dict:
+        n = getattr(self, "_npart", 0)
+        out = {k: np.empty((n, 3)) for k in ("pos", "vel", "omg", "force", "torque")}
+        self._call("lbm_particles_get", *(_dptr(out[k]) for k in ("pos", "vel", "omg", "force", "torque")))
+        return out
+
+    def particle_counts(self) -> tuple[int, int, int]:
+        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        self._call("lbm_particle_counts", ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+        return a.value, b.value, c.value
+
     def save_flow(self, path: str | Path, kind: int, ints) -> None:
         arr = (ctypes.c_int32 * 3)(*list(ints) + [0] * (3 - len(ints)))
         self._call("lbm_save_flow", str(path).encode(), kind, arr)
@@ -408,6 +449,16 @@ def channel_velocity(nx: int, ny: int, nz: int, uc: float, amp: float, seed: int
     _check(lib, lib.lbm_channel_velocity(nx, ny, nz, uc, amp, ctypes.c_uint64(seed), *map(_dptr, out)),
            "lbm_channel_velocity")
     return tuple(out)
+
+
+def place_spheres(nx: int, ny: int, nz: int, npart: int, radius: float, gap: float = 2.0,
+                  wall_gap: float = 1.0, seed: int = 12345) -> np.ndarray:
+    """Seeded non-overlapping sphere centres (reference axes), shape (npart, 3)."""
+    lib = load_library()
+    pos = np.empty((npart, 3), dtype=np.float64)
+    _check(lib, lib.lbm_particles_place(nx, ny, nz, npart, radius, gap, wall_gap, ctypes.c_uint64(seed),
+                                        _dptr(pos)), "lbm_particles_place")
+    return pos
 
 
 def statistics(prof: np.ndarray, ustar: float) -> dict:

@@ -29,6 +29,10 @@ struct lbm_ctx {
     double* d_rho = nullptr;   // pre-relaxation density
     unsigned long long* d_max = nullptr;
     int* d_err = nullptr;      // set by a kernel whose bounded wait gave up
+    DeviceParticles P{};       // spheres (npart == 0: none)
+    lbm_particle_params pp{};
+    int have_prev = 0;         // Adams-Bashforth history available
+    unsigned long long* d_count = nullptr;
 };
 
 namespace {
@@ -129,6 +133,14 @@ int sync(lbm_ctx* c) {
         if (flag) {
             cudaMemset(c->d_err, 0, sizeof(int));
             return fail(LBM_ERR_CUDA, "a step kernel's bulk-copy wait timed out; populations are invalid");
+        }
+    }
+    if (c->P.npart > 0) {
+        unsigned flag = 0;
+        CK(cudaMemcpy(&flag, c->P.counters + 3, sizeof(unsigned), cudaMemcpyDeviceToHost));
+        if (flag) {
+            cudaMemset(c->P.counters + 3, 0, sizeof(unsigned));
+            return fail(LBM_ERR_STATE, "refill list overflow: spheres moved too far in one step");
         }
     }
     return LBM_OK;
@@ -361,6 +373,12 @@ int lbm_destroy(lbm_ctx* c) {
     cudaFree(c->d_rho);
     cudaFree(c->d_max);
     cudaFree(c->d_err);
+    cudaFree(c->d_count);
+    cudaFree(c->P.pos);
+    cudaFree(c->P.owner);
+    cudaFree(c->P.refill_node);
+    cudaFree(c->P.refill_part);
+    cudaFree(c->P.counters);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return LBM_OK;
@@ -449,6 +467,10 @@ int lbm_step_async(lbm_ctx* c, int32_t nsteps) {
         else CK(launch_step(c->s, c->parity, c->stream));
         c->parity ^= 1;
         ++c->nsteps;
+        if (c->P.npart > 0) {
+            CK(particles_after_step(c->s, c->P, c->parity, c->have_prev, c->stream));
+            c->have_prev = 1;
+        }
     }
     return LBM_OK;
 }
@@ -680,6 +702,157 @@ int lbm_load_flow(lbm_ctx* c, const char* path, int32_t kind, int32_t* ints) {
     if (ints) for (int i = 0; i < nints; ++i) ints[i] = hdr[i];
     c->parity = 0;
     c->nsteps = 0;
+    return LBM_OK;
+}
+
+int lbm_particle_params_init(lbm_particle_params* pp, int32_t npart, double radius, double rho_ratio) {
+    if (!pp) return fail(LBM_ERR_INVALID_ARG, "null params");
+    if (npart < 0 || !(radius > 0.0) || !(rho_ratio > 0.0)) return fail(LBM_ERR_INVALID_ARG, "bad sphere parameters");
+    std::memset(pp, 0, sizeof(*pp));
+    pp->npart = npart;
+    pp->radius = radius;
+    pp->rho_ratio = rho_ratio;
+    // Feng & Michaelides stiffness constants of para.f90:357-360
+    pp->stf0 = 0.025; pp->stf1 = 0.002; pp->stf0_w = 0.025; pp->stf1_w = 0.002;
+    pp->zeta = 1.0;
+    return LBM_OK;
+}
+
+int lbm_particles_place(int32_t nx, int32_t ny, int32_t nz, int32_t npart, double radius, double gap,
+                        double wall_gap, uint64_t seed, double* pos) {
+    if (nx < 1 || ny < 1 || nz < 1 || npart < 0 || !(radius > 0.0) || !pos || gap < 0 || wall_gap < 0)
+        return fail(LBM_ERR_INVALID_ARG, "bad placement arguments");
+    const double lo = radius + wall_gap, hi = (double)nx - radius - wall_gap;
+    if (!(hi > lo)) return fail(LBM_ERR_INVALID_ARG, "channel too narrow for the spheres");
+    const double dmin = 2.0 * radius + gap;
+    // cell grid for the overlap test: cells at least dmin wide
+    const int cy = std::max(1, (int)(ny / dmin)), cz = std::max(1, (int)(nz / dmin)), cx = std::max(1, (int)(nx / dmin));
+    std::vector<std::vector<int>> cells((size_t)cx * cy * cz);
+    auto cell_of = [&](double x, double y, double z, int& a, int& b, int& c2) {
+        a = std::min(cx - 1, (int)(x / nx * cx));
+        b = std::min(cy - 1, (int)(y / ny * cy));
+        c2 = std::min(cz - 1, (int)(z / nz * cz));
+    };
+    auto mi = [](double d, double L) { return d >= 0.5 * L ? d - L : (d < -0.5 * L ? d + L : d); };
+    uint64_t key = 0;
+    for (int32_t k = 0; k < npart; ++k) {
+        bool placed = false;
+        for (int attempt = 0; attempt < 100000 && !placed; ++attempt) {
+            const double x = lo + (hi - lo) * 0.5 * (uniform_pm1(seed, key++) + 1.0);
+            const double y = ny * 0.5 * (uniform_pm1(seed, key++) + 1.0);
+            const double z = nz * 0.5 * (uniform_pm1(seed, key++) + 1.0);
+            int a, b, c2;
+            cell_of(x, y, z, a, b, c2);
+            bool ok = true;
+            for (int da = -1; da <= 1 && ok; ++da) {
+                const int aa = a + da;
+                if (aa < 0 || aa >= cx) continue;
+                for (int db = -1; db <= 1 && ok; ++db) {
+                    if (cy < 3 && db != 0 && (cy == 1 || db == 1)) continue;
+                    const int bb = ((b + db) % cy + cy) % cy;
+                    for (int dc = -1; dc <= 1 && ok; ++dc) {
+                        if (cz < 3 && dc != 0 && (cz == 1 || dc == 1)) continue;
+                        const int cc = ((c2 + dc) % cz + cz) % cz;
+                        for (int j : cells[((size_t)aa * cy + bb) * cz + cc]) {
+                            const double d0 = pos[3 * j] - x, d1 = mi(pos[3 * j + 1] - y, ny), d2 = mi(pos[3 * j + 2] - z, nz);
+                            if (d0 * d0 + d1 * d1 + d2 * d2 < dmin * dmin) { ok = false; break; }
+                        }
+                    }
+                }
+            }
+            if (!ok) continue;
+            pos[3 * k] = x; pos[3 * k + 1] = y; pos[3 * k + 2] = z;
+            cells[((size_t)a * cy + b) * cz + c2].push_back(k);
+            placed = true;
+        }
+        if (!placed) return fail(LBM_ERR_INVALID_ARG, "could not place all spheres (volume fraction too high)");
+    }
+    return LBM_OK;
+}
+
+int lbm_particles_set(lbm_ctx* c, const lbm_particle_params* pp, const double* pos, const double* vel,
+                      const double* omg) {
+    if (check_ctx(c) || !pp || (pp->npart > 0 && !pos)) return fail(LBM_ERR_INVALID_ARG, "null argument");
+    if (pp->npart < 0 || !(pp->radius > 0.0) || !(pp->rho_ratio > 0.0) || !(pp->zeta > 0.0))
+        return fail(LBM_ERR_INVALID_ARG, "bad sphere parameters");
+    for (int32_t k = 0; k < pp->npart; ++k) {
+        const double x = pos[3 * k];
+        if (!(x - pp->radius > 0.0) || !(x + pp->radius < (double)c->p.nx))
+            return fail(LBM_ERR_INVALID_ARG, "sphere " + std::to_string(k) + " crosses a wall");
+        if (!std::isfinite(pos[3 * k + 1]) || !std::isfinite(pos[3 * k + 2]))
+            return fail(LBM_ERR_INVALID_ARG, "non-finite sphere position");
+    }
+    if (int rc = set_device(c)) return rc;
+    const int n = pp->npart;
+    DeviceParticles& P = c->P;
+    if (P.pos) { cudaFree(P.pos); P.pos = nullptr; }
+    if (!P.owner) CK(cudaMalloc(&P.owner, c->s.N * sizeof(int)));
+    if (!P.counters) CK(cudaMalloc(&P.counters, 4 * sizeof(unsigned)));
+    if (!c->d_count) CK(cudaMalloc(&c->d_count, sizeof(unsigned long long)));
+    const int cap = std::max(4096, 64 * n);
+    if (P.refill_cap < cap) {
+        cudaFree(P.refill_node);
+        cudaFree(P.refill_part);
+        P.refill_node = nullptr;
+        P.refill_part = nullptr;
+        CK(cudaMalloc(&P.refill_node, (size_t)cap * sizeof(uint32_t)));
+        CK(cudaMalloc(&P.refill_part, (size_t)cap * sizeof(int)));
+        P.refill_cap = cap;
+    }
+    const size_t m = 3 * (size_t)std::max(n, 1);
+    CK(cudaMalloc(&P.pos, 8 * m * sizeof(double)));
+    P.vel = P.pos + m; P.omg = P.vel + m; P.force = P.omg + m; P.torque = P.force + m;
+    P.fprev = P.torque + m; P.tprev = P.fprev + m; P.rep = P.tprev + m;
+    CK(cudaMemsetAsync(P.pos, 0, 8 * m * sizeof(double), c->stream));
+    if (n > 0) {
+        CK(cudaMemcpyAsync(P.pos, pos, 3 * (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        if (vel) CK(cudaMemcpyAsync(P.vel, vel, 3 * (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        if (omg) CK(cudaMemcpyAsync(P.omg, omg, 3 * (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    }
+    CK(cudaMemsetAsync(P.counters, 0, 4 * sizeof(unsigned), c->stream));
+    CK(cudaMemsetAsync(P.owner, 0xff, c->s.N * sizeof(int), c->stream));   // -1: fluid
+    P.npart = n;
+    P.R = pp->radius; P.rho_ratio = pp->rho_ratio;
+    P.stf0 = pp->stf0; P.stf1 = pp->stf1; P.stf0_w = pp->stf0_w; P.stf1_w = pp->stf1_w; P.zeta = pp->zeta;
+    c->pp = *pp;
+    c->have_prev = 0;
+    CK(particles_claim(c->s, P, c->stream));
+    c->s.owner = P.owner;
+    c->s.ppos = P.pos; c->s.pvel = P.vel; c->s.pomg = P.omg;
+    c->s.prho = pp->rho_ratio;
+    return sync(c);
+}
+
+int lbm_particles_get(lbm_ctx* c, double* pos, double* vel, double* omg, double* force, double* torque) {
+    if (check_ctx(c)) return LBM_ERR_INVALID_ARG;
+    if (c->P.npart == 0) return fail(LBM_ERR_STATE, "no spheres set");
+    if (int rc = set_device(c)) return rc;
+    const size_t b = 3 * (size_t)c->P.npart * sizeof(double);
+    const double* src[5] = {c->P.pos, c->P.vel, c->P.omg, c->P.force, c->P.torque};
+    double* dst[5] = {pos, vel, omg, force, torque};
+    for (int k = 0; k < 5; ++k)
+        if (dst[k]) CK(cudaMemcpyAsync(dst[k], src[k], b, cudaMemcpyDeviceToHost, c->stream));
+    return sync(c);
+}
+
+int lbm_particle_counts(lbm_ctx* c, int64_t* nsolid, int64_t* nlinks, int64_t* nrefill) {
+    if (check_ctx(c)) return LBM_ERR_INVALID_ARG;
+    if (c->P.npart == 0) {
+        if (nsolid) *nsolid = 0;
+        if (nlinks) *nlinks = 0;
+        if (nrefill) *nrefill = 0;
+        return LBM_OK;
+    }
+    if (int rc = set_device(c)) return rc;
+    unsigned cnt[4];
+    CK(cudaMemcpyAsync(cnt, c->P.counters, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
+    unsigned long long ns = 0;
+    CK(particles_count_solid(c->s, c->P, c->d_count, c->stream));
+    CK(cudaMemcpyAsync(&ns, c->d_count, sizeof(ns), cudaMemcpyDeviceToHost, c->stream));
+    if (int rc = sync(c)) return rc;
+    if (nsolid) *nsolid = (int64_t)ns;
+    if (nlinks) *nlinks = cnt[1];
+    if (nrefill) *nrefill = cnt[0];
     return LBM_OK;
 }
 

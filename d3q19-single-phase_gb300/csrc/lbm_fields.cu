@@ -209,6 +209,21 @@ __global__ void k_macro(DeviceState s, int parity, double* rho, double* ux, doub
     const double F[3] = {(double)s.cd.Fx, (double)s.cd.Fy, (double)s.cd.Fz};
     double d, a, b, c;
     macro_of<double>(f, F, d, a, b, c);
+    const int own = s.owner ? s.owner[gpu_lin(s.g, r.ix, r.iy, r.iz)] : -1;
+    if (own >= 0) {
+        // solid node: rigid-body velocity and rho = rhopart (collision.f90:420-458)
+        const double* X = s.ppos + 3 * own;
+        const double* U = s.pvel + 3 * own;
+        const double* W = s.pomg + 3 * own;
+        auto mi = [](double v, double L) { return v >= 0.5 * L ? v - L : (v < -0.5 * L ? v + L : v); };
+        const double x0 = (r.ix + 0.5) - X[0];
+        const double y0 = mi((r.iy + 0.5) - X[1], (double)s.g.NX);
+        const double z0c = mi((r.iz + 0.5) - X[2], (double)s.g.NY);
+        a = U[0] + (W[1] * z0c - W[2] * y0);
+        b = U[1] + (W[2] * x0 - W[0] * z0c);
+        c = U[2] + (W[0] * y0 - W[1] * x0);
+        d = s.prho;
+    }
     const size_t o = ref_lin(s.g, r.ix, r.iy, r.iz - z0);
     if (rho) rho[o] = d;
     if (ux) ux[o] = a;
@@ -243,6 +258,7 @@ k_profiles(DeviceState s, int parity, double* __restrict__ partial) {
     const uint32_t plane = g.NXY;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < plane; t += gridDim.x * blockDim.x) {
         const int x = t % g.NX, y = t / g.NX;
+        if (s.owner && s.owner[t + plane * (uint32_t)z] >= 0) continue;     // solid node
         R f[Q];
         gather_natural_r<T, R>(s, parity, x, y, z, f);
         R rho, ux, uy, uz;
@@ -285,6 +301,7 @@ k_extrema(DeviceState s, int parity, double* __restrict__ partial) {
     for (uint32_t r = blockIdx.x; r < rows; r += gridDim.x) {
         const int y = (int)(r % (uint32_t)g.NY), z = (int)(r / (uint32_t)g.NY);
         for (int x = threadIdx.x; x < g.NX; x += blockDim.x) {
+            if (s.owner && s.owner[x + g.NX * r] >= 0) continue;            // solid node
             R f[Q];
             gather_natural_r<T, R>(s, parity, x, y, z, f);
             bool finite = true;

@@ -35,6 +35,21 @@ struct Geometry {
     uint32_t NXY;        // NX*NY
 };
 
+// Moving spheres on the device (all FP64 state, 3 values per sphere).
+struct DeviceParticles {
+    int npart;
+    int refill_cap;
+    double R, rho_ratio, stf0, stf1, stf0_w, stf1_w, zeta;
+    double *pos, *vel, *omg;          // centre, velocity, angular velocity
+    double *force, *torque;           // hydrodynamic part of the last step
+    double *fprev, *tprev;            // total force/torque of the previous step
+    double *rep;                      // repulsion of the current step
+    int* owner;                       // per node: sphere id, -1 fluid, -2 pending refill
+    uint32_t* refill_node;
+    int* refill_part;
+    unsigned* counters;               // [0] refills, [1] links, [3] overflow flag
+};
+
 // Everything a step needs; built once per context.
 struct DeviceState {
     int prec;
@@ -46,6 +61,11 @@ struct DeviceState {
     CollideConsts<float> cf;
     int sm_count;        // SMs of the device (persistent grids)
     int use_rows;        // 1: row-pipelined bulk-copy kernels for the step
+    // spheres (owner == nullptr without spheres): fluid masks and the rigid
+    // velocity of solid nodes for the diagnostics and macrovar
+    const int* owner;
+    const double *ppos, *pvel, *pomg;
+    double prho;
 };
 
 // launchers (lbm_step.cu)
@@ -103,6 +123,13 @@ __host__ __device__ inline double uniform_pm1(uint64_t seed, uint64_t key) {
     const uint64_t z = splitmix64(seed * 0xD1B54A32D192ED03ull + key);
     return (double)(z >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
 }
+
+// moving spheres (lbm_particles.cu)
+cudaError_t particles_claim(const DeviceState& s, const DeviceParticles& P, cudaStream_t st);
+cudaError_t particles_after_step(const DeviceState& s, const DeviceParticles& P, int parity, int have_prev,
+                                 cudaStream_t st);
+cudaError_t particles_count_solid(const DeviceState& s, const DeviceParticles& P, unsigned long long* d_out,
+                                  cudaStream_t st);
 
 void channel_velocity_host(int nx, int ny, int nz, double uc, double amp,
                            uint64_t seed, double* ux, double* uy, double* uz);

@@ -1,0 +1,481 @@
+// Moving spheres: geometry, interpolated bounce-back with momentum exchange,
+// Newton-Euler and refilling, run after every fluid step.
+//
+// The reference declares the particle data (links, fill lists, particle state:
+// var_inc.f90:120-150, para.f90:332-379; solid-node velocity in macrovar,
+// collision.f90:420-458) but its particle library is not in the source tree.
+// The algorithm here is this project's own (see the oracle's statement of the
+// same steps):
+//  1. the fluid step collides and streams every node, solid ones included;
+//  2. k_ibb, one CTA per sphere: every link (fluid x_f, direction c_i into the
+//     sphere) gets the population coming back from the wall by quadratic
+//     interpolated bounce-back (Bouzidi, Firdaouss & Lallemand 2001) with the
+//     moving-wall term, read and written through the AA orientation of the
+//     step just taken; the momentum exchanged (Galilean-invariant form, Wen et
+//     al. 2014) is reduced per sphere with warp shuffles into FP64 force and
+//     torque;
+//  3. k_newton, one thread per sphere: soft-sphere repulsion and the FP64
+//     Newton-Euler update (second-order Adams-Bashforth);
+//  4. k_release / k_claim: node ownership follows the new positions; nodes
+//     that leave a sphere are queued;
+//  5. k_refill: queued nodes get the equilibrium at the wall velocity plus the
+//     non-equilibrium part of the fluid neighbour closest to the outward
+//     normal.
+// Geometry decisions (inside tests, q, the refill direction) use explicit
+// round-to-nearest FP64 operations so that they agree bit for bit with the
+// CPU oracle.
+#include <cmath>
+
+#include "lbm_internal.h"
+
+namespace lbm {
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kInvSqrt2 = 0.70710678118654752440;
+constexpr int kPThreads = 256;
+
+__device__ __forceinline__ double dmin_image(double d, double L) {
+    if (d >= 0.5 * L) d = __dsub_rn(d, L);
+    else if (d < -0.5 * L) d = __dadd_rn(d, L);
+    return d;
+}
+
+// offset from the centre of sphere p to the node with reference indices
+// (ix, iy, iz) (0-based)
+__device__ __forceinline__ void offset(const DeviceParticles& P, const Geometry& g, int p, int ix, int iy, int iz,
+                                       double d[3]) {
+    d[0] = __dsub_rn((double)ix + 0.5, P.pos[3 * p + 0]);
+    d[1] = dmin_image(__dsub_rn((double)iy + 0.5, P.pos[3 * p + 1]), (double)g.NX);
+    d[2] = dmin_image(__dsub_rn((double)iz + 0.5, P.pos[3 * p + 2]), (double)g.NY);
+}
+__device__ __forceinline__ double norm2_rn(const double d[3]) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])), __dmul_rn(d[2], d[2]));
+}
+__device__ __forceinline__ bool inside(const double d[3], double R) { return norm2_rn(d) <= __dmul_rn(R, R); }
+
+__device__ __forceinline__ int wrapi(int a, int n) {
+    a %= n;
+    return a < 0 ? a + n : a;
+}
+
+// node-index range of a bounding box along one axis (same rule as the oracle)
+struct Range { int lo, n; };
+__device__ __forceinline__ Range box(double c, double ext, int n, bool periodic) {
+    int a = (int)floor(__dsub_rn(__dsub_rn(c, ext), 0.5));
+    int b = (int)ceil(__dsub_rn(__dadd_rn(c, ext), 0.5));
+    if (periodic) {
+        if (b - a + 1 >= n) { a = 0; b = n - 1; }
+    } else {
+        if (a < 0) a = 0;
+        if (b > n - 1) b = n - 1;
+    }
+    Range r;
+    r.lo = a;
+    r.n = b >= a ? b - a + 1 : 0;
+    return r;
+}
+
+// GPU node index of reference indices (ix wall-normal, iy streamwise, iz spanwise)
+__device__ __forceinline__ uint32_t gnode(const Geometry& g, int ix, int iy, int iz) {
+    return (uint32_t)iy + (uint32_t)g.NX * ((uint32_t)iz + (uint32_t)g.NY * (uint32_t)ix);
+}
+
+template <typename T>
+__device__ __forceinline__ T* plane(const DeviceState& s, int k) {
+    return static_cast<T*>(s.f) + (size_t)k * s.pstride;
+}
+
+// Storage location of the natural post-stream population k at reference node
+// (ix,iy,iz): parity 0 -> slot k there; parity 1 (after an even AA step) ->
+// slot opp(k) at the node - c_k, or slot k there when that is beyond a wall.
+struct Slot { int k; uint32_t n; };
+__device__ __forceinline__ Slot natural_slot(const Geometry& g, int parity, int k, int ix, int iy, int iz) {
+    Slot s;
+    s.k = k;
+    s.n = gnode(g, ix, iy, iz);
+    if (parity) {
+        const int sx = ix - CXf(k);
+        if (sx >= 0 && sx < g.NZ) {
+            s.k = OPPf(k);
+            s.n = gnode(g, sx, wrapi(iy - CYf(k), g.NX), wrapi(iz - CZf(k), g.NY));
+        }
+    }
+    return s;
+}
+template <typename T>
+__device__ __forceinline__ double read_nat(const DeviceState& s, int parity, int k, int ix, int iy, int iz) {
+    const Slot sl = natural_slot(s.g, parity, k, ix, iy, iz);
+    return (double)ld_pop(plane<T>(s, sl.k) + sl.n) * s.cd.invS;
+}
+template <typename T>
+__device__ __forceinline__ void write_nat(const DeviceState& s, int parity, int k, int ix, int iy, int iz, double v) {
+    const Slot sl = natural_slot(s.g, parity, k, ix, iy, iz);
+    T* p = plane<T>(s, sl.k) + sl.n;
+    if constexpr (sizeof(T) == 8) *p = v * s.cd.S;
+    else st_pop(p, (float)(v * s.cd.S));
+}
+
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kPThreads) k_claim(DeviceParticles P, Geometry g, int* owner) {
+    const int p = blockIdx.x;
+    const Range rx = box(P.pos[3 * p], P.R, g.NZ, false);
+    const Range ry = box(P.pos[3 * p + 1], P.R, g.NX, true);
+    const Range rz = box(P.pos[3 * p + 2], P.R, g.NY, true);
+    const int total = rx.n * ry.n * rz.n;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int a = t % rx.n, b = (t / rx.n) % ry.n, c = t / (rx.n * ry.n);
+        const int ix = rx.lo + a, iy = wrapi(ry.lo + b, g.NX), iz = wrapi(rz.lo + c, g.NY);
+        double d[3];
+        offset(P, g, p, ix, iy, iz, d);
+        if (inside(d, P.R)) owner[gnode(g, ix, iy, iz)] = p;
+    }
+}
+
+__global__ void __launch_bounds__(kPThreads) k_release(DeviceParticles P, Geometry g, int* owner) {
+    const int p = blockIdx.x;
+    const double ext = P.R + 1.5;
+    const Range rx = box(P.pos[3 * p], ext, g.NZ, false);
+    const Range ry = box(P.pos[3 * p + 1], ext, g.NX, true);
+    const Range rz = box(P.pos[3 * p + 2], ext, g.NY, true);
+    const int total = rx.n * ry.n * rz.n;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int a = t % rx.n, b = (t / rx.n) % ry.n, c = t / (rx.n * ry.n);
+        const int ix = rx.lo + a, iy = wrapi(ry.lo + b, g.NX), iz = wrapi(rz.lo + c, g.NY);
+        const uint32_t n = gnode(g, ix, iy, iz);
+        if (owner[n] != p) continue;
+        double d[3];
+        offset(P, g, p, ix, iy, iz, d);
+        if (inside(d, P.R)) continue;
+        owner[n] = -2;
+        const unsigned k = atomicAdd(&P.counters[0], 1u);
+        if (k < (unsigned)P.refill_cap) {
+            P.refill_node[k] = n;
+            P.refill_part[k] = p;
+        } else {
+            atomicExch(&P.counters[3], 1u);      // refill list overflow
+        }
+    }
+}
+
+// Interpolated bounce-back on every link of sphere blockIdx.x, after a step
+// that left the populations in orientation `parity`.  RT: link arithmetic
+// (FP64 for FP64 storage, FP32 otherwise; FP64 sums per node and per sphere).
+template <typename T, typename RT>
+__global__ void __launch_bounds__(kPThreads) k_ibb(DeviceState s, DeviceParticles P, int parity) {
+    const Geometry& g = s.g;
+    const int p = blockIdx.x;
+    const double R = P.R;
+    const double* U = P.vel + 3 * p;
+    const double* W = P.omg + 3 * p;
+    const int* owner = P.owner;
+    const double ext = R + 1.5;
+    const Range rx = box(P.pos[3 * p], ext, g.NZ, false);
+    const Range ry = box(P.pos[3 * p + 1], ext, g.NX, true);
+    const Range rz = box(P.pos[3 * p + 2], ext, g.NY, true);
+    const int total = rx.n * ry.n * rz.n;
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    unsigned nl = 0;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int a = t % rx.n, b = (t / rx.n) % ry.n, c = t / (rx.n * ry.n);
+        const int ix = rx.lo + a, iy = wrapi(ry.lo + b, g.NX), iz = wrapi(rz.lo + c, g.NY);
+        if (owner[gnode(g, ix, iy, iz)] != -1) continue;
+        double d[3];
+        offset(P, g, p, ix, iy, iz, d);
+        RT nacc[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll 1
+        for (int i = 1; i < Q; ++i) {
+            const int cx = CXf(i), cy = CYf(i), cz = CZf(i);
+            const int sx = ix + cx;
+            if (sx < 0 || sx >= g.NZ) continue;
+            const int sy = wrapi(iy + cy, g.NX), sz = wrapi(iz + cz, g.NY);
+            if (owner[gnode(g, sx, sy, sz)] != p) continue;
+            ++nl;
+            // boundary-link fraction q (FP64 geometry, as the oracle)
+            const double qa = (double)(cx * cx + cy * cy + cz * cz);
+            const double qb = __dadd_rn(__dadd_rn(d[0] * cx, d[1] * cy), d[2] * cz);
+            const double qc = __dsub_rn(norm2_rn(d), __dmul_rn(R, R));
+            double disc = __dsub_rn(__dmul_rn(qb, qb), __dmul_rn(qa, qc));
+            if (disc < 0.0) disc = 0.0;
+            double qd = __ddiv_rn(__dsub_rn(-qb, __dsqrt_rn(disc)), qa);
+            if (qd < 1e-6) qd = 1e-6;
+            if (qd > 1.0) qd = 1.0;
+            const RT q = (RT)qd;
+            // wall point relative to the centre and wall velocity
+            const RT r0 = (RT)(d[0] + qd * cx), r1 = (RT)(d[1] + qd * cy), r2 = (RT)(d[2] + qd * cz);
+            const RT uw0 = (RT)U[0] + ((RT)W[1] * r2 - (RT)W[2] * r1);
+            const RT uw1 = (RT)U[1] + ((RT)W[2] * r0 - (RT)W[0] * r2);
+            const RT uw2 = (RT)U[2] + ((RT)W[0] * r1 - (RT)W[1] * r0);
+            const RT cu = (cx * uw0 + cy * uw1) + cz * uw2;
+            const RT mw = RT(-6.0 * weight(i)) * cu;
+            const int ib = OPPf(i);
+            // stencil x_f - c_i, x_f - 2 c_i
+            const int ax = ix - cx, bx = ix - 2 * cx;
+            bool ok1 = false, ok2 = false;
+            int ay = 0, az = 0, by = 0, bz = 0;
+            if (ax >= 0 && ax < g.NZ) {
+                ay = wrapi(iy - cy, g.NX); az = wrapi(iz - cz, g.NY);
+                ok1 = owner[gnode(g, ax, ay, az)] == -1;
+            }
+            if (ok1 && bx >= 0 && bx < g.NZ) {
+                by = wrapi(iy - 2 * cy, g.NX); bz = wrapi(iz - 2 * cz, g.NY);
+                ok2 = owner[gnode(g, bx, by, bz)] == -1;
+            }
+            const RT A = (RT)read_nat<T>(s, parity, i, sx, sy, sz);
+            RT fn;
+            if (q < RT(0.5)) {
+                if (ok2) {
+                    const RT B = (RT)read_nat<T>(s, parity, i, ix, iy, iz);
+                    const RT C = (RT)read_nat<T>(s, parity, i, ax, ay, az);
+                    fn = q * (RT(1) + RT(2) * q) * A + (RT(1) - RT(4) * q * q) * B + q * (RT(2) * q - RT(1)) * C + mw;
+                } else if (ok1) {
+                    const RT B = (RT)read_nat<T>(s, parity, i, ix, iy, iz);
+                    fn = RT(2) * q * A + (RT(1) - RT(2) * q) * B + mw;
+                } else {
+                    fn = A + mw;
+                }
+            } else {
+                if (ok2) {
+                    const RT D = (RT)read_nat<T>(s, parity, ib, ax, ay, az);
+                    const RT E = (RT)read_nat<T>(s, parity, ib, bx, by, bz);
+                    const RT k = RT(1) / (q * (RT(2) * q + RT(1)));
+                    fn = k * A + (RT(2) * q - RT(1)) / q * D - (RT(2) * q - RT(1)) / (RT(2) * q + RT(1)) * E + k * mw;
+                } else if (ok1) {
+                    const RT D = (RT)read_nat<T>(s, parity, ib, ax, ay, az);
+                    fn = (A + mw) / (RT(2) * q) + (RT(2) * q - RT(1)) / (RT(2) * q) * D;
+                } else {
+                    fn = A + mw;
+                }
+            }
+            write_nat<T>(s, parity, ib, ix, iy, iz, (double)fn);
+            // Galilean-invariant momentum exchange
+            const RT sA = A + fn, dA = fn - A;
+            const RT p0 = cx * sA + uw0 * dA, p1 = cy * sA + uw1 * dA, p2 = cz * sA + uw2 * dA;
+            nacc[0] += p0; nacc[1] += p1; nacc[2] += p2;
+            nacc[3] += r1 * p2 - r2 * p1;
+            nacc[4] += r2 * p0 - r0 * p2;
+            nacc[5] += r0 * p1 - r1 * p0;
+        }
+#pragma unroll
+        for (int k = 0; k < 6; ++k) acc[k] += (double)nacc[k];
+    }
+    // per-sphere FP64 reduction: warp shuffles, then across warps
+    __shared__ double sh[6][kPThreads / 32];
+    __shared__ unsigned shn[kPThreads / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        double v = acc[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) sh[k][wid] = v;
+    }
+    for (int o = 16; o > 0; o >>= 1) nl += __shfl_down_sync(0xffffffffu, nl, o);
+    if (lane == 0) shn[wid] = nl;
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        double v = 0.0;
+        for (int w = 0; w < kPThreads / 32; ++w) v += sh[threadIdx.x][w];
+        if (threadIdx.x < 3) P.force[3 * p + threadIdx.x] = v;
+        else P.torque[3 * p + threadIdx.x - 3] = v;
+    }
+    if (threadIdx.x == 0) {
+        unsigned n = 0;
+        for (int w = 0; w < kPThreads / 32; ++w) n += shn[w];
+        atomicAdd(&P.counters[1], n);
+    }
+}
+
+__device__ __forceinline__ double repulse(double h, double zeta, double k0, double k1) {
+    if (h >= zeta) return 0.0;
+    const double a = __ddiv_rn(__dsub_rn(zeta, h), zeta);
+    double f = __dmul_rn(__dmul_rn(k0, a), a);
+    if (h < 0.0) f = __dadd_rn(f, __ddiv_rn(__dmul_rn(k1, -h), zeta));
+    return f;
+}
+
+// Soft-sphere repulsion gathered per sphere in index order (old positions).
+__global__ void k_repulsion(DeviceParticles P, Geometry g) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= P.npart) return;
+    const double R = P.R;
+    const double L1 = (double)g.NX, L2 = (double)g.NY;
+    double rep[3] = {0.0, 0.0, 0.0};
+    const double xs0 = P.pos[3 * s], xs1 = P.pos[3 * s + 1], xs2 = P.pos[3 * s + 2];
+    for (int t = 0; t < P.npart; ++t) {
+        if (t == s) continue;
+        const double d0 = __dsub_rn(P.pos[3 * t], xs0);
+        const double d1 = dmin_image(__dsub_rn(P.pos[3 * t + 1], xs1), L1);
+        const double d2 = dmin_image(__dsub_rn(P.pos[3 * t + 2], xs2), L2);
+        const double dd[3] = {d0, d1, d2};
+        const double dist = __dsqrt_rn(norm2_rn(dd));
+        const double fm = repulse(__dsub_rn(dist, 2.0 * R), P.zeta, P.stf0, P.stf1);
+        if (fm != 0.0 && dist > 0.0) {
+            rep[0] = __dsub_rn(rep[0], __ddiv_rn(__dmul_rn(fm, d0), dist));
+            rep[1] = __dsub_rn(rep[1], __ddiv_rn(__dmul_rn(fm, d1), dist));
+            rep[2] = __dsub_rn(rep[2], __ddiv_rn(__dmul_rn(fm, d2), dist));
+        }
+    }
+    const double hl = __dsub_rn(xs0, R), hu = __dsub_rn(__dsub_rn((double)g.NZ, xs0), R);
+    rep[0] = __dadd_rn(rep[0], repulse(hl, P.zeta, P.stf0_w, P.stf1_w));
+    rep[0] = __dsub_rn(rep[0], repulse(hu, P.zeta, P.stf0_w, P.stf1_w));
+    P.rep[3 * s] = rep[0]; P.rep[3 * s + 1] = rep[1]; P.rep[3 * s + 2] = rep[2];
+}
+
+// Newton-Euler update (second-order Adams-Bashforth, FP64); the body force
+// that drives the fluid also acts on the sphere volume.
+__global__ void k_newton(DeviceParticles P, Geometry g, double bfx, double bfy, double bfz, int have_prev) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= P.npart) return;
+    const double R = P.R;
+    const double L1 = (double)g.NX, L2 = (double)g.NY;
+    const double vol = __dmul_rn(__dmul_rn(__dmul_rn(4.0 / 3.0 * kPi, R), R), R);
+    const double m = __dmul_rn(P.rho_ratio, vol);
+    const double I = __dmul_rn(__dmul_rn(__dmul_rn(0.4, m), R), R);
+    const double bf[3] = {bfx, bfy, bfz};
+    for (int a = 0; a < 3; ++a) {
+        const double Ft = __dadd_rn(__dadd_rn(P.force[3 * s + a], P.rep[3 * s + a]), __dmul_rn(bf[a], vol));
+        const double Tt = P.torque[3 * s + a];
+        const double fp = have_prev ? P.fprev[3 * s + a] : Ft;
+        const double tp = have_prev ? P.tprev[3 * s + a] : Tt;
+        const double u0 = P.vel[3 * s + a];
+        const double u1 = __dadd_rn(u0, __ddiv_rn(__dsub_rn(__dmul_rn(1.5, Ft), __dmul_rn(0.5, fp)), m));
+        P.vel[3 * s + a] = u1;
+        P.omg[3 * s + a] = __dadd_rn(P.omg[3 * s + a], __ddiv_rn(__dsub_rn(__dmul_rn(1.5, Tt), __dmul_rn(0.5, tp)), I));
+        P.pos[3 * s + a] = __dadd_rn(P.pos[3 * s + a], __dmul_rn(0.5, __dadd_rn(u0, u1)));
+        P.fprev[3 * s + a] = Ft;
+        P.tprev[3 * s + a] = Tt;
+    }
+    double y = P.pos[3 * s + 1], z = P.pos[3 * s + 2];
+    if (y >= L1) y = __dsub_rn(y, L1);
+    else if (y < 0.0) y = __dadd_rn(y, L1);
+    if (z >= L2) z = __dsub_rn(z, L2);
+    else if (z < 0.0) z = __dadd_rn(z, L2);
+    P.pos[3 * s + 1] = y;
+    P.pos[3 * s + 2] = z;
+}
+
+__device__ __forceinline__ void feq_dev(double rho, double ux, double uy, double uz, double* fe) {
+    const double usqr = __dmul_rn(1.5, __dadd_rn(__dadd_rn(__dmul_rn(ux, ux), __dmul_rn(uy, uy)), __dmul_rn(uz, uz)));
+    fe[0] = __dmul_rn(W0, __dsub_rn(rho, usqr));
+#pragma unroll
+    for (int i = 1; i < Q; ++i) {
+        const double G = __dadd_rn(__dadd_rn(CXf(i) * ux, CYf(i) * uy), CZf(i) * uz);
+        fe[i] = __dmul_rn(weight(i), __dsub_rn(__dadd_rn(__dadd_rn(rho, __dmul_rn(3.0, G)), __dmul_rn(__dmul_rn(4.5, G), G)), usqr));
+    }
+}
+
+// Refilling of nodes queued by k_release that are still fluid (-2).
+template <typename T>
+__global__ void k_refill(DeviceState s, DeviceParticles P, int parity) {
+    const unsigned k = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned cnt = min(P.counters[0], (unsigned)P.refill_cap);
+    if (k >= cnt) return;
+    const Geometry& g = s.g;
+    const uint32_t n = P.refill_node[k];
+    const int* owner = P.owner;
+    if (owner[n] != -2) return;
+    const int p = P.refill_part[k];
+    const int iy = (int)(n % (uint32_t)g.NX);
+    const int iz = (int)((n / (uint32_t)g.NX) % (uint32_t)g.NY);
+    const int ix = (int)(n / g.NXY);
+    double d[3];
+    offset(P, g, p, ix, iy, iz, d);
+    int best = -1, bx = 0, by = 0, bz = 0;
+    double bs = -1e300;
+    for (int i = 1; i < Q; ++i) {
+        const int sx = ix + CXf(i);
+        if (sx < 0 || sx >= g.NZ) continue;
+        const int sy = wrapi(iy + CYf(i), g.NX), sz = wrapi(iz + CZf(i), g.NY);
+        if (owner[gnode(g, sx, sy, sz)] != -1) continue;
+        double sc = __dadd_rn(__dadd_rn(d[0] * CXf(i), d[1] * CYf(i)), d[2] * CZf(i));
+        if (i >= 7) sc = __dmul_rn(sc, kInvSqrt2);
+        if (sc > bs) { bs = sc; best = i; bx = sx; by = sy; bz = sz; }
+    }
+    const double* U = P.vel + 3 * p;
+    const double* W = P.omg + 3 * p;
+    const double uw0 = __dadd_rn(U[0], __dsub_rn(__dmul_rn(W[1], d[2]), __dmul_rn(W[2], d[1])));
+    const double uw1 = __dadd_rn(U[1], __dsub_rn(__dmul_rn(W[2], d[0]), __dmul_rn(W[0], d[2])));
+    const double uw2 = __dadd_rn(U[2], __dsub_rn(__dmul_rn(W[0], d[1]), __dmul_rn(W[1], d[0])));
+    double fe[Q];
+    if (best < 0) {
+        feq_dev(0.0, uw0, uw1, uw2, fe);
+        for (int i = 0; i < Q; ++i) write_nat<T>(s, parity, i, ix, iy, iz, fe[i]);
+        return;
+    }
+    double gq[Q];
+    double r = 0.0, a = 0.0, b = 0.0, c = 0.0;
+    for (int i = 0; i < Q; ++i) {
+        gq[i] = read_nat<T>(s, parity, i, bx, by, bz);
+        r = __dadd_rn(r, gq[i]);
+        a = __dadd_rn(a, CXf(i) * gq[i]);
+        b = __dadd_rn(b, CYf(i) * gq[i]);
+        c = __dadd_rn(c, CZf(i) * gq[i]);
+    }
+    a = __dadd_rn(a, s.cd.Fx / 2.0);
+    b = __dadd_rn(b, s.cd.Fy / 2.0);
+    c = __dadd_rn(c, s.cd.Fz / 2.0);
+    double fn[Q];
+    feq_dev(r, a, b, c, fn);
+    feq_dev(r, uw0, uw1, uw2, fe);
+    for (int i = 0; i < Q; ++i) write_nat<T>(s, parity, i, ix, iy, iz, __dadd_rn(fe[i], __dsub_rn(gq[i], fn[i])));
+}
+
+__global__ void k_refill_done(DeviceParticles P) {
+    const unsigned k = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned cnt = min(P.counters[0], (unsigned)P.refill_cap);
+    if (k >= cnt) return;
+    const uint32_t n = P.refill_node[k];
+    if (P.owner[n] == -2) P.owner[n] = -1;
+}
+
+__global__ void k_count_solid(const int* owner, size_t N, unsigned long long* out) {
+    unsigned long long c = 0;
+    for (size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x; n < N; n += (size_t)gridDim.x * blockDim.x)
+        c += owner[n] >= 0;
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, c);
+}
+
+}  // namespace
+
+cudaError_t particles_claim(const DeviceState& s, const DeviceParticles& P, cudaStream_t st) {
+    if (P.npart == 0) return cudaSuccess;
+    k_claim<<<P.npart, kPThreads, 0, st>>>(P, s.g, P.owner);
+    return cudaGetLastError();
+}
+
+// Everything that follows a fluid step when spheres are present.
+cudaError_t particles_after_step(const DeviceState& s, const DeviceParticles& P, int parity, int have_prev,
+                                 cudaStream_t st) {
+    if (P.npart == 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(P.counters, 0, 2 * sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    switch (s.prec) {
+        case LBM_PREC_FP64: k_ibb<double, double><<<P.npart, kPThreads, 0, st>>>(s, P, parity); break;
+        case LBM_PREC_FP32: k_ibb<float, float><<<P.npart, kPThreads, 0, st>>>(s, P, parity); break;
+        default: k_ibb<__half, float><<<P.npart, kPThreads, 0, st>>>(s, P, parity); break;
+    }
+    k_repulsion<<<(P.npart + 127) / 128, 128, 0, st>>>(P, s.g);
+    k_newton<<<(P.npart + 127) / 128, 128, 0, st>>>(P, s.g, s.cd.Fx, s.cd.Fy, s.cd.Fz, have_prev);
+    k_release<<<P.npart, kPThreads, 0, st>>>(P, s.g, P.owner);
+    k_claim<<<P.npart, kPThreads, 0, st>>>(P, s.g, P.owner);
+    const unsigned nb = (unsigned)((P.refill_cap + 255) / 256);
+    switch (s.prec) {
+        case LBM_PREC_FP64: k_refill<double><<<nb, 256, 0, st>>>(s, P, parity); break;
+        case LBM_PREC_FP32: k_refill<float><<<nb, 256, 0, st>>>(s, P, parity); break;
+        default: k_refill<__half><<<nb, 256, 0, st>>>(s, P, parity); break;
+    }
+    k_refill_done<<<nb, 256, 0, st>>>(P);
+    return cudaGetLastError();
+}
+
+cudaError_t particles_count_solid(const DeviceState& s, const DeviceParticles& P, unsigned long long* d_out,
+                                  cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(d_out, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
+    k_count_solid<<<1024, 256, 0, st>>>(P.owner, s.N, d_out);
+    return cudaGetLastError();
+}
+
+}  // namespace lbm

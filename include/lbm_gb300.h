@@ -225,6 +225,48 @@ int lbm_save_flow(lbm_ctx* ctx, const char* path, int32_t kind,
 int lbm_load_flow(lbm_ctx* ctx, const char* path, int32_t kind,
                   int32_t* ints);
 
+/* ---- moving spheres ------------------------------------------------------
+ * The reference declares particle state, links and fill lists
+ * (var_inc.f90:120-150, para.f90:332-379, macrovar's solid branch
+ * collision.f90:420-458) but ships no particle algorithm.  With spheres set,
+ * every lbm_step also does: interpolated bounce-back (quadratic Bouzidi,
+ * moving wall) and Galilean-invariant momentum exchange on every boundary
+ * link, soft-sphere repulsion (sphere-sphere and sphere-wall), the FP64
+ * Newton-Euler update (second-order Adams-Bashforth), the geometry update and
+ * the refilling of uncovered nodes.  Positions are in reference axes with node
+ * (ix,iy,iz) (1-based) at (ix-1/2, iy-1/2, iz-1/2), as in macrovar. */
+typedef struct lbm_particle_params {
+    int32_t npart;            /* number of spheres (npart, var_inc.f90:66)     */
+    int32_t flags;
+    double  radius;           /* rad (var_inc.f90:67)                          */
+    double  rho_ratio;        /* rhopart / rho0                                */
+    double  stf0, stf1;       /* sphere-sphere repulsion (para.f90:357-358)    */
+    double  stf0_w, stf1_w;   /* sphere-wall repulsion (para.f90:359-360)      */
+    double  zeta;             /* repulsion range, lattice units                */
+} lbm_particle_params;
+
+/* Defaults of para.f90:339-379 for npart spheres of the given radius. */
+int lbm_particle_params_init(lbm_particle_params* pp, int32_t npart, double radius,
+                             double rho_ratio);
+/* Seeded random placement (counter-based generator): centres uniform in the
+ * domain, at least `gap` lattice units between sphere surfaces (periodic in
+ * y and z) and `wall_gap` between a surface and a wall.  pos: 3*npart. */
+int lbm_particles_place(int32_t nx, int32_t ny, int32_t nz, int32_t npart,
+                        double radius, double gap, double wall_gap,
+                        uint64_t seed, double* pos);
+/* Attach spheres to a context (allocates the node ownership array and the
+ * particle state on the device) and mark the solid nodes.  vel/omg may be
+ * NULL (zero). */
+int lbm_particles_set(lbm_ctx* ctx, const lbm_particle_params* pp,
+                      const double* pos, const double* vel, const double* omg);
+/* Particle state after the last step; any pointer may be NULL.  force and
+ * torque are the hydrodynamic (momentum-exchange) parts of the last step. */
+int lbm_particles_get(lbm_ctx* ctx, double* pos, double* vel, double* omg,
+                      double* force, double* torque);
+/* Solid node count, boundary links and refilled nodes of the last step. */
+int lbm_particle_counts(lbm_ctx* ctx, int64_t* nsolid, int64_t* nlinks,
+                        int64_t* nrefill);
+
 #ifdef __cplusplus
 }
 #endif

@@ -478,3 +478,367 @@ void orc_channel_velocity(int nx, int ny, int nz, double uc, double amp, uint64_
                 uz[n] = a * upm1(seed, 3 * lin + 2);
             }
 }
+
+/* =========================================================================
+ * Moving spheres.  The reference declares links, fill lists and particle
+ * state (var_inc.f90:120-150, para.f90:332-379, solid-node velocity in
+ * macrovar collision.f90:420-458) but ships no algorithm; the
+ * algorithm below is the project's own design, restated on the CPU as the
+ * checker of the GPU kernels:
+ *   - geometry: node (ix,iy,iz) (0-based) sits at (ix+1/2, iy+1/2, iz+1/2);
+ *     it is solid for sphere p when |r - X_p|^2 <= R^2 (minimal image in the
+ *     periodic y and z);
+ *   - link (x_f, i): fluid x_f with x_f + c_i inside sphere p; q in (0,1] is
+ *     the fraction of c_i from x_f to the surface;
+ *   - interpolated bounce-back after streaming: quadratic Bouzidi,
+ *     Firdaouss & Lallemand (2001) with the moving-wall term
+ *     -6 w_i c_i.u_w, falling back to linear, then to simple bounce-back,
+ *     when the stencil leaves the fluid or the domain;
+ *   - momentum exchange in the Galilean-invariant form of Wen et al. (2014),
+ *     on the stored deviations (the rest-state term 2 w_i rho0 c_i, a pure
+ *     geometry sum over the surface, is left out);
+ *   - soft-sphere repulsion between spheres and from the walls within zeta,
+ *     magnitude stf0 ((zeta-h)/zeta)^2 + stf1 (-h)/zeta for overlap, with the
+ *     reference's constants (para.f90:357-360);
+ *   - Newton-Euler in FP64 with second-order Adams-Bashforth; the body force
+ *     that drives the fluid also acts on the sphere volume;
+ *   - refilling of uncovered nodes: equilibrium at the local wall velocity
+ *     plus the non-equilibrium part of the fluid neighbour closest to the
+ *     outward normal (equilibrium + non-equilibrium extrapolation).
+ * ========================================================================= */
+
+static double min_image(double d, double L) {
+    if (d >= 0.5 * L) d -= L;
+    else if (d < -0.5 * L) d += L;
+    return d;
+}
+
+/* offset from sphere center to node (ix,iy,iz) and the inside test */
+static void node_offset(const orc_particles* P, int p, int ix, int iy, int iz, int ny, int nz, double d[3]) {
+    d[0] = ((double)ix + 0.5) - P->pos[3 * p + 0];
+    d[1] = min_image(((double)iy + 0.5) - P->pos[3 * p + 1], (double)ny);
+    d[2] = min_image(((double)iz + 0.5) - P->pos[3 * p + 2], (double)nz);
+}
+static int inside_d(const double d[3], double R) {
+    return (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2] <= R * R;
+}
+
+/* bounding-box range along one axis: [lo, hi] of node indices, periodic or not;
+ * a periodic range that would cover the whole axis is returned as [0, n-1] */
+static void box_range(double c, double ext, int n, int periodic, int* lo, int* hi) {
+    int a = (int)floor(c - ext - 0.5), b = (int)ceil(c + ext - 0.5);
+    if (periodic) {
+        if (b - a + 1 >= n) { a = 0; b = n - 1; }
+    } else {
+        if (a < 0) a = 0;
+        if (b > n - 1) b = n - 1;
+    }
+    *lo = a; *hi = b;
+}
+static int wrapi(int a, int n) { a %= n; return a < 0 ? a + n : a; }
+
+void orc_mark_solid(const orc_particles* P, int nx, int ny, int nz, int* owner) {
+    const size_t N = (size_t)nx * ny * nz;
+    for (size_t n = 0; n < N; ++n) owner[n] = -1;
+    for (int p = 0; p < P->npart; ++p) {
+        int x0, x1, y0, y1, z0, z1;
+        box_range(P->pos[3 * p], P->radius, nx, 0, &x0, &x1);
+        box_range(P->pos[3 * p + 1], P->radius, ny, 1, &y0, &y1);
+        box_range(P->pos[3 * p + 2], P->radius, nz, 1, &z0, &z1);
+        for (int zz = z0; zz <= z1; ++zz)
+            for (int yy = y0; yy <= y1; ++yy)
+                for (int ix = x0; ix <= x1; ++ix) {
+                    const int iy = wrapi(yy, ny), iz = wrapi(zz, nz);
+                    double d[3];
+                    node_offset(P, p, ix, iy, iz, ny, nz, d);
+                    if (inside_d(d, P->radius)) owner[NODE(ix, iy, iz)] = p;
+                }
+    }
+}
+
+/* incompressible deviation equilibrium (initial.f90:26-44 at density rho) */
+static void feq_dev(double rho, double ux, double uy, double uz, double* fe) {
+    const double usqr = 1.5 * ((ux * ux + uy * uy) + uz * uz);
+    fe[0] = weight(0) * (rho - usqr);
+    for (int i = 1; i < Q; ++i) {
+        const double G = (CX[i] * ux + CY[i] * uy) + CZ[i] * uz;
+        fe[i] = weight(i) * (((rho + 3.0 * G) + (4.5 * G) * G) - usqr);
+    }
+}
+
+static double link_q(const double d[3], int i, double R) {
+    const double a = (double)(CX[i] * CX[i] + CY[i] * CY[i] + CZ[i] * CZ[i]);
+    const double b = (d[0] * CX[i] + d[1] * CY[i]) + d[2] * CZ[i];
+    const double c = ((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]) - R * R;
+    double disc = b * b - a * c;
+    if (disc < 0.0) disc = 0.0;
+    double q = (-b - sqrt(disc)) / a;
+    if (q < 1e-6) q = 1e-6;
+    if (q > 1.0) q = 1.0;
+    return q;
+}
+
+/* Interpolated bounce-back for every link of every sphere on natural
+ * post-stream populations F; accumulates force and torque. */
+static int ibb_pass(const orc_params* p, orc_particles* P, double* F, int nx, int ny, int nz, const int* owner) {
+    int nl = 0;
+    const double R = P->radius;
+    for (int s = 0; s < P->npart; ++s) {
+        double fx = 0, fy = 0, fz = 0, tx = 0, ty = 0, tz = 0;
+        const double* U = P->vel + 3 * s;
+        const double* W = P->omg + 3 * s;
+        int x0, x1, y0, y1, z0, z1;
+        box_range(P->pos[3 * s], R + 1.5, nx, 0, &x0, &x1);
+        box_range(P->pos[3 * s + 1], R + 1.5, ny, 1, &y0, &y1);
+        box_range(P->pos[3 * s + 2], R + 1.5, nz, 1, &z0, &z1);
+        for (int zz = z0; zz <= z1; ++zz)
+            for (int yy = y0; yy <= y1; ++yy)
+                for (int ix = x0; ix <= x1; ++ix) {
+                    const int iy = wrapi(yy, ny), iz = wrapi(zz, nz);
+                    const size_t xf = NODE(ix, iy, iz);
+                    if (owner[xf] != -1) continue;
+                    double d[3];
+                    node_offset(P, s, ix, iy, iz, ny, nz, d);
+                    for (int i = 1; i < Q; ++i) {
+                        const int sx = ix + CX[i];
+                        if (sx < 0 || sx >= nx) continue;
+                        const size_t ys = NODE(sx, wrapi(iy + CY[i], ny), wrapi(iz + CZ[i], nz));
+                        if (owner[ys] != s) continue;
+                        ++nl;
+                        const double q = link_q(d, i, R);
+                        const double r0 = d[0] + q * CX[i], r1 = d[1] + q * CY[i], r2 = d[2] + q * CZ[i];
+                        const double uw0 = U[0] + (W[1] * r2 - W[2] * r1);
+                        const double uw1 = U[1] + (W[2] * r0 - W[0] * r2);
+                        const double uw2 = U[2] + (W[0] * r1 - W[1] * r0);
+                        const double cu = (CX[i] * uw0 + CY[i] * uw1) + CZ[i] * uw2;
+                        const double mw = -6.0 * weight(i) * cu;
+                        const int ib = OPP[i];
+                        /* stencil nodes x_f - c_i, x_f - 2 c_i */
+                        const int ax = ix - CX[i], bx = ix - 2 * CX[i];
+                        int ok1 = 0, ok2 = 0;
+                        size_t n1 = 0, n2 = 0;
+                        if (ax >= 0 && ax < nx) {
+                            n1 = NODE(ax, wrapi(iy - CY[i], ny), wrapi(iz - CZ[i], nz));
+                            ok1 = owner[n1] == -1;
+                        }
+                        if (ok1 && bx >= 0 && bx < nx) {
+                            n2 = NODE(bx, wrapi(iy - 2 * CY[i], ny), wrapi(iz - 2 * CZ[i], nz));
+                            ok2 = owner[n2] == -1;
+                        }
+                        const double A = F[(size_t)i + Q * ys];
+                        double fn;
+                        if (q < 0.5) {
+                            if (ok2) {
+                                const double B = F[(size_t)i + Q * xf], C = F[(size_t)i + Q * n1];
+                                fn = q * (1.0 + 2.0 * q) * A + (1.0 - 4.0 * q * q) * B + q * (2.0 * q - 1.0) * C + mw;
+                            } else if (ok1) {
+                                const double B = F[(size_t)i + Q * xf];
+                                fn = 2.0 * q * A + (1.0 - 2.0 * q) * B + mw;
+                            } else {
+                                fn = A + mw;
+                            }
+                        } else {
+                            if (ok2) {
+                                const double D = F[(size_t)ib + Q * n1], E = F[(size_t)ib + Q * n2];
+                                const double k = 1.0 / (q * (2.0 * q + 1.0));
+                                fn = k * A + (2.0 * q - 1.0) / q * D - (2.0 * q - 1.0) / (2.0 * q + 1.0) * E + k * mw;
+                            } else if (ok1) {
+                                const double D = F[(size_t)ib + Q * n1];
+                                fn = (A + mw) / (2.0 * q) + (2.0 * q - 1.0) / (2.0 * q) * D;
+                            } else {
+                                fn = A + mw;
+                            }
+                        }
+                        F[(size_t)ib + Q * xf] = fn;
+                        /* Galilean-invariant momentum exchange */
+                        const double sA = A + fn, dA = fn - A;
+                        const double p0 = CX[i] * sA + uw0 * dA, p1 = CY[i] * sA + uw1 * dA, p2 = CZ[i] * sA + uw2 * dA;
+                        fx += p0; fy += p1; fz += p2;
+                        tx += r1 * p2 - r2 * p1;
+                        ty += r2 * p0 - r0 * p2;
+                        tz += r0 * p1 - r1 * p0;
+                    }
+                }
+        P->force[3 * s] = fx; P->force[3 * s + 1] = fy; P->force[3 * s + 2] = fz;
+        P->torque[3 * s] = tx; P->torque[3 * s + 1] = ty; P->torque[3 * s + 2] = tz;
+    }
+    (void)p;
+    return nl;
+}
+
+static double repulse(double h, double zeta, double k0, double k1) {
+    if (h >= zeta) return 0.0;
+    const double a = (zeta - h) / zeta;
+    double f = k0 * a * a;
+    if (h < 0.0) f += k1 * (-h) / zeta;
+    return f;
+}
+
+/* soft-sphere repulsion, gathered per sphere in index order */
+static void repulsion(const orc_particles* P, int nx, int ny, int nz, int s, double out[3]) {
+    const double R = P->radius;
+    out[0] = out[1] = out[2] = 0.0;
+    for (int t = 0; t < P->npart; ++t) {
+        if (t == s) continue;
+        const double d0 = P->pos[3 * t] - P->pos[3 * s];
+        const double d1 = min_image(P->pos[3 * t + 1] - P->pos[3 * s + 1], (double)ny);
+        const double d2 = min_image(P->pos[3 * t + 2] - P->pos[3 * s + 2], (double)nz);
+        const double dist = sqrt((d0 * d0 + d1 * d1) + d2 * d2);
+        const double fm = repulse(dist - 2.0 * R, P->zeta, P->stf0, P->stf1);
+        if (fm != 0.0 && dist > 0.0) {
+            out[0] -= fm * d0 / dist; out[1] -= fm * d1 / dist; out[2] -= fm * d2 / dist;
+        }
+    }
+    const double hl = P->pos[3 * s] - R, hu = (double)nx - P->pos[3 * s] - R;
+    out[0] += repulse(hl, P->zeta, P->stf0_w, P->stf1_w);
+    out[0] -= repulse(hu, P->zeta, P->stf0_w, P->stf1_w);
+}
+
+static void newton_euler(const orc_params* p, orc_particles* P, int nx, int ny, int nz) {
+    const double R = P->radius;
+    const double vol = 4.0 / 3.0 * 3.14159265358979323846 * R * R * R;
+    const double m = P->rho_ratio * vol, I = 0.4 * m * R * R;
+    double* rep = (double*)malloc(sizeof(double) * 3 * (size_t)P->npart);
+    for (int s = 0; s < P->npart; ++s) repulsion(P, nx, ny, nz, s, rep + 3 * s);
+    for (int s = 0; s < P->npart; ++s) {
+        double Ft[3], Tt[3];
+        for (int a = 0; a < 3; ++a) {
+            Ft[a] = P->force[3 * s + a] + rep[3 * s + a] + p->force[a] * vol;
+            Tt[a] = P->torque[3 * s + a];
+        }
+        if (!P->have_prev)
+            for (int a = 0; a < 3; ++a) { P->force_prev[3 * s + a] = Ft[a]; P->torque_prev[3 * s + a] = Tt[a]; }
+        for (int a = 0; a < 3; ++a) {
+            const double u0 = P->vel[3 * s + a];
+            const double u1 = u0 + (1.5 * Ft[a] - 0.5 * P->force_prev[3 * s + a]) / m;
+            P->vel[3 * s + a] = u1;
+            P->omg[3 * s + a] += (1.5 * Tt[a] - 0.5 * P->torque_prev[3 * s + a]) / I;
+            P->pos[3 * s + a] += 0.5 * (u0 + u1);
+            P->force_prev[3 * s + a] = Ft[a];
+            P->torque_prev[3 * s + a] = Tt[a];
+        }
+        const double L1 = (double)ny, L2 = (double)nz;
+        if (P->pos[3 * s + 1] >= L1) P->pos[3 * s + 1] -= L1;
+        else if (P->pos[3 * s + 1] < 0.0) P->pos[3 * s + 1] += L1;
+        if (P->pos[3 * s + 2] >= L2) P->pos[3 * s + 2] -= L2;
+        else if (P->pos[3 * s + 2] < 0.0) P->pos[3 * s + 2] += L2;
+    }
+    P->have_prev = 1;
+    free(rep);
+}
+
+static const double INV_SQRT2 = 0.70710678118654752440;
+
+/* geometry update to the new positions and refilling of uncovered nodes */
+static int regeometry(const orc_params* p, orc_particles* P, double* F, int nx, int ny, int nz, int* owner) {
+    const double R = P->radius;
+    size_t cap = 1024, cnt = 0;
+    size_t* list = (size_t*)malloc(cap * sizeof(size_t));
+    int* lpart = (int*)malloc(cap * sizeof(int));
+    /* release: nodes that leave their sphere become pending (-2) */
+    for (int s = 0; s < P->npart; ++s) {
+        int x0, x1, y0, y1, z0, z1;
+        box_range(P->pos[3 * s], R + 1.5, nx, 0, &x0, &x1);
+        box_range(P->pos[3 * s + 1], R + 1.5, ny, 1, &y0, &y1);
+        box_range(P->pos[3 * s + 2], R + 1.5, nz, 1, &z0, &z1);
+        for (int zz = z0; zz <= z1; ++zz)
+            for (int yy = y0; yy <= y1; ++yy)
+                for (int ix = x0; ix <= x1; ++ix) {
+                    const int iy = wrapi(yy, ny), iz = wrapi(zz, nz);
+                    const size_t n = NODE(ix, iy, iz);
+                    if (owner[n] != s) continue;
+                    double d[3];
+                    node_offset(P, s, ix, iy, iz, ny, nz, d);
+                    if (inside_d(d, R)) continue;
+                    owner[n] = -2;
+                    if (cnt == cap) {
+                        cap *= 2;
+                        list = (size_t*)realloc(list, cap * sizeof(size_t));
+                        lpart = (int*)realloc(lpart, cap * sizeof(int));
+                    }
+                    list[cnt] = n; lpart[cnt] = s; ++cnt;
+                }
+    }
+    /* claim: nodes inside the new spheres */
+    for (int s = 0; s < P->npart; ++s) {
+        int x0, x1, y0, y1, z0, z1;
+        box_range(P->pos[3 * s], R, nx, 0, &x0, &x1);
+        box_range(P->pos[3 * s + 1], R, ny, 1, &y0, &y1);
+        box_range(P->pos[3 * s + 2], R, nz, 1, &z0, &z1);
+        for (int zz = z0; zz <= z1; ++zz)
+            for (int yy = y0; yy <= y1; ++yy)
+                for (int ix = x0; ix <= x1; ++ix) {
+                    const int iy = wrapi(yy, ny), iz = wrapi(zz, nz);
+                    double d[3];
+                    node_offset(P, s, ix, iy, iz, ny, nz, d);
+                    if (inside_d(d, R)) owner[NODE(ix, iy, iz)] = s;
+                }
+    }
+    /* refill pending nodes from the fluid neighbour closest to the normal */
+    int nref = 0;
+    for (size_t k = 0; k < cnt; ++k) {
+        const size_t n = list[k];
+        if (owner[n] != -2) continue;
+        const int s = lpart[k];
+        const int ix = (int)(n % (size_t)nx), iy = (int)((n / (size_t)nx) % (size_t)ny), iz = (int)(n / ((size_t)nx * ny));
+        double d[3];
+        node_offset(P, s, ix, iy, iz, ny, nz, d);
+        int best = -1;
+        double bs = -1e300;
+        size_t bn = 0;
+        for (int i = 1; i < Q; ++i) {
+            const int sx = ix + CX[i];
+            if (sx < 0 || sx >= nx) continue;
+            const size_t y = NODE(sx, wrapi(iy + CY[i], ny), wrapi(iz + CZ[i], nz));
+            if (owner[y] != -1) continue;
+            double sc = (d[0] * CX[i] + d[1] * CY[i]) + d[2] * CZ[i];
+            if (i >= 7) sc = sc * INV_SQRT2;
+            if (sc > bs) { bs = sc; best = i; bn = y; }
+        }
+        const double* U = P->vel + 3 * s;
+        const double* W = P->omg + 3 * s;
+        const double uw0 = U[0] + (W[1] * d[2] - W[2] * d[1]);
+        const double uw1 = U[1] + (W[2] * d[0] - W[0] * d[2]);
+        const double uw2 = U[2] + (W[0] * d[1] - W[1] * d[0]);
+        double fe[Q];
+        if (best < 0) {
+            feq_dev(0.0, uw0, uw1, uw2, fe);
+            for (int i = 0; i < Q; ++i) F[(size_t)i + Q * n] = fe[i];
+        } else {
+            const double* g = F + Q * bn;
+            double r = 0.0, a = 0.0, b = 0.0, c = 0.0;
+            for (int i = 0; i < Q; ++i) { r += g[i]; a += CX[i] * g[i]; b += CY[i] * g[i]; c += CZ[i] * g[i]; }
+            a += p->force[0] / 2.0; b += p->force[1] / 2.0; c += p->force[2] / 2.0;
+            double fn[Q];
+            feq_dev(r, a, b, c, fn);
+            feq_dev(r, uw0, uw1, uw2, fe);
+            for (int i = 0; i < Q; ++i) F[(size_t)i + Q * n] = fe[i] + (g[i] - fn[i]);
+        }
+        ++nref;
+    }
+    /* refilled nodes join the fluid only now, so no refill reads another's */
+    for (size_t k = 0; k < cnt; ++k)
+        if (owner[list[k]] == -2) owner[list[k]] = -1;
+    free(list);
+    free(lpart);
+    return nref;
+}
+
+int orc_particle_step(const orc_params* p, orc_particles* P, double* f, int nx, int ny, int nz, int* owner,
+                      int* nlinks, int* nrefill) {
+    const size_t N = (size_t)nx * ny * nz;
+    double* m = (double*)malloc(4 * N * sizeof(double));
+    double* g = (double*)malloc((size_t)Q * N * sizeof(double));
+    if (!m || !g) { free(m); free(g); return -1; }
+    orc_macrovar(p, f, nx, ny, nz, m, m + N, m + 2 * N, m + 3 * N);
+    orc_step_push(p, f, g, nx, ny, nz, m, m + N, m + 2 * N, m + 3 * N);
+    const int nl = ibb_pass(p, P, g, nx, ny, nz, owner);
+    newton_euler(p, P, nx, ny, nz);
+    const int nr = regeometry(p, P, g, nx, ny, nz, owner);
+    memcpy(f, g, (size_t)Q * N * sizeof(double));
+    free(m);
+    free(g);
+    if (nlinks) *nlinks = nl;
+    if (nrefill) *nrefill = nr;
+    return 0;
+}

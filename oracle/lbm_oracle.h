@@ -76,4 +76,25 @@ void orc_profiles(const double* rho, const double* ux, const double* uy,
 void orc_channel_velocity(int nx, int ny, int nz, double uc, double amp,
                           uint64_t seed, double* ux, double* uy, double* uz);
 
+/* ---- moving spheres (the reference declares the data but ships no
+ * algorithm; this is the project's own design, restated here as
+ * the checker of the GPU kernels) ---------------------------------------- */
+typedef struct orc_particles {
+    int npart;
+    double radius, rho_ratio;
+    double stf0, stf1, stf0_w, stf1_w, zeta;
+    double *pos, *vel, *omg;          /* 3*npart each, reference axes        */
+    double *force, *torque;           /* hydrodynamic, last step (3*npart)   */
+    double *force_prev, *torque_prev; /* total of the previous step (AB2)    */
+    int have_prev;
+} orc_particles;
+
+/* owner[n] = particle id of the node, -1 for fluid (reference layout) */
+void orc_mark_solid(const orc_particles* P, int nx, int ny, int nz, int* owner);
+/* one full particle-laden step on natural-orientation populations:
+ * push step -> interpolated bounce-back + momentum exchange -> repulsion ->
+ * Newton-Euler -> geometry update -> refilling */
+int orc_particle_step(const orc_params* p, orc_particles* P, double* f, int nx, int ny, int nz,
+                      int* owner, int* nlinks, int* nrefill);
+
 #endif

@@ -221,3 +221,78 @@ def poiseuille_transient(nx: int, ustar: float, visc: float, istep: int, nterms:
         s += (4 * (-1) ** n) / (np.pi * (n + 0.5)) ** 3 * np.exp(-((n + 0.5) ** 2) * np.pi**2 * time1) * \
             np.cos((n + 0.5) * np.pi * (xx0 / (nx / 2.0)))
     return (1 - (xx0 / (nx / 2.0)) ** 2) - s
+
+
+# ---- moving spheres --------------------------------------------------------
+class OrcParticles(ctypes.Structure):
+    _fields_ = [("npart", ctypes.c_int), ("radius", ctypes.c_double), ("rho_ratio", ctypes.c_double),
+                ("stf0", ctypes.c_double), ("stf1", ctypes.c_double), ("stf0_w", ctypes.c_double),
+                ("stf1_w", ctypes.c_double), ("zeta", ctypes.c_double)] + \
+               [(n, ctypes.POINTER(ctypes.c_double)) for n in
+                ("pos", "vel", "omg", "force", "torque", "force_prev", "torque_prev")] + \
+               [("have_prev", ctypes.c_int)]
+
+
+class Spheres:
+    """Sphere state for the oracle; arrays (npart, 3) float64, reference axes."""
+
+    def __init__(self, pos, radius, rho_ratio=2.0, vel=None, omg=None, stf0=0.025, stf1=0.002,
+                 stf0_w=0.025, stf1_w=0.002, zeta=1.0):
+        self.pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3).copy()
+        n = len(self.pos)
+        self.vel = np.zeros((n, 3)) if vel is None else np.array(vel, dtype=np.float64).reshape(n, 3)
+        self.omg = np.zeros((n, 3)) if omg is None else np.array(omg, dtype=np.float64).reshape(n, 3)
+        self.force = np.zeros((n, 3))
+        self.torque = np.zeros((n, 3))
+        self.force_prev = np.zeros((n, 3))
+        self.torque_prev = np.zeros((n, 3))
+        self.c = OrcParticles()
+        self.c.npart = n
+        self.c.radius = radius
+        self.c.rho_ratio = rho_ratio
+        self.c.stf0, self.c.stf1, self.c.stf0_w, self.c.stf1_w, self.c.zeta = stf0, stf1, stf0_w, stf1_w, zeta
+        for name in ("pos", "vel", "omg", "force", "torque", "force_prev", "torque_prev"):
+            setattr(self.c, name, _p(getattr(self, name)))
+        self.c.have_prev = 0
+
+
+def _bind_particles():
+    L = lib()
+    if getattr(L, "_particles_bound", False):
+        return L
+    dp = ctypes.POINTER(ctypes.c_double)
+    ip = ctypes.POINTER(ctypes.c_int)
+    L.orc_mark_solid.restype = None
+    L.orc_mark_solid.argtypes = [ctypes.POINTER(OrcParticles), ctypes.c_int, ctypes.c_int, ctypes.c_int, ip]
+    L.orc_particle_step.restype = ctypes.c_int
+    L.orc_particle_step.argtypes = [ctypes.POINTER(OrcParams), ctypes.POINTER(OrcParticles), dp, ctypes.c_int,
+                                    ctypes.c_int, ctypes.c_int, ip, ip, ip]
+    L._particles_bound = True
+    return L
+
+
+def mark_solid(sp: Spheres, shape) -> np.ndarray:
+    L = _bind_particles()
+    owner = np.empty(shape, dtype=np.int32, order="F")
+    L.orc_mark_solid(ctypes.byref(sp.c), *shape, owner.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    return owner
+
+
+def particle_run(p: OrcParams, sp: Spheres, f: np.ndarray, nsteps: int, owner=None):
+    """nsteps particle-laden steps in place on a copy of f; returns (f, owner, links, refills)."""
+    L = _bind_particles()
+    f = np.array(f, dtype=np.float64, order="F", copy=True)
+    _, nx, ny, nz = f.shape
+    if owner is None:
+        owner = mark_solid(sp, (nx, ny, nz))
+    ip = ctypes.POINTER(ctypes.c_int)
+    nl, nr = ctypes.c_int(), ctypes.c_int()
+    links, refills = [], []
+    for _ in range(nsteps):
+        rc = L.orc_particle_step(ctypes.byref(p), ctypes.byref(sp.c), _p(f), nx, ny, nz,
+                                 owner.ctypes.data_as(ip), ctypes.byref(nl), ctypes.byref(nr))
+        if rc != 0:
+            raise RuntimeError("oracle particle step failed")
+        links.append(nl.value)
+        refills.append(nr.value)
+    return f, owner, links, refills
