@@ -2,12 +2,14 @@
 """Throughput of the D3Q19 channel-flow time step on GB300.
 
 One bench step = one lattice time step (collision + streaming + walls +
-periodic wrap) over the whole domain.  Default workload: the large channel
-1024 x 512 x 512 (streamwise x spanwise x wall-normal), FP32 arithmetic on
-populations stored as FP16 deviations with a fixed scale, nu = 0.0024,
-u* = 0.0034, h = 256, seeded Poiseuille + 5 % noise initial state.  The
-moving spheres of that configuration are not part of this step yet, so the
-workload is named "particle-free".
+periodic wrap, and with spheres the interpolated bounce-back, momentum
+exchange, Newton-Euler update and refilling) over the whole domain.  Default
+workload: the large particle-laden channel 1024 x 512 x 512 (streamwise x
+spanwise x wall-normal) with 16384 spheres of radius 8 (density ratio 2,
+seeded placement with >= 2-node gaps and >= 1 node from the walls), FP32
+arithmetic on populations stored as FP16 deviations with a fixed scale,
+nu = 0.0024, u* = 0.0034, h = 256, seeded Poiseuille + 5 % noise initial
+state.  --no-particles leaves the spheres out.
 
 Printed JSON line (rank 0):
   value      GLUPS over all ranks, device-resident state, CUDA-event timed
@@ -170,35 +172,72 @@ def allmax(world, v: float) -> float:
     return float(t.item())
 
 
-def workload_name(cfg, prec) -> str:
+def workload_name(cfg, prec, spheres=True) -> str:
+    if cfg.spheres and spheres:
+        return (f"channel {cfg.stream}x{cfg.span}x{cfg.wall} {prec}-store, {cfg.spheres} spheres r={cfg.radius:g} "
+                f"({cfg.name})")
     return f"channel {cfg.stream}x{cfg.span}x{cfg.wall} {prec}-store particle-free ({cfg.name})"
 
 
-# --------------------------------------------------------------------------
-def cpu_sample(orc, cfg, budget_s: float, threads: int, warmup_steps: int = 1, fixed_steps: int | None = None):
-    """Time the oracle's OpenMP step on a spanwise slab of the channel.
+def sphere_positions(pkg, cfg):
+    """Seeded placement of the configuration's spheres: >= 2-node gaps, >= 1 node from the walls."""
+    return pkg.place_spheres(cfg.wall, cfg.stream, cfg.span, cfg.spheres, cfg.radius, gap=2.0, wall_gap=1.0,
+                             seed=cfg.seed)
 
-    Returns (glups, nodes, steps, seconds, shape)."""
+
+# --------------------------------------------------------------------------
+def cpu_sample(orc, pkg, cfg, budget_s: float, threads: int, spheres: bool):
+    """Time the oracle on a bounded sample of the workload.
+
+    Particle-free: a 2-plane spanwise slab of the channel, OpenMP push.
+    With spheres: a 64^3 box at the channel's sphere volume fraction (fluid
+    push on OpenMP threads, sphere steps serial).  Returns (glups, nodes,
+    steps, seconds, description)."""
     run = cfg.params("fp64")
     p = orc.params_from(run)
-    nz = 2
-    shape = (cfg.wall, cfg.stream, nz)
+    if spheres and cfg.spheres:
+        shape = (64, 64, 64)
+        n = max(1, round(cfg.spheres * 64**3 / cfg.nodes))
+        pos = pkg.place_spheres(*shape, n, cfg.radius, gap=2.0, wall_gap=1.0, seed=cfg.seed)
+        u = orc.channel_velocity(*shape, cfg.uc, cfg.amp, cfg.seed)
+        f = orc.initpop(*u)
+        sp = orc.Spheres(pos, radius=cfg.radius, rho_ratio=2.0)
+        f, owner, _, _ = orc.particle_run(p, sp, f, 1)
+        t0 = time.perf_counter()
+        f, owner, _, _ = orc.particle_run(p, sp, f, 1, owner=owner)
+        t1 = time.perf_counter() - t0
+        steps = max(1, int(budget_s / max(t1, 1e-6)))
+        t0 = time.perf_counter()
+        orc.particle_run(p, sp, f, steps, owner=owner)
+        dt = time.perf_counter() - t0
+        nodes = 64**3
+        desc = (f"FP64 oracle port, 64x64x64 box with {n} spheres r={cfg.radius:g} (the channel's volume fraction), "
+                f"{steps} steps in {dt:.1f} s")
+        return nodes * steps / dt / 1e9, nodes, steps, dt, desc
+    shape = (cfg.wall, cfg.stream, 2)
     u = orc.channel_velocity(*shape, cfg.uc, cfg.amp, cfg.seed)
     f = orc.initpop(*u)
-    orc.run_omp(p, f, warmup_steps, threads)
+    orc.run_omp(p, f, 1, threads)
     t0 = time.perf_counter()
     orc.run_omp(p, f, 1, threads)
     t1 = time.perf_counter() - t0
     nodes = int(np.prod(shape))
-    steps = fixed_steps if fixed_steps is not None else max(1, int(budget_s / max(t1, 1e-6)))
+    steps = max(1, int(budget_s / max(t1, 1e-6)))
     t0 = time.perf_counter()
     orc.run_omp(p, f, steps, threads)
     dt = time.perf_counter() - t0
-    return nodes * steps / dt / 1e9, nodes, steps, dt, shape
+    desc = (f"FP64 oracle port (OpenMP two-lattice push) on a {shape[1]}x{shape[2]}x{shape[0]} slab of the same "
+            f"channel, {steps} steps in {dt:.1f} s")
+    return nodes * steps / dt / 1e9, nodes, steps, dt, desc
 
 
 def run_reference(args, world, rank):
-    """--impl reference: the CPU implementation of the step, rank 0 only."""
+    """--impl reference: the CPU implementation of the step, rank 0 only.
+
+    The Fortran reference cannot be built on these machines (no Fortran
+    compiler, no MPI), so the CPU implementation timed is the FP64 oracle port
+    with all host threads; each step is one time step of a bounded sample of
+    the workload, sized so that warm-up + timed steps take ~cpu_budget s."""
     if rank != 0:
         return
     sys.path.insert(0, str(REPO / "oracle"))
@@ -207,39 +246,18 @@ def run_reference(args, world, rank):
     cfg = pkg.CHANNEL_CONFIGS[args.config]
     prec = args.precision or cfg.precision
     threads = os.cpu_count() or 1
-    run = cfg.params("fp64")
-    p = orc.params_from(run)
-    # slab sample sized so that warm-up + timed steps take about args.cpu_budget seconds
-    shape = (cfg.wall, cfg.stream, 1)
-    u = orc.channel_velocity(*shape, cfg.uc, cfg.amp, cfg.seed)
-    f = orc.initpop(*u)
-    orc.run_omp(p, f, 1, threads)
-    t0 = time.perf_counter()
-    orc.run_omp(p, f, 2, threads)
-    per_plane_step = (time.perf_counter() - t0) / 2
-    per_step_budget = args.cpu_budget / max(1, args.steps + args.warmup)
-    nz = max(1, min(cfg.span, int(per_step_budget / max(per_plane_step, 1e-9))))
-    shape = (cfg.wall, cfg.stream, nz)
-    u = orc.channel_velocity(*shape, cfg.uc, cfg.amp, cfg.seed)
-    f = orc.initpop(*u)
-    orc.run_omp(p, f, args.warmup, threads)
-    t0 = time.perf_counter()
-    orc.run_omp(p, f, args.steps, threads)
-    dt = time.perf_counter() - t0
-    nodes = int(np.prod(shape))
-    glups = nodes * args.steps / dt / 1e9
-    sample = (f"each step = one FP64 time step of the oracle port (no Fortran compiler on these machines) "
-              f"on a {cfg.stream}x{nz}x{cfg.wall} slab ({nodes} nodes) of the {cfg.stream}x{cfg.span}x{cfg.wall} "
-              f"channel, two-lattice push, {threads} OpenMP threads")
+    spheres = bool(cfg.spheres) and not args.no_particles
+    per_step = args.cpu_budget / max(1, args.steps + args.warmup)
+    g, nodes, steps, dt, desc = cpu_sample(orc, pkg, cfg, per_step * (args.steps + args.warmup), threads, spheres)
+    sample = f"each step = one time step of: {desc}; {threads} host threads"
     line = {
-        "impl": "reference", "metric": "GLUPS (lattice updates per second / 1e9)", "value": round(glups, 6),
+        "impl": "reference", "metric": "GLUPS (lattice updates per second / 1e9)", "value": round(g, 6),
         "unit": "GLUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(dt / args.steps * 1e3, 4), "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": round(dt / max(steps, 1) * 1e3, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload_name(cfg, prec), "sample_nodes": nodes},
-        "cpu_baseline": {"value": round(glups, 6), "unit": "GLUPS", "cores": threads, "kind": "port",
-                         "sample": sample},
-        "e2e": {"value": round(glups, 6), "unit": "GLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "config": {"workload": workload_name(cfg, prec, spheres), "sample_nodes": nodes, "sample_steps": steps},
+        "cpu_baseline": {"value": round(g, 6), "unit": "GLUPS", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": round(g, 6), "unit": "GLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
@@ -254,10 +272,16 @@ def run_gpu(args, world, rank, local):
     N = cfg.nodes
     bpn = 38 * BYTES[prec]
     run = cfg.params(prec, device=local, flags=pkg.FLAG_SIMPLE_STEP if args.simple else 0)
+    spheres = bool(cfg.spheres) and not args.no_particles
+    wname = workload_name(cfg, prec, spheres)
     torch.cuda.set_device(local)
     lat = pkg.Lattice(run)
     lat.init_channel(cfg.uc, cfg.amp, cfg.seed)
-    log(f"[bench] rank {rank}: {workload_name(cfg, prec)}, {N} nodes, {lat.device_bytes() / 1e9:.2f} GB on device")
+    pos = None
+    if spheres:
+        pos = sphere_positions(pkg, cfg)
+        lat.set_particles(pos, cfg.radius, 2.0)
+    log(f"[bench] rank {rank}: {wname}, {N} nodes, {lat.device_bytes() / 1e9:.2f} GB on device")
     lat.step(args.warmup)
     stream = torch.cuda.ExternalStream(lat.stream())
     evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
@@ -267,6 +291,7 @@ def run_gpu(args, world, rank, local):
     sampler.start()
     time.sleep(0.3)
     parity0 = lat.step_count() % 2
+    lat.timing_enable(args.steps)
     for k in range(args.steps):
         evs[k].record(stream)
         lat.step_async(1)
@@ -283,41 +308,44 @@ def run_gpu(args, world, rank, local):
     if st.nonfinite:
         raise RuntimeError("non-finite populations after the timed steps")
 
-    # roofline of the step kernels (even/odd AA launches alternate)
+    # roofline of the fluid step kernel (even/odd AA launches alternate), timed
+    # by events the library records around each launch inside the timed loop
+    tm = lat.timing()
     peaks = measured_peaks()
-    even = per[(np.arange(args.steps) + parity0) % 2 == 0]
-    odd = per[(np.arange(args.steps) + parity0) % 2 == 1]
+    ev_ms = tm["even_ms"] / max(tm["even"], 1)
+    od_ms = tm["odd_ms"] / max(tm["odd"], 1)
+    fluid_ms = (tm["even_ms"] + tm["odd_ms"]) / max(tm["even"] + tm["odd"], 1)
     alg = bpn * N
-    achieved = alg / (per.mean() / 1e3) / 1e9
-    traffic = committed_traffic(workload_name(cfg, prec))
+    achieved = alg / (fluid_ms / 1e3) / 1e9
+    traffic = committed_traffic(wname)
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "frac": round(achieved / peaks["hbm_gbs"], 4),
             "traffic": (round((traffic["even_bytes"] + traffic["odd_bytes"]) / 2) if traffic else None),
             "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json hbm_gbs)",
             "algorithmic_bytes_per_launch": alg,
-            "kernels": {"even_local": {"ms": round(float(even.mean()), 4),
-                                       "achieved": round(alg / (even.mean() / 1e3) / 1e9, 1)},
-                        "odd_neighbour": {"ms": round(float(odd.mean()), 4),
-                                          "achieved": round(alg / (odd.mean() / 1e3) / 1e9, 1)}}}
+            "kernels": {"even_local": {"ms": round(ev_ms, 4), "achieved": round(alg / (ev_ms / 1e3) / 1e9, 1)},
+                        "odd_neighbour": {"ms": round(od_ms, 4), "achieved": round(alg / (od_ms / 1e3) / 1e9, 1)},
+                        "spheres_per_step_ms": round(tm["particle_ms"] / max(tm["even"] + tm["odd"], 1), 4)}}
+    if spheres:
+        ns, nl, nr = lat.particle_counts()
+        roof["spheres"] = {"solid_nodes": ns, "links_last_step": nl, "refills_last_step": nr}
 
+    lat.close()
     accuracy = None
     if rank == 0 and args.accuracy_steps > 0 and prec != "fp64":
-        accuracy = accuracy_window(pkg, cfg, prec, args.accuracy_steps, local, lat)
-    lat.close()
+        accuracy = accuracy_window(pkg, cfg, prec, args.accuracy_steps, local, pos)
 
     e2e = None
     if not args.no_e2e:
-        e2e = e2e_run(pkg, torch, cfg, prec, args.steps, local, world)
+        e2e = e2e_run(pkg, torch, cfg, prec, args.steps, local, world, pos)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
         sys.path.insert(0, str(REPO / "oracle"))
         import oracle as orc
         threads = os.cpu_count() or 1
-        g, nodes, steps, dt, shape = cpu_sample(orc, cfg, args.cpu_budget, threads)
-        cpu = {"value": round(g, 6), "unit": "GLUPS", "cores": threads, "kind": "port",
-               "sample": f"FP64 oracle port (OpenMP two-lattice push) on a {shape[1]}x{shape[2]}x{shape[0]} slab "
-                         f"of the same channel, {steps} steps in {dt:.1f} s"}
+        g, nodes, steps, dt, desc = cpu_sample(orc, pkg, cfg, args.cpu_budget, threads, spheres)
+        cpu = {"value": round(g, 6), "unit": "GLUPS", "cores": threads, "kind": "port", "sample": desc}
 
     if rank == 0:
         line = {
@@ -326,7 +354,7 @@ def run_gpu(args, world, rank, local):
             "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32" if prec != "fp64" else "f64",
             "data": "synthetic (seeded Poiseuille + uniform noise initial state)",
-            "config": {"workload": workload_name(cfg, prec), "storage": prec, "nodes": N,
+            "config": {"workload": wname, "storage": prec, "nodes": N,
                        "grid_stream_span_wall": [cfg.stream, cfg.span, cfg.wall], "visc": cfg.visc,
                        "ustar": cfg.ustar, "h": cfg.h, "mrt": "MRTtype 1 (para.f90)",
                        "l2": f"populations {N * 19 * BYTES[prec] / 1e9:.1f} GB >> 129 MB L2, no flush needed",
@@ -337,7 +365,7 @@ def run_gpu(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
-def accuracy_window(pkg, cfg, prec, steps, device, lat_lp):
+def accuracy_window(pkg, cfg, prec, steps, device, pos):
     """FP64 vs the low-precision run over `steps` steps from the same initial
     state (the FP64 spot check of the large configuration)."""
     out = {}
@@ -345,10 +373,13 @@ def accuracy_window(pkg, cfg, prec, steps, device, lat_lp):
     for p in ("fp64", prec):
         with pkg.Lattice(cfg.params(p, device=device)) as lat:
             lat.init_channel(cfg.uc, cfg.amp, cfg.seed)
+            if pos is not None:
+                lat.set_particles(pos, cfg.radius, 2.0)
             d0 = lat.diag()
             lat.step(steps)
             d1 = lat.diag()
-            res[p] = (pkg.statistics(lat.profiles(), cfg.ustar), d1.rho_sum - d0.rho_sum)
+            part = lat.particles() if pos is not None else None
+            res[p] = (pkg.statistics(lat.profiles(), cfg.ustar), d1.rho_sum - d0.rho_sum, part)
     ref, lp = res["fp64"][0], res[prec][0]
     mref = ref["mean"][:, 1]
     out["steps"] = steps
@@ -358,10 +389,17 @@ def accuracy_window(pkg, cfg, prec, steps, device, lat_lp):
     out["reynolds_stress_max_fp64"] = float(np.abs(sref).max())
     out["mass_drift_fp64"] = res["fp64"][1]
     out[f"mass_drift_{prec}"] = res[prec][1]
+    if pos is not None:
+        a, b = res[prec][2], res["fp64"][2]
+        fb = b["force"]
+        out["particle_force_rel_err"] = float(np.abs(a["force"] - fb).max() / max(np.abs(fb).max(), 1e-300))
+        out["particle_force_mean_rel_err"] = float(np.abs(a["force"].mean(0) - fb.mean(0)).max()
+                                                   / max(np.abs(fb.mean(0)).max(), 1e-300))
+        out["particle_velocity_rel_err"] = float(np.abs(a["vel"] - b["vel"]).max() / max(np.abs(b["vel"]).max(), 1e-300))
     return out
 
 
-def e2e_run(pkg, torch, cfg, prec, steps, device, world):
+def e2e_run(pkg, torch, cfg, prec, steps, device, world, pos=None):
     """GLUPS through the public C ABI with pinned host buffers in and out."""
     N = cfg.nodes
     shape = (cfg.wall, cfg.stream, cfg.span)
@@ -379,6 +417,8 @@ def e2e_run(pkg, torch, cfg, prec, steps, device, world):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     lat.initpop(arrs[0], arrs[1], arrs[2])
+    if pos is not None:
+        lat.set_particles(pos, cfg.radius, 2.0)
     ndiags = 0
     for k in range(1, steps + 1):
         lat.step(1)
@@ -386,13 +426,19 @@ def e2e_run(pkg, torch, cfg, prec, steps, device, world):
             lat.diag()
             ndiags += 1
     lib.lbm_macrovar(lat._ctx, *(pkg._dptr(a) for a in arrs))
+    pbytes = 0
+    if pos is not None:
+        lat.particles()
+        pbytes = 5 * pos.size * 8
     dt = time.perf_counter() - t0
     dt = allmax(world, dt)
     lat.close()
     return {"value": round(world * N * steps / dt / 1e9, 4), "unit": "GLUPS",
-            "h2d_bytes_per_step": int(3 * N * 8 / steps),
-            "d2h_bytes_per_step": int((4 * N * 8 + ndiags * diag_bytes) / steps),
-            "path": "lbm_initpop(host u) -> lbm_step(1) x steps (+lbm_diag every 250) -> lbm_macrovar(host)",
+            "h2d_bytes_per_step": int((3 * N * 8 + (pos.size * 8 if pos is not None else 0)) / steps),
+            "d2h_bytes_per_step": int((4 * N * 8 + ndiags * diag_bytes + pbytes) / steps),
+            "path": ("lbm_initpop(host u)" + (" + lbm_particles_set(host)" if pos is not None else "")
+                     + " -> lbm_step(1) x steps (+lbm_diag every 250) -> lbm_macrovar(host)"
+                     + (" + lbm_particles_get(host)" if pos is not None else "")),
             "seconds": round(dt, 3)}
 
 
@@ -409,6 +455,7 @@ def main():
     ap.add_argument("--grid", type=int, nargs=3, metavar=("STREAM", "SPAN", "WALL"), default=None,
                     help="override the lattice (streamwise spanwise wall-normal), e.g. for a small ncu capture")
     ap.add_argument("--simple", action="store_true", help="one-node-per-thread step kernels (A/B reference)")
+    ap.add_argument("--no-particles", action="store_true", help="leave the configuration's spheres out")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

@@ -48,6 +48,7 @@ EXPORTS = (
     "lbm_step_count", "lbm_prerelax", "lbm_macrovar", "lbm_diag", "lbm_profiles", "lbm_avedensity",
     "lbm_save_flow", "lbm_load_flow", "lbm_profiles_noalloc", "lbm_particle_params_init",
     "lbm_particles_place", "lbm_particles_set", "lbm_particles_get", "lbm_particle_counts",
+    "lbm_timing_enable", "lbm_timing_get",
 )
 
 
@@ -136,6 +137,9 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
         "lbm_avedensity": (ctypes.c_int, [ctx, dp]),
         "lbm_save_flow": (ctypes.c_int, [ctx, ctypes.c_char_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]),
         "lbm_load_flow": (ctypes.c_int, [ctx, ctypes.c_char_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]),
+        "lbm_timing_enable": (ctypes.c_int, [ctx, ctypes.c_int32]),
+        "lbm_timing_get": (ctypes.c_int, [ctx, dp, dp, dp, ctypes.POINTER(ctypes.c_int64),
+                                          ctypes.POINTER(ctypes.c_int64)]),
         "lbm_particle_params_init": (ctypes.c_int, [ctypes.POINTER(LBMParticleParams), ctypes.c_int32,
                                                     ctypes.c_double, ctypes.c_double]),
         "lbm_particles_place": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
@@ -426,6 +430,16 @@ class Lattice:
         out = {k: np.empty((n, 3)) for k in ("pos", "vel", "omg", "force", "torque")}
         self._call("lbm_particles_get", *(_dptr(out[k]) for k in ("pos", "vel", "omg", "force", "torque")))
         return out
+
+    def timing_enable(self, capacity: int) -> None:
+        self._call("lbm_timing_enable", capacity)
+
+    def timing(self) -> dict:
+        fe, fo, pm = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        ne, no = ctypes.c_int64(), ctypes.c_int64()
+        self._call("lbm_timing_get", ctypes.byref(fe), ctypes.byref(fo), ctypes.byref(pm), ctypes.byref(ne),
+                   ctypes.byref(no))
+        return dict(even_ms=fe.value, odd_ms=fo.value, particle_ms=pm.value, even=ne.value, odd=no.value)
 
     def particle_counts(self) -> tuple[int, int, int]:
         a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()

@@ -33,6 +33,10 @@ struct lbm_ctx {
     lbm_particle_params pp{};
     int have_prev = 0;         // Adams-Bashforth history available
     unsigned long long* d_count = nullptr;
+    // per-step timing (lbm_timing_enable): 3 events per recorded step
+    std::vector<cudaEvent_t> tev;
+    std::vector<int> tpar;
+    int tcap = 0, tn = 0;
 };
 
 namespace {
@@ -374,6 +378,7 @@ int lbm_destroy(lbm_ctx* c) {
     cudaFree(c->d_max);
     cudaFree(c->d_err);
     cudaFree(c->d_count);
+    for (cudaEvent_t e : c->tev) cudaEventDestroy(e);
     cudaFree(c->P.pos);
     cudaFree(c->P.owner);
     cudaFree(c->P.refill_node);
@@ -463,13 +468,22 @@ int lbm_step_async(lbm_ctx* c, int32_t nsteps) {
     if (check_ctx(c)) return LBM_ERR_INVALID_ARG;
     if (nsteps < 0) return fail(LBM_ERR_INVALID_ARG, "negative step count");
     for (int32_t k = 0; k < nsteps; ++k) {
+        const bool timed = c->tn < c->tcap;
+        if (timed) CK(cudaEventRecord(c->tev[3 * c->tn], c->stream));
         if (c->s.use_rows) CK(launch_step_rows(c->s, c->parity, c->d_err, c->stream));
         else CK(launch_step(c->s, c->parity, c->stream));
+        if (timed) CK(cudaEventRecord(c->tev[3 * c->tn + 1], c->stream));
+        const int was = c->parity;
         c->parity ^= 1;
         ++c->nsteps;
         if (c->P.npart > 0) {
             CK(particles_after_step(c->s, c->P, c->parity, c->have_prev, c->stream));
             c->have_prev = 1;
+        }
+        if (timed) {
+            CK(cudaEventRecord(c->tev[3 * c->tn + 2], c->stream));
+            c->tpar[c->tn] = was;
+            ++c->tn;
         }
     }
     return LBM_OK;
@@ -853,6 +867,39 @@ int lbm_particle_counts(lbm_ctx* c, int64_t* nsolid, int64_t* nlinks, int64_t* n
     if (nsolid) *nsolid = (int64_t)ns;
     if (nlinks) *nlinks = cnt[1];
     if (nrefill) *nrefill = cnt[0];
+    return LBM_OK;
+}
+
+int lbm_timing_enable(lbm_ctx* c, int32_t capacity) {
+    if (check_ctx(c) || capacity < 0) return fail(LBM_ERR_INVALID_ARG, "bad argument");
+    if (int rc = set_device(c)) return rc;
+    CK(cudaStreamSynchronize(c->stream));
+    for (cudaEvent_t e : c->tev) cudaEventDestroy(e);
+    c->tev.assign(3 * (size_t)capacity, nullptr);
+    for (auto& e : c->tev) CK(cudaEventCreate(&e));
+    c->tpar.assign(capacity, 0);
+    c->tcap = capacity;
+    c->tn = 0;
+    return LBM_OK;
+}
+
+int lbm_timing_get(lbm_ctx* c, double* fe, double* fo, double* pm, int64_t* ne, int64_t* no) {
+    if (check_ctx(c)) return LBM_ERR_INVALID_ARG;
+    if (int rc = sync(c)) return rc;
+    double se = 0, so = 0, sp = 0;
+    int64_t ce = 0, co = 0;
+    for (int k = 0; k < c->tn; ++k) {
+        float a = 0, b = 0;
+        CK(cudaEventElapsedTime(&a, c->tev[3 * k], c->tev[3 * k + 1]));
+        CK(cudaEventElapsedTime(&b, c->tev[3 * k + 1], c->tev[3 * k + 2]));
+        if (c->tpar[k] == 0) { se += a; ++ce; } else { so += a; ++co; }
+        sp += b;
+    }
+    if (fe) *fe = se;
+    if (fo) *fo = so;
+    if (pm) *pm = sp;
+    if (ne) *ne = ce;
+    if (no) *no = co;
     return LBM_OK;
 }
 

@@ -165,6 +165,14 @@ int lbm_step(lbm_ctx* ctx, int32_t nsteps);
 /* Same, enqueued on the context's stream without waiting. */
 int lbm_step_async(lbm_ctx* ctx, int32_t nsteps);
 int lbm_synchronize(lbm_ctx* ctx);
+/* Per-step CUDA-event timing inside lbm_step: with timing enabled (capacity =
+ * steps to record), every step records events around its fluid kernel and
+ * around the particle kernels that follow it.  lbm_timing_get returns the
+ * summed milliseconds of the recorded steps (fluid kernels of even and odd
+ * steps separately) and the number recorded; it synchronizes the stream. */
+int lbm_timing_enable(lbm_ctx* ctx, int32_t capacity);
+int lbm_timing_get(lbm_ctx* ctx, double* fluid_even_ms, double* fluid_odd_ms,
+                   double* particle_ms, int64_t* steps_even, int64_t* steps_odd);
 /* The context's cudaStream_t, for event timing by the caller. */
 int lbm_stream(lbm_ctx* ctx, void** stream);
 /* Steps taken since the last upload / init. */

@@ -332,6 +332,8 @@ static void push_node(const orc_params* p, const double* fin, double* fout, int 
 
 void orc_step_push(const orc_params* p, const double* fin, double* fout, int nx, int ny, int nz,
                    const double* rho, const double* ux, const double* uy, const double* uz) {
+    init_tables();
+#pragma omp parallel for schedule(static)
     for (int iz = 0; iz < nz; ++iz)
         for (int iy = 0; iy < ny; ++iy)
             for (int ix = 0; ix < nx; ++ix) {
