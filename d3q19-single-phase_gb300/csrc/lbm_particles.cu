@@ -36,6 +36,60 @@ constexpr double kPi = 3.14159265358979323846;
 constexpr double kInvSqrt2 = 0.70710678118654752440;
 constexpr int kPThreads = 256;
 
+// Lattice lookups with a runtime direction index, packed into 64-bit words at
+// compile time (a constexpr table indexed at run time would live in local
+// memory).
+constexpr uint64_t pack_c(int which) {
+    uint64_t w = 0;
+    for (int i = 0; i < Q; ++i) {
+        const int v = which == 0 ? CXf(i) : (which == 1 ? CYf(i) : CZf(i));
+        w |= (uint64_t)(v + 1) << (2 * i);
+    }
+    return w;
+}
+constexpr uint64_t kCX = pack_c(0), kCY = pack_c(1), kCZ = pack_c(2);
+constexpr uint64_t pack_opp(int lo) {
+    uint64_t w = 0;
+    for (int i = lo; i < lo + 12 && i < Q; ++i) w |= (uint64_t)OPPf(i) << (5 * (i - lo));
+    return w;
+}
+constexpr uint64_t kOPP0 = pack_opp(0), kOPP1 = pack_opp(12);
+__device__ __forceinline__ int cx_rt(int i) { return (int)((kCX >> (2 * i)) & 3u) - 1; }
+__device__ __forceinline__ int cy_rt(int i) { return (int)((kCY >> (2 * i)) & 3u) - 1; }
+__device__ __forceinline__ int cz_rt(int i) { return (int)((kCZ >> (2 * i)) & 3u) - 1; }
+__device__ __forceinline__ int opp_rt(int i) {
+    return i < 12 ? (int)((kOPP0 >> (5 * i)) & 31u) : (int)((kOPP1 >> (5 * (i - 12))) & 31u);
+}
+__device__ __forceinline__ double w_rt(int i) { return i == 0 ? W0 : (i <= 6 ? W1 : W2); }
+
+// Walk a bounding box with a stride of blockDim.x nodes without integer
+// division per node.
+struct BoxWalk {
+    int a, b, c, na, nb, nc;
+    int sa, sb, sc;                       // the stride in mixed radix (na, nb)
+    __device__ __forceinline__ BoxWalk(int t, int step, int na_, int nb_, int nc_) : na(na_), nb(nb_), nc(nc_) {
+        if (na <= 0 || nb <= 0) { a = b = 0; c = nc; sa = sb = sc = 0; return; }
+        a = t % na;
+        const int r = t / na;
+        b = r % nb;
+        c = r / nb;
+        sa = step % na;
+        const int rs = step / na;
+        sb = rs % nb;
+        sc = rs / nb;
+    }
+    __device__ __forceinline__ bool valid() const { return c < nc; }
+    __device__ __forceinline__ void advance() {
+        a += sa;
+        int carry = 0;
+        if (a >= na) { a -= na; carry = 1; }
+        b += sb + carry;
+        carry = 0;
+        if (b >= nb) { b -= nb; carry = 1; }
+        c += sc + carry;
+    }
+};
+
 __device__ __forceinline__ double dmin_image(double d, double L) {
     if (d >= 0.5 * L) d = __dsub_rn(d, L);
     else if (d < -0.5 * L) d = __dadd_rn(d, L);
@@ -54,6 +108,17 @@ __device__ __forceinline__ double norm2_rn(const double d[3]) {
     return __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])), __dmul_rn(d[2], d[2]));
 }
 __device__ __forceinline__ bool inside(const double d[3], double R) { return norm2_rn(d) <= __dmul_rn(R, R); }
+
+// Squared distance in FP32 from FP64 offsets: decides the inside test alone
+// when it is far from R^2; the exact FP64 test runs only near the surface.
+__device__ __forceinline__ int inside_fast(const double d[3], double R) {
+    const float x = (float)d[0], y = (float)d[1], z = (float)d[2];
+    const float r2 = x * x + y * y + z * z, R2 = (float)(R * R);
+    const float band = 1e-4f * R2 + 1e-3f;
+    if (r2 < R2 - band) return 1;
+    if (r2 > R2 + band) return 0;
+    return inside(d, R) ? 1 : 0;
+}
 
 __device__ __forceinline__ int wrapi(int a, int n) {
     a %= n;
@@ -96,10 +161,10 @@ __device__ __forceinline__ Slot natural_slot(const Geometry& g, int parity, int 
     s.k = k;
     s.n = gnode(g, ix, iy, iz);
     if (parity) {
-        const int sx = ix - CXf(k);
+        const int sx = ix - cx_rt(k);
         if (sx >= 0 && sx < g.NZ) {
-            s.k = OPPf(k);
-            s.n = gnode(g, sx, wrapi(iy - CYf(k), g.NX), wrapi(iz - CZf(k), g.NY));
+            s.k = opp_rt(k);
+            s.n = gnode(g, sx, wrapi(iy - cy_rt(k), g.NX), wrapi(iz - cz_rt(k), g.NY));
         }
     }
     return s;
@@ -123,13 +188,11 @@ __global__ void __launch_bounds__(kPThreads) k_claim(DeviceParticles P, Geometry
     const Range rx = box(P.pos[3 * p], P.R, g.NZ, false);
     const Range ry = box(P.pos[3 * p + 1], P.R, g.NX, true);
     const Range rz = box(P.pos[3 * p + 2], P.R, g.NY, true);
-    const int total = rx.n * ry.n * rz.n;
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-        const int a = t % rx.n, b = (t / rx.n) % ry.n, c = t / (rx.n * ry.n);
-        const int ix = rx.lo + a, iy = wrapi(ry.lo + b, g.NX), iz = wrapi(rz.lo + c, g.NY);
+    for (BoxWalk w(threadIdx.x, blockDim.x, rx.n, ry.n, rz.n); w.valid(); w.advance()) {
+        const int ix = rx.lo + w.a, iy = wrapi(ry.lo + w.b, g.NX), iz = wrapi(rz.lo + w.c, g.NY);
         double d[3];
         offset(P, g, p, ix, iy, iz, d);
-        if (inside(d, P.R)) owner[gnode(g, ix, iy, iz)] = p;
+        if (inside_fast(d, P.R)) owner[gnode(g, ix, iy, iz)] = p;
     }
 }
 
@@ -139,15 +202,13 @@ __global__ void __launch_bounds__(kPThreads) k_release(DeviceParticles P, Geomet
     const Range rx = box(P.pos[3 * p], ext, g.NZ, false);
     const Range ry = box(P.pos[3 * p + 1], ext, g.NX, true);
     const Range rz = box(P.pos[3 * p + 2], ext, g.NY, true);
-    const int total = rx.n * ry.n * rz.n;
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-        const int a = t % rx.n, b = (t / rx.n) % ry.n, c = t / (rx.n * ry.n);
-        const int ix = rx.lo + a, iy = wrapi(ry.lo + b, g.NX), iz = wrapi(rz.lo + c, g.NY);
+    for (BoxWalk w(threadIdx.x, blockDim.x, rx.n, ry.n, rz.n); w.valid(); w.advance()) {
+        const int ix = rx.lo + w.a, iy = wrapi(ry.lo + w.b, g.NX), iz = wrapi(rz.lo + w.c, g.NY);
         const uint32_t n = gnode(g, ix, iy, iz);
         if (owner[n] != p) continue;
         double d[3];
         offset(P, g, p, ix, iy, iz, d);
-        if (inside(d, P.R)) continue;
+        if (inside_fast(d, P.R)) continue;
         owner[n] = -2;
         const unsigned k = atomicAdd(&P.counters[0], 1u);
         if (k < (unsigned)P.refill_cap) {
@@ -160,56 +221,74 @@ __global__ void __launch_bounds__(kPThreads) k_release(DeviceParticles P, Geomet
 }
 
 // Interpolated bounce-back on every link of sphere blockIdx.x, after a step
-// that left the populations in orientation `parity`.  RT: link arithmetic
-// (FP64 for FP64 storage, FP32 otherwise; FP64 sums per node and per sphere).
+// that left the populations in orientation `parity`.  RT: link arithmetic and
+// q (FP64 for FP64 storage; FP32 for FP32/FP16 storage, where an FP64 q per
+// link would cost more than the fluid step at GB300's FP64 rate), node
+// offsets always from FP64 positions, sums in FP64 per node and per sphere.
+// qc = |d|^2 - R^2 of the node, computed once per node in FP64
+template <typename RT>
+__device__ __forceinline__ RT link_q(const double d[3], int cx, int cy, int cz, double qc) {
+    if constexpr (sizeof(RT) == 8) {
+        const double qa = (double)(cx * cx + cy * cy + cz * cz);
+        const double qb = __dadd_rn(__dadd_rn(d[0] * cx, d[1] * cy), d[2] * cz);
+        double disc = __dsub_rn(__dmul_rn(qb, qb), __dmul_rn(qa, qc));
+        if (disc < 0.0) disc = 0.0;
+        double q = __ddiv_rn(__dsub_rn(-qb, __dsqrt_rn(disc)), qa);
+        return q < 1e-6 ? 1e-6 : (q > 1.0 ? 1.0 : q);
+    } else {
+        const float x = (float)d[0], y = (float)d[1], z = (float)d[2];
+        const float qa = (float)(cx * cx + cy * cy + cz * cz);
+        const float qb = x * cx + y * cy + z * cz;
+        float disc = qb * qb - qa * (float)qc;
+        disc = disc < 0.f ? 0.f : disc;
+        float q = (-qb - sqrtf(disc)) / qa;
+        return q < 1e-6f ? 1e-6f : (q > 1.f ? 1.f : q);
+    }
+}
+
 template <typename T, typename RT>
 __global__ void __launch_bounds__(kPThreads) k_ibb(DeviceState s, DeviceParticles P, int parity) {
     const Geometry& g = s.g;
     const int p = blockIdx.x;
     const double R = P.R;
-    const double* U = P.vel + 3 * p;
-    const double* W = P.omg + 3 * p;
+    const RT U0 = (RT)P.vel[3 * p], U1 = (RT)P.vel[3 * p + 1], U2 = (RT)P.vel[3 * p + 2];
+    const RT W0_ = (RT)P.omg[3 * p], W1_ = (RT)P.omg[3 * p + 1], W2_ = (RT)P.omg[3 * p + 2];
     const int* owner = P.owner;
     const double ext = R + 1.5;
+    const float shell2 = (float)((R + 1.5) * (R + 1.5));
     const Range rx = box(P.pos[3 * p], ext, g.NZ, false);
     const Range ry = box(P.pos[3 * p + 1], ext, g.NX, true);
     const Range rz = box(P.pos[3 * p + 2], ext, g.NY, true);
-    const int total = rx.n * ry.n * rz.n;
     double acc[6] = {0, 0, 0, 0, 0, 0};
     unsigned nl = 0;
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-        const int a = t % rx.n, b = (t / rx.n) % ry.n, c = t / (rx.n * ry.n);
-        const int ix = rx.lo + a, iy = wrapi(ry.lo + b, g.NX), iz = wrapi(rz.lo + c, g.NY);
+    for (BoxWalk w(threadIdx.x, blockDim.x, rx.n, ry.n, rz.n); w.valid(); w.advance()) {
+        const int ix = rx.lo + w.a, iy = wrapi(ry.lo + w.b, g.NX), iz = wrapi(rz.lo + w.c, g.NY);
         if (owner[gnode(g, ix, iy, iz)] != -1) continue;
         double d[3];
         offset(P, g, p, ix, iy, iz, d);
+        {
+            const float x = (float)d[0], y = (float)d[1], z = (float)d[2];
+            if (x * x + y * y + z * z > shell2) continue;       // too far from the surface for a link
+        }
+        const double qc = __dsub_rn(norm2_rn(d), __dmul_rn(R, R));
         RT nacc[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll 1
         for (int i = 1; i < Q; ++i) {
-            const int cx = CXf(i), cy = CYf(i), cz = CZf(i);
+            const int cx = cx_rt(i), cy = cy_rt(i), cz = cz_rt(i);
             const int sx = ix + cx;
             if (sx < 0 || sx >= g.NZ) continue;
             const int sy = wrapi(iy + cy, g.NX), sz = wrapi(iz + cz, g.NY);
             if (owner[gnode(g, sx, sy, sz)] != p) continue;
             ++nl;
-            // boundary-link fraction q (FP64 geometry, as the oracle)
-            const double qa = (double)(cx * cx + cy * cy + cz * cz);
-            const double qb = __dadd_rn(__dadd_rn(d[0] * cx, d[1] * cy), d[2] * cz);
-            const double qc = __dsub_rn(norm2_rn(d), __dmul_rn(R, R));
-            double disc = __dsub_rn(__dmul_rn(qb, qb), __dmul_rn(qa, qc));
-            if (disc < 0.0) disc = 0.0;
-            double qd = __ddiv_rn(__dsub_rn(-qb, __dsqrt_rn(disc)), qa);
-            if (qd < 1e-6) qd = 1e-6;
-            if (qd > 1.0) qd = 1.0;
-            const RT q = (RT)qd;
+            const RT q = link_q<RT>(d, cx, cy, cz, qc);
             // wall point relative to the centre and wall velocity
-            const RT r0 = (RT)(d[0] + qd * cx), r1 = (RT)(d[1] + qd * cy), r2 = (RT)(d[2] + qd * cz);
-            const RT uw0 = (RT)U[0] + ((RT)W[1] * r2 - (RT)W[2] * r1);
-            const RT uw1 = (RT)U[1] + ((RT)W[2] * r0 - (RT)W[0] * r2);
-            const RT uw2 = (RT)U[2] + ((RT)W[0] * r1 - (RT)W[1] * r0);
+            const RT r0 = (RT)d[0] + q * cx, r1 = (RT)d[1] + q * cy, r2 = (RT)d[2] + q * cz;
+            const RT uw0 = U0 + (W1_ * r2 - W2_ * r1);
+            const RT uw1 = U1 + (W2_ * r0 - W0_ * r2);
+            const RT uw2 = U2 + (W0_ * r1 - W1_ * r0);
             const RT cu = (cx * uw0 + cy * uw1) + cz * uw2;
-            const RT mw = RT(-6.0 * weight(i)) * cu;
-            const int ib = OPPf(i);
+            const RT mw = RT(-6.0 * w_rt(i)) * cu;
+            const int ib = opp_rt(i);
             // stencil x_f - c_i, x_f - 2 c_i
             const int ax = ix - cx, bx = ix - 2 * cx;
             bool ok1 = false, ok2 = false;
@@ -295,27 +374,50 @@ __device__ __forceinline__ double repulse(double h, double zeta, double k0, doub
 }
 
 // Soft-sphere repulsion gathered per sphere in index order (old positions).
-__global__ void k_repulsion(DeviceParticles P, Geometry g) {
+// Pairs are screened in FP32 (positions staged in shared memory) with a
+// margin; only pairs within reach get the exact FP64 evaluation.
+constexpr int kRepTile = 128;
+__global__ void __launch_bounds__(kRepTile) k_repulsion(DeviceParticles P, Geometry g) {
+    __shared__ float3 tile[kRepTile];
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= P.npart) return;
+    const bool act = s < P.npart;
     const double R = P.R;
     const double L1 = (double)g.NX, L2 = (double)g.NY;
+    const float fL1 = (float)L1, fL2 = (float)L2;
+    const float reach = (float)(2.0 * R + P.zeta) + 0.01f;
+    const float reach2 = reach * reach;
     double rep[3] = {0.0, 0.0, 0.0};
-    const double xs0 = P.pos[3 * s], xs1 = P.pos[3 * s + 1], xs2 = P.pos[3 * s + 2];
-    for (int t = 0; t < P.npart; ++t) {
-        if (t == s) continue;
-        const double d0 = __dsub_rn(P.pos[3 * t], xs0);
-        const double d1 = dmin_image(__dsub_rn(P.pos[3 * t + 1], xs1), L1);
-        const double d2 = dmin_image(__dsub_rn(P.pos[3 * t + 2], xs2), L2);
-        const double dd[3] = {d0, d1, d2};
-        const double dist = __dsqrt_rn(norm2_rn(dd));
-        const double fm = repulse(__dsub_rn(dist, 2.0 * R), P.zeta, P.stf0, P.stf1);
-        if (fm != 0.0 && dist > 0.0) {
-            rep[0] = __dsub_rn(rep[0], __ddiv_rn(__dmul_rn(fm, d0), dist));
-            rep[1] = __dsub_rn(rep[1], __ddiv_rn(__dmul_rn(fm, d1), dist));
-            rep[2] = __dsub_rn(rep[2], __ddiv_rn(__dmul_rn(fm, d2), dist));
+    const double xs0 = act ? P.pos[3 * s] : 0.0, xs1 = act ? P.pos[3 * s + 1] : 0.0, xs2 = act ? P.pos[3 * s + 2] : 0.0;
+    const float fx0 = (float)xs0, fx1 = (float)xs1, fx2 = (float)xs2;
+    for (int base = 0; base < P.npart; base += kRepTile) {
+        const int j = base + threadIdx.x;
+        if (j < P.npart) tile[threadIdx.x] = make_float3((float)P.pos[3 * j], (float)P.pos[3 * j + 1], (float)P.pos[3 * j + 2]);
+        __syncthreads();
+        const int nt = min(kRepTile, P.npart - base);
+        if (act) {
+            for (int k = 0; k < nt; ++k) {
+                const int t = base + k;
+                if (t == s) continue;
+                float e0 = tile[k].x - fx0, e1 = tile[k].y - fx1, e2 = tile[k].z - fx2;
+                e1 = e1 >= 0.5f * fL1 ? e1 - fL1 : (e1 < -0.5f * fL1 ? e1 + fL1 : e1);
+                e2 = e2 >= 0.5f * fL2 ? e2 - fL2 : (e2 < -0.5f * fL2 ? e2 + fL2 : e2);
+                if (e0 * e0 + e1 * e1 + e2 * e2 > reach2) continue;
+                const double d0 = __dsub_rn(P.pos[3 * t], xs0);
+                const double d1 = dmin_image(__dsub_rn(P.pos[3 * t + 1], xs1), L1);
+                const double d2 = dmin_image(__dsub_rn(P.pos[3 * t + 2], xs2), L2);
+                const double dd[3] = {d0, d1, d2};
+                const double dist = __dsqrt_rn(norm2_rn(dd));
+                const double fm = repulse(__dsub_rn(dist, 2.0 * R), P.zeta, P.stf0, P.stf1);
+                if (fm != 0.0 && dist > 0.0) {
+                    rep[0] = __dsub_rn(rep[0], __ddiv_rn(__dmul_rn(fm, d0), dist));
+                    rep[1] = __dsub_rn(rep[1], __ddiv_rn(__dmul_rn(fm, d1), dist));
+                    rep[2] = __dsub_rn(rep[2], __ddiv_rn(__dmul_rn(fm, d2), dist));
+                }
+            }
         }
+        __syncthreads();
     }
+    if (!act) return;
     const double hl = __dsub_rn(xs0, R), hu = __dsub_rn(__dsub_rn((double)g.NZ, xs0), R);
     rep[0] = __dadd_rn(rep[0], repulse(hl, P.zeta, P.stf0_w, P.stf1_w));
     rep[0] = __dsub_rn(rep[0], repulse(hu, P.zeta, P.stf0_w, P.stf1_w));
@@ -384,11 +486,12 @@ __global__ void k_refill(DeviceState s, DeviceParticles P, int parity) {
     int best = -1, bx = 0, by = 0, bz = 0;
     double bs = -1e300;
     for (int i = 1; i < Q; ++i) {
-        const int sx = ix + CXf(i);
+        const int cx = cx_rt(i), cy = cy_rt(i), cz = cz_rt(i);
+        const int sx = ix + cx;
         if (sx < 0 || sx >= g.NZ) continue;
-        const int sy = wrapi(iy + CYf(i), g.NX), sz = wrapi(iz + CZf(i), g.NY);
+        const int sy = wrapi(iy + cy, g.NX), sz = wrapi(iz + cz, g.NY);
         if (owner[gnode(g, sx, sy, sz)] != -1) continue;
-        double sc = __dadd_rn(__dadd_rn(d[0] * CXf(i), d[1] * CYf(i)), d[2] * CZf(i));
+        double sc = __dadd_rn(__dadd_rn(d[0] * cx, d[1] * cy), d[2] * cz);
         if (i >= 7) sc = __dmul_rn(sc, kInvSqrt2);
         if (sc > bs) { bs = sc; best = i; bx = sx; by = sy; bz = sz; }
     }
@@ -400,11 +503,13 @@ __global__ void k_refill(DeviceState s, DeviceParticles P, int parity) {
     double fe[Q];
     if (best < 0) {
         feq_dev(0.0, uw0, uw1, uw2, fe);
+#pragma unroll
         for (int i = 0; i < Q; ++i) write_nat<T>(s, parity, i, ix, iy, iz, fe[i]);
         return;
     }
     double gq[Q];
     double r = 0.0, a = 0.0, b = 0.0, c = 0.0;
+#pragma unroll
     for (int i = 0; i < Q; ++i) {
         gq[i] = read_nat<T>(s, parity, i, bx, by, bz);
         r = __dadd_rn(r, gq[i]);
@@ -418,6 +523,7 @@ __global__ void k_refill(DeviceState s, DeviceParticles P, int parity) {
     double fn[Q];
     feq_dev(r, a, b, c, fn);
     feq_dev(r, uw0, uw1, uw2, fe);
+#pragma unroll
     for (int i = 0; i < Q; ++i) write_nat<T>(s, parity, i, ix, iy, iz, __dadd_rn(fe[i], __dsub_rn(gq[i], fn[i])));
 }
 
@@ -456,7 +562,7 @@ cudaError_t particles_after_step(const DeviceState& s, const DeviceParticles& P,
         case LBM_PREC_FP32: k_ibb<float, float><<<P.npart, kPThreads, 0, st>>>(s, P, parity); break;
         default: k_ibb<__half, float><<<P.npart, kPThreads, 0, st>>>(s, P, parity); break;
     }
-    k_repulsion<<<(P.npart + 127) / 128, 128, 0, st>>>(P, s.g);
+    k_repulsion<<<(P.npart + kRepTile - 1) / kRepTile, kRepTile, 0, st>>>(P, s.g);
     k_newton<<<(P.npart + 127) / 128, 128, 0, st>>>(P, s.g, s.cd.Fx, s.cd.Fy, s.cd.Fz, have_prev);
     k_release<<<P.npart, kPThreads, 0, st>>>(P, s.g, P.owner);
     k_claim<<<P.npart, kPThreads, 0, st>>>(P, s.g, P.owner);
