@@ -466,8 +466,10 @@ def main():
         import dataclasses
         pkg = importlib.import_module(PKG)
         c = pkg.CHANNEL_CONFIGS[args.config]
+        nodes = args.grid[0] * args.grid[1] * args.grid[2]
         pkg.CHANNEL_CONFIGS[args.config] = dataclasses.replace(
             c, stream=args.grid[0], span=args.grid[1], wall=args.grid[2], h=args.grid[2] / 2,
+            spheres=round(c.spheres * nodes / c.nodes),      # same sphere volume fraction
             name=f"{c.name}@{args.grid[0]}x{args.grid[1]}x{args.grid[2]}")
     if args.impl == "reference":
         run_reference(args, world, rank)

@@ -109,21 +109,35 @@ __device__ __forceinline__ double norm2_rn(const double d[3]) {
 }
 __device__ __forceinline__ bool inside(const double d[3], double R) { return norm2_rn(d) <= __dmul_rn(R, R); }
 
-// Squared distance in FP32 from FP64 offsets: decides the inside test alone
-// when it is far from R^2; the exact FP64 test runs only near the surface.
-__device__ __forceinline__ int inside_fast(const double d[3], double R) {
-    const float x = (float)d[0], y = (float)d[1], z = (float)d[2];
-    const float r2 = x * x + y * y + z * z, R2 = (float)(R * R);
-    const float band = 1e-4f * R2 + 1e-3f;
-    if (r2 < R2 - band) return 1;
-    if (r2 > R2 + band) return 0;
-    return inside(d, R) ? 1 : 0;
+// Inside test screened in FP32 (node and centre coordinates rounded to FP32,
+// error well below the band); only nodes within the band around the surface
+// get the exact FP64 test, which is the one the oracle uses.
+struct Centre { double x, y, z; float fx, fy, fz; };
+__device__ __forceinline__ Centre centre_of(const DeviceParticles& P, int p) {
+    Centre c;
+    c.x = P.pos[3 * p]; c.y = P.pos[3 * p + 1]; c.z = P.pos[3 * p + 2];
+    c.fx = (float)c.x; c.fy = (float)c.y; c.fz = (float)c.z;
+    return c;
+}
+__device__ __forceinline__ float fmin_image(float d, float L) {
+    return d >= 0.5f * L ? d - L : (d < -0.5f * L ? d + L : d);
+}
+__device__ __forceinline__ float dist2_fast(const Centre& c, const Geometry& g, int ix, int iy, int iz) {
+    const float x = ((float)ix + 0.5f) - c.fx;
+    const float y = fmin_image(((float)iy + 0.5f) - c.fy, (float)g.NX);
+    const float z = fmin_image(((float)iz + 0.5f) - c.fz, (float)g.NY);
+    return x * x + y * y + z * z;
+}
+// 1 inside, 0 outside, -1 undecided (needs the exact FP64 test)
+__device__ __forceinline__ int inside_screen(float r2, double R) {
+    const float R2 = (float)(R * R);
+    const float band = 1e-3f * R2 + 0.05f;
+    return r2 < R2 - band ? 1 : (r2 > R2 + band ? 0 : -1);
 }
 
-__device__ __forceinline__ int wrapi(int a, int n) {
-    a %= n;
-    return a < 0 ? a + n : a;
-}
+// periodic wrap of an index within one period of [0, n) (all callers stay
+// within [-n, 2n): box edges and stencils reach at most R + 3 nodes out)
+__device__ __forceinline__ int wrapi(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
 
 // node-index range of a bounding box along one axis (same rule as the oracle)
 struct Range { int lo, n; };
@@ -188,16 +202,22 @@ __global__ void __launch_bounds__(kPThreads) k_claim(DeviceParticles P, Geometry
     const Range rx = box(P.pos[3 * p], P.R, g.NZ, false);
     const Range ry = box(P.pos[3 * p + 1], P.R, g.NX, true);
     const Range rz = box(P.pos[3 * p + 2], P.R, g.NY, true);
+    const Centre c = centre_of(P, p);
     for (BoxWalk w(threadIdx.x, blockDim.x, rx.n, ry.n, rz.n); w.valid(); w.advance()) {
         const int ix = rx.lo + w.a, iy = wrapi(ry.lo + w.b, g.NX), iz = wrapi(rz.lo + w.c, g.NY);
-        double d[3];
-        offset(P, g, p, ix, iy, iz, d);
-        if (inside_fast(d, P.R)) owner[gnode(g, ix, iy, iz)] = p;
+        int in = inside_screen(dist2_fast(c, g, ix, iy, iz), P.R);
+        if (in < 0) {
+            double d[3];
+            offset(P, g, p, ix, iy, iz, d);
+            in = inside(d, P.R);
+        }
+        if (in) owner[gnode(g, ix, iy, iz)] = p;
     }
 }
 
 __global__ void __launch_bounds__(kPThreads) k_release(DeviceParticles P, Geometry g, int* owner) {
     const int p = blockIdx.x;
+    const Centre c = centre_of(P, p);
     const double ext = P.R + 1.5;
     const Range rx = box(P.pos[3 * p], ext, g.NZ, false);
     const Range ry = box(P.pos[3 * p + 1], ext, g.NX, true);
@@ -206,9 +226,13 @@ __global__ void __launch_bounds__(kPThreads) k_release(DeviceParticles P, Geomet
         const int ix = rx.lo + w.a, iy = wrapi(ry.lo + w.b, g.NX), iz = wrapi(rz.lo + w.c, g.NY);
         const uint32_t n = gnode(g, ix, iy, iz);
         if (owner[n] != p) continue;
-        double d[3];
-        offset(P, g, p, ix, iy, iz, d);
-        if (inside_fast(d, P.R)) continue;
+        int in = inside_screen(dist2_fast(c, g, ix, iy, iz), P.R);
+        if (in < 0) {
+            double d[3];
+            offset(P, g, p, ix, iy, iz, d);
+            in = inside(d, P.R);
+        }
+        if (in) continue;
         owner[n] = -2;
         const unsigned k = atomicAdd(&P.counters[0], 1u);
         if (k < (unsigned)P.refill_cap) {
@@ -256,6 +280,7 @@ __global__ void __launch_bounds__(kPThreads) k_ibb(DeviceState s, DeviceParticle
     const int* owner = P.owner;
     const double ext = R + 1.5;
     const float shell2 = (float)((R + 1.5) * (R + 1.5));
+    const Centre cen = centre_of(P, p);
     const Range rx = box(P.pos[3 * p], ext, g.NZ, false);
     const Range ry = box(P.pos[3 * p + 1], ext, g.NX, true);
     const Range rz = box(P.pos[3 * p + 2], ext, g.NY, true);
@@ -264,12 +289,9 @@ __global__ void __launch_bounds__(kPThreads) k_ibb(DeviceState s, DeviceParticle
     for (BoxWalk w(threadIdx.x, blockDim.x, rx.n, ry.n, rz.n); w.valid(); w.advance()) {
         const int ix = rx.lo + w.a, iy = wrapi(ry.lo + w.b, g.NX), iz = wrapi(rz.lo + w.c, g.NY);
         if (owner[gnode(g, ix, iy, iz)] != -1) continue;
+        if (dist2_fast(cen, g, ix, iy, iz) > shell2) continue;   // too far from the surface for a link
         double d[3];
         offset(P, g, p, ix, iy, iz, d);
-        {
-            const float x = (float)d[0], y = (float)d[1], z = (float)d[2];
-            if (x * x + y * y + z * z > shell2) continue;       // too far from the surface for a link
-        }
         const double qc = __dsub_rn(norm2_rn(d), __dmul_rn(R, R));
         RT nacc[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll 1
