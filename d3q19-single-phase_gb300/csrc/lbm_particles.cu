@@ -63,7 +63,8 @@ __device__ __forceinline__ int opp_rt(int i) {
 __device__ __forceinline__ double w_rt(int i) { return i == 0 ? W0 : (i <= 6 ? W1 : W2); }
 
 // Walk a bounding box with a stride of blockDim.x nodes without integer
-// division per node.
+// division per node; callers put the streamwise (contiguous) axis first so
+// that the lanes of a warp touch neighbouring addresses.
 struct BoxWalk {
     int a, b, c, na, nb, nc;
     int sa, sb, sc;                       // the stride in mixed radix (na, nb)
@@ -183,6 +184,22 @@ __device__ __forceinline__ Slot natural_slot(const Geometry& g, int parity, int 
     }
     return s;
 }
+// Same in the link arithmetic type RT (no FP64 conversions for FP32/FP16).
+template <typename T, typename RT>
+__device__ __forceinline__ RT read_nat_r(const DeviceState& s, int parity, int k, int ix, int iy, int iz) {
+    const Slot sl = natural_slot(s.g, parity, k, ix, iy, iz);
+    if constexpr (sizeof(RT) == 8) return (double)ld_pop(plane<T>(s, sl.k) + sl.n) * s.cd.invS;
+    else return (float)ld_pop(plane<T>(s, sl.k) + sl.n) * s.cf.invS;
+}
+template <typename T, typename RT>
+__device__ __forceinline__ void write_nat_r(const DeviceState& s, int parity, int k, int ix, int iy, int iz, RT v) {
+    const Slot sl = natural_slot(s.g, parity, k, ix, iy, iz);
+    T* p = plane<T>(s, sl.k) + sl.n;
+    if constexpr (sizeof(T) == 8) *p = (double)v * s.cd.S;
+    else if constexpr (sizeof(RT) == 8) st_pop(p, (float)(v * s.cd.S));
+    else st_pop(p, v * s.cf.S);
+}
+
 template <typename T>
 __device__ __forceinline__ double read_nat(const DeviceState& s, int parity, int k, int ix, int iy, int iz) {
     const Slot sl = natural_slot(s.g, parity, k, ix, iy, iz);
@@ -203,8 +220,8 @@ __global__ void __launch_bounds__(kPThreads) k_claim(DeviceParticles P, Geometry
     const Range ry = box(P.pos[3 * p + 1], P.R, g.NX, true);
     const Range rz = box(P.pos[3 * p + 2], P.R, g.NY, true);
     const Centre c = centre_of(P, p);
-    for (BoxWalk w(threadIdx.x, blockDim.x, rx.n, ry.n, rz.n); w.valid(); w.advance()) {
-        const int ix = rx.lo + w.a, iy = wrapi(ry.lo + w.b, g.NX), iz = wrapi(rz.lo + w.c, g.NY);
+    for (BoxWalk w(threadIdx.x, blockDim.x, ry.n, rz.n, rx.n); w.valid(); w.advance()) {
+        const int iy = wrapi(ry.lo + w.a, g.NX), iz = wrapi(rz.lo + w.b, g.NY), ix = rx.lo + w.c;
         int in = inside_screen(dist2_fast(c, g, ix, iy, iz), P.R);
         if (in < 0) {
             double d[3];
@@ -222,8 +239,8 @@ __global__ void __launch_bounds__(kPThreads) k_release(DeviceParticles P, Geomet
     const Range rx = box(P.pos[3 * p], ext, g.NZ, false);
     const Range ry = box(P.pos[3 * p + 1], ext, g.NX, true);
     const Range rz = box(P.pos[3 * p + 2], ext, g.NY, true);
-    for (BoxWalk w(threadIdx.x, blockDim.x, rx.n, ry.n, rz.n); w.valid(); w.advance()) {
-        const int ix = rx.lo + w.a, iy = wrapi(ry.lo + w.b, g.NX), iz = wrapi(rz.lo + w.c, g.NY);
+    for (BoxWalk w(threadIdx.x, blockDim.x, ry.n, rz.n, rx.n); w.valid(); w.advance()) {
+        const int iy = wrapi(ry.lo + w.a, g.NX), iz = wrapi(rz.lo + w.b, g.NY), ix = rx.lo + w.c;
         const uint32_t n = gnode(g, ix, iy, iz);
         if (owner[n] != p) continue;
         int in = inside_screen(dist2_fast(c, g, ix, iy, iz), P.R);
@@ -286,13 +303,14 @@ __global__ void __launch_bounds__(kPThreads) k_ibb(DeviceState s, DeviceParticle
     const Range rz = box(P.pos[3 * p + 2], ext, g.NY, true);
     double acc[6] = {0, 0, 0, 0, 0, 0};
     unsigned nl = 0;
-    for (BoxWalk w(threadIdx.x, blockDim.x, rx.n, ry.n, rz.n); w.valid(); w.advance()) {
-        const int ix = rx.lo + w.a, iy = wrapi(ry.lo + w.b, g.NX), iz = wrapi(rz.lo + w.c, g.NY);
+    for (BoxWalk w(threadIdx.x, blockDim.x, ry.n, rz.n, rx.n); w.valid(); w.advance()) {
+        const int iy = wrapi(ry.lo + w.a, g.NX), iz = wrapi(rz.lo + w.b, g.NY), ix = rx.lo + w.c;
         if (owner[gnode(g, ix, iy, iz)] != -1) continue;
         if (dist2_fast(cen, g, ix, iy, iz) > shell2) continue;   // too far from the surface for a link
         double d[3];
         offset(P, g, p, ix, iy, iz, d);
         const double qc = __dsub_rn(norm2_rn(d), __dmul_rn(R, R));
+        const RT dr0 = (RT)d[0], dr1 = (RT)d[1], dr2 = (RT)d[2];
         RT nacc[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll 1
         for (int i = 1; i < Q; ++i) {
@@ -304,12 +322,12 @@ __global__ void __launch_bounds__(kPThreads) k_ibb(DeviceState s, DeviceParticle
             ++nl;
             const RT q = link_q<RT>(d, cx, cy, cz, qc);
             // wall point relative to the centre and wall velocity
-            const RT r0 = (RT)d[0] + q * cx, r1 = (RT)d[1] + q * cy, r2 = (RT)d[2] + q * cz;
+            const RT r0 = dr0 + q * cx, r1 = dr1 + q * cy, r2 = dr2 + q * cz;
             const RT uw0 = U0 + (W1_ * r2 - W2_ * r1);
             const RT uw1 = U1 + (W2_ * r0 - W0_ * r2);
             const RT uw2 = U2 + (W0_ * r1 - W1_ * r0);
             const RT cu = (cx * uw0 + cy * uw1) + cz * uw2;
-            const RT mw = RT(-6.0 * w_rt(i)) * cu;
+            const RT mw = (i <= 6 ? RT(-6.0 * (1.0 / 18.0)) : RT(-6.0 * (1.0 / 36.0))) * cu;
             const int ib = opp_rt(i);
             // stencil x_f - c_i, x_f - 2 c_i
             const int ax = ix - cx, bx = ix - 2 * cx;
@@ -323,33 +341,33 @@ __global__ void __launch_bounds__(kPThreads) k_ibb(DeviceState s, DeviceParticle
                 by = wrapi(iy - 2 * cy, g.NX); bz = wrapi(iz - 2 * cz, g.NY);
                 ok2 = owner[gnode(g, bx, by, bz)] == -1;
             }
-            const RT A = (RT)read_nat<T>(s, parity, i, sx, sy, sz);
+            const RT A = read_nat_r<T, RT>(s, parity, i, sx, sy, sz);
             RT fn;
             if (q < RT(0.5)) {
                 if (ok2) {
-                    const RT B = (RT)read_nat<T>(s, parity, i, ix, iy, iz);
-                    const RT C = (RT)read_nat<T>(s, parity, i, ax, ay, az);
+                    const RT B = read_nat_r<T, RT>(s, parity, i, ix, iy, iz);
+                    const RT C = read_nat_r<T, RT>(s, parity, i, ax, ay, az);
                     fn = q * (RT(1) + RT(2) * q) * A + (RT(1) - RT(4) * q * q) * B + q * (RT(2) * q - RT(1)) * C + mw;
                 } else if (ok1) {
-                    const RT B = (RT)read_nat<T>(s, parity, i, ix, iy, iz);
+                    const RT B = read_nat_r<T, RT>(s, parity, i, ix, iy, iz);
                     fn = RT(2) * q * A + (RT(1) - RT(2) * q) * B + mw;
                 } else {
                     fn = A + mw;
                 }
             } else {
                 if (ok2) {
-                    const RT D = (RT)read_nat<T>(s, parity, ib, ax, ay, az);
-                    const RT E = (RT)read_nat<T>(s, parity, ib, bx, by, bz);
+                    const RT D = read_nat_r<T, RT>(s, parity, ib, ax, ay, az);
+                    const RT E = read_nat_r<T, RT>(s, parity, ib, bx, by, bz);
                     const RT k = RT(1) / (q * (RT(2) * q + RT(1)));
                     fn = k * A + (RT(2) * q - RT(1)) / q * D - (RT(2) * q - RT(1)) / (RT(2) * q + RT(1)) * E + k * mw;
                 } else if (ok1) {
-                    const RT D = (RT)read_nat<T>(s, parity, ib, ax, ay, az);
+                    const RT D = read_nat_r<T, RT>(s, parity, ib, ax, ay, az);
                     fn = (A + mw) / (RT(2) * q) + (RT(2) * q - RT(1)) / (RT(2) * q) * D;
                 } else {
                     fn = A + mw;
                 }
             }
-            write_nat<T>(s, parity, ib, ix, iy, iz, (double)fn);
+            write_nat_r<T, RT>(s, parity, ib, ix, iy, iz, fn);
             // Galilean-invariant momentum exchange
             const RT sA = A + fn, dA = fn - A;
             const RT p0 = cx * sA + uw0 * dA, p1 = cy * sA + uw1 * dA, p2 = cz * sA + uw2 * dA;
