@@ -789,6 +789,12 @@ int lbm_particles_set(lbm_ctx* c, const lbm_particle_params* pp, const double* p
     if (check_ctx(c) || !pp || (pp->npart > 0 && !pos)) return fail(LBM_ERR_INVALID_ARG, "null argument");
     if (pp->npart < 0 || !(pp->radius > 0.0) || !(pp->rho_ratio > 0.0) || !(pp->zeta > 0.0))
         return fail(LBM_ERR_INVALID_ARG, "bad sphere parameters");
+    // the bounce-back kernel stages a sphere's bounding box in shared memory,
+    // and the periodic spans must hold a sphere with its stencil reach
+    if (lbm::particles_smem_bytes(pp->radius) > 227u * 1024u)
+        return fail(LBM_ERR_INVALID_ARG, "sphere radius too large (at most 24 lattice units)");
+    if (pp->npart > 0 && ((double)c->p.ny < 2.0 * pp->radius + 6.0 || (double)c->p.nz < 2.0 * pp->radius + 6.0))
+        return fail(LBM_ERR_INVALID_ARG, "periodic span smaller than 2*radius + 6");
     for (int32_t k = 0; k < pp->npart; ++k) {
         const double x = pos[3 * k];
         if (!(x - pp->radius > 0.0) || !(x + pp->radius < (double)c->p.nx))

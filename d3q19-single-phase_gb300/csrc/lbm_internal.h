@@ -125,6 +125,8 @@ __host__ __device__ inline double uniform_pm1(uint64_t seed, uint64_t key) {
 }
 
 // moving spheres (lbm_particles.cu)
+// dynamic shared memory of the bounce-back kernel for spheres of radius R
+size_t particles_smem_bytes(double R);
 cudaError_t particles_claim(const DeviceState& s, const DeviceParticles& P, cudaStream_t st);
 cudaError_t particles_after_step(const DeviceState& s, const DeviceParticles& P, int parity, int have_prev,
                                  cudaStream_t st);

@@ -200,6 +200,19 @@ __device__ __forceinline__ void write_nat_r(const DeviceState& s, int parity, in
     else st_pop(p, v * s.cf.S);
 }
 
+// population at a storage address, in the link arithmetic type RT
+template <typename T, typename RT>
+__device__ __forceinline__ RT pop_r(const DeviceState& s, const T* a) {
+    if constexpr (sizeof(RT) == 8) return (double)ld_pop(a) * s.cd.invS;
+    else return (float)ld_pop(a) * s.cf.invS;
+}
+template <typename T, typename RT>
+__device__ __forceinline__ void put_r(const DeviceState& s, T* a, RT v) {
+    if constexpr (sizeof(T) == 8) *a = (double)v * s.cd.S;
+    else if constexpr (sizeof(RT) == 8) st_pop(a, (float)(v * s.cd.S));
+    else st_pop(a, v * s.cf.S);
+}
+
 template <typename T>
 __device__ __forceinline__ double read_nat(const DeviceState& s, int parity, int k, int ix, int iy, int iz) {
     const Slot sl = natural_slot(s.g, parity, k, ix, iy, iz);
@@ -287,122 +300,235 @@ __device__ __forceinline__ RT link_q(const double d[3], int cx, int cy, int cz, 
     }
 }
 
+constexpr int kBucket = 512;                           // links per direction bucket
+constexpr int kBucketBytes = (Q - 1) * kBucket * 4;
+
+// Interpolated bounce-back on every link of sphere blockIdx.x, after a step
+// that left the populations in orientation `parity`.
+//
+// Staging: the owner values of the sphere's bounding box plus a two-node
+// stencil margin are loaded once into shared memory as one byte per node
+// (0 fluid, 1 this sphere, 2 another sphere, a node being refilled or beyond
+// a wall).  Phase 1 finds the links of a batch of box nodes (one node per
+// thread) from those bytes and appends them, with warp-aggregated counts, to
+// 18 per-direction buckets; when a bucket could overflow, or at the end,
+// phase 2 processes the buckets direction by direction with every lane on a
+// link of the same direction, so that the population gathers of a warp fall
+// on neighbouring streamwise addresses.
+//
+// With the AA orientation the six accesses of a link touch the four nodes
+// x_f + c_i (solid), x_f, x_f - c_i, x_f - 2c_i in the planes i and opp(i):
+// orientation 1 swaps the two planes and moves the slot-i accesses by -c_i
+// and the slot-opp(i) accesses by +c_i.
+//
+// RT: link arithmetic and q (FP64 for FP64 storage; FP32 for FP32/FP16
+// storage, where an FP64 q per link would cost more than the fluid step at
+// GB300's FP64 rate); force and torque are summed in FP64 per thread and per
+// sphere.
 template <typename T, typename RT>
-__global__ void __launch_bounds__(kPThreads) k_ibb(DeviceState s, DeviceParticles P, int parity) {
+__global__ void __launch_bounds__(kPThreads, sizeof(RT) == 8 ? 2 : 4) k_ibb(DeviceState s, DeviceParticles P, int parity) {
+    extern __shared__ __align__(16) unsigned char ibb_smem[];
+    uint32_t* bucket = reinterpret_cast<uint32_t*>(ibb_smem);     // [Q-1][kBucket] packed (a,b,c)
+    uint8_t* flag = ibb_smem + kBucketBytes;                        // staged owner bytes
+    __shared__ int cnt[Q - 1];
     const Geometry& g = s.g;
     const int p = blockIdx.x;
     const double R = P.R;
-    const RT U0 = (RT)P.vel[3 * p], U1 = (RT)P.vel[3 * p + 1], U2 = (RT)P.vel[3 * p + 2];
-    const RT W0_ = (RT)P.omg[3 * p], W1_ = (RT)P.omg[3 * p + 1], W2_ = (RT)P.omg[3 * p + 2];
-    const int* owner = P.owner;
+    const int* __restrict__ owner = P.owner;
     const double ext = R + 1.5;
-    const float shell2 = (float)((R + 1.5) * (R + 1.5));
-    const Centre cen = centre_of(P, p);
     const Range rx = box(P.pos[3 * p], ext, g.NZ, false);
     const Range ry = box(P.pos[3 * p + 1], ext, g.NX, true);
     const Range rz = box(P.pos[3 * p + 2], ext, g.NY, true);
+    const int SA = ry.n + 4, SB = rz.n + 4, SC = rx.n + 4, SAB = SA * SB;
+    if (threadIdx.x < Q - 1) cnt[threadIdx.x] = 0;
+    {
+        BoxWalk w(threadIdx.x, blockDim.x, SA, SB, SC);
+        const int tot = SAB * SC;
+        for (int done = 0; done < tot; done += 4 * (int)blockDim.x) {
+            int o[4], li[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                li[u] = -1;
+                o[u] = -3;
+                if (w.valid()) {
+                    li[u] = w.a + SA * w.b + SAB * w.c;
+                    const int ix = rx.lo - 2 + w.c;
+                    if (ix >= 0 && ix < g.NZ)
+                        o[u] = __ldg(owner + gnode(g, ix, wrapi(ry.lo - 2 + w.a, g.NX), wrapi(rz.lo - 2 + w.b, g.NY)));
+                    w.advance();
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (li[u] >= 0) flag[li[u]] = o[u] == -1 ? 0 : (o[u] == p ? 1 : 2);
+        }
+    }
+    // per-sphere constants of the link arithmetic
+    const Centre cen = centre_of(P, p);
+    const float shell2 = (float)((R + 1.5) * (R + 1.5));
+    const int cix = (int)floor(cen.x), ciy = (int)floor(cen.y), ciz = (int)floor(cen.z);
+    const float hfx = 0.5f - (float)(cen.x - cix), hfy = 0.5f - (float)(cen.y - ciy), hfz = 0.5f - (float)(cen.z - ciz);
+    const float R2f = (float)(R * R);
+    const double R2 = __dmul_rn(R, R);
+    const RT U0 = (RT)P.vel[3 * p], U1 = (RT)P.vel[3 * p + 1], U2 = (RT)P.vel[3 * p + 2];
+    const RT Wx = (RT)P.omg[3 * p], Wy = (RT)P.omg[3 * p + 1], Wz = (RT)P.omg[3 * p + 2];
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
     double acc[6] = {0, 0, 0, 0, 0, 0};
     unsigned nl = 0;
-    for (BoxWalk w(threadIdx.x, blockDim.x, ry.n, rz.n, rx.n); w.valid(); w.advance()) {
-        const int iy = wrapi(ry.lo + w.a, g.NX), iz = wrapi(rz.lo + w.b, g.NY), ix = rx.lo + w.c;
-        if (owner[gnode(g, ix, iy, iz)] != -1) continue;
-        if (dist2_fast(cen, g, ix, iy, iz) > shell2) continue;   // too far from the surface for a link
-        double d[3];
-        offset(P, g, p, ix, iy, iz, d);
-        const double qc = __dsub_rn(norm2_rn(d), __dmul_rn(R, R));
-        const RT dr0 = (RT)d[0], dr1 = (RT)d[1], dr2 = (RT)d[2];
+    __syncthreads();
+    const int total = rx.n * ry.n * rz.n;
+    const int rounds = (total + blockDim.x - 1) / blockDim.x;
+    BoxWalk w(threadIdx.x, blockDim.x, ry.n, rz.n, rx.n);
+    for (int round = 0; round < rounds; ++round) {
+        // phase 1: links of this thread's node, from the staged bytes
+        unsigned mask = 0;
+        uint32_t packed = 0;
+        if (w.valid()) {
+            const int base = (w.a + 2) + SA * (w.b + 2) + SAB * (w.c + 2);
+            packed = (uint32_t)w.a | ((uint32_t)w.b << 8) | ((uint32_t)w.c << 16);
+            if (flag[base] == 0 &&
+                dist2_fast(cen, g, rx.lo + w.c, wrapi(ry.lo + w.a, g.NX), wrapi(rz.lo + w.b, g.NY)) <= shell2) {
+#pragma unroll
+                for (int i = 1; i < Q; ++i)
+                    if (flag[base + CYf(i) + SA * CZf(i) + SAB * CXf(i)] == 1) mask |= 1u << i;
+            }
+            w.advance();
+        }
+        int over = 0;
+#pragma unroll
+        for (int i = 1; i < Q; ++i) {
+            const bool has = (mask >> i) & 1u;
+            const unsigned bal = __ballot_sync(0xffffffffu, has);
+            if (!bal) continue;
+            int b0 = 0;
+            if (lane == 0) {
+                b0 = atomicAdd(&cnt[i - 1], __popc(bal));
+                over |= b0 + __popc(bal) > kBucket - (int)blockDim.x;
+            }
+            b0 = __shfl_sync(0xffffffffu, b0, 0);
+            if (has) bucket[(i - 1) * kBucket + b0 + __popc(bal & lt)] = packed;
+        }
+        if (!__syncthreads_or(over) && round != rounds - 1) continue;
+        // phase 2: the buckets, one direction at a time
         RT nacc[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll 1
         for (int i = 1; i < Q; ++i) {
-            const int cx = cx_rt(i), cy = cy_rt(i), cz = cz_rt(i);
-            const int sx = ix + cx;
-            if (sx < 0 || sx >= g.NZ) continue;
-            const int sy = wrapi(iy + cy, g.NX), sz = wrapi(iz + cz, g.NY);
-            if (owner[gnode(g, sx, sy, sz)] != p) continue;
-            ++nl;
-            const RT q = link_q<RT>(d, cx, cy, cz, qc);
-            // wall point relative to the centre and wall velocity
-            const RT r0 = dr0 + q * cx, r1 = dr1 + q * cy, r2 = dr2 + q * cz;
-            const RT uw0 = U0 + (W1_ * r2 - W2_ * r1);
-            const RT uw1 = U1 + (W2_ * r0 - W0_ * r2);
-            const RT uw2 = U2 + (W0_ * r1 - W1_ * r0);
-            const RT cu = (cx * uw0 + cy * uw1) + cz * uw2;
-            const RT mw = (i <= 6 ? RT(-6.0 * (1.0 / 18.0)) : RT(-6.0 * (1.0 / 36.0))) * cu;
-            const int ib = opp_rt(i);
-            // stencil x_f - c_i, x_f - 2 c_i
-            const int ax = ix - cx, bx = ix - 2 * cx;
-            bool ok1 = false, ok2 = false;
-            int ay = 0, az = 0, by = 0, bz = 0;
-            if (ax >= 0 && ax < g.NZ) {
-                ay = wrapi(iy - cy, g.NX); az = wrapi(iz - cz, g.NY);
-                ok1 = owner[gnode(g, ax, ay, az)] == -1;
-            }
-            if (ok1 && bx >= 0 && bx < g.NZ) {
-                by = wrapi(iy - 2 * cy, g.NX); bz = wrapi(iz - 2 * cz, g.NY);
-                ok2 = owner[gnode(g, bx, by, bz)] == -1;
-            }
-            const RT A = read_nat_r<T, RT>(s, parity, i, sx, sy, sz);
-            RT fn;
-            if (q < RT(0.5)) {
-                if (ok2) {
-                    const RT B = read_nat_r<T, RT>(s, parity, i, ix, iy, iz);
-                    const RT C = read_nat_r<T, RT>(s, parity, i, ax, ay, az);
-                    fn = q * (RT(1) + RT(2) * q) * A + (RT(1) - RT(4) * q * q) * B + q * (RT(2) * q - RT(1)) * C + mw;
-                } else if (ok1) {
-                    const RT B = read_nat_r<T, RT>(s, parity, i, ix, iy, iz);
-                    fn = RT(2) * q * A + (RT(1) - RT(2) * q) * B + mw;
+            const int n = cnt[i - 1];
+            if (threadIdx.x == 0) nl += n;
+            const int cx = cx_rt(i), cy = cy_rt(i), cz = cz_rt(i), ib = opp_rt(i);
+            const int off = cy + SA * cz + SAB * cx;
+            const RT qa = (RT)(cx * cx + cy * cy + cz * cz);
+            const RT mw6 = RT(-6) * (RT)w_rt(i);
+            const T* __restrict__ Pi = plane<T>(s, i);
+            const T* __restrict__ Pib = plane<T>(s, ib);
+            for (int e = threadIdx.x; e < n; e += blockDim.x) {
+                const uint32_t v = bucket[(i - 1) * kBucket + e];
+                const int a = v & 255, b = (v >> 8) & 255, c = (v >> 16) & 255;
+                const int base = (a + 2) + SA * (b + 2) + SAB * (c + 2);
+                const bool ok1 = flag[base - off] == 0;
+                const bool ok2 = ok1 && flag[base - 2 * off] == 0;
+                const int ix = rx.lo + c, iy = wrapi(ry.lo + a, g.NX), iz = wrapi(rz.lo + b, g.NY);
+                RT q, d0, d1, d2;
+                if constexpr (sizeof(RT) == 8) {
+                    double d[3];
+                    offset(P, g, p, ix, iy, iz, d);
+                    q = link_q<double>(d, cx, cy, cz, __dsub_rn(norm2_rn(d), R2));
+                    d0 = d[0]; d1 = d[1]; d2 = d[2];
                 } else {
-                    fn = A + mw;
+                    // offsets from the integer part of the centre: exact
+                    // integers plus an FP32 fraction (no FP64 per link)
+                    int oy = iy - ciy, oz = iz - ciz;
+                    oy = oy >= g.NX / 2 ? oy - g.NX : (oy < -(g.NX / 2) ? oy + g.NX : oy);
+                    oz = oz >= g.NY / 2 ? oz - g.NY : (oz < -(g.NY / 2) ? oz + g.NY : oz);
+                    d0 = (float)(ix - cix) + hfx;
+                    d1 = (float)oy + hfy;
+                    d2 = (float)oz + hfz;
+                    const float qc = d0 * d0 + d1 * d1 + d2 * d2 - R2f;
+                    const float qb = d0 * cx + d1 * cy + d2 * cz;
+                    float disc = qb * qb - qa * qc;
+                    disc = disc < 0.f ? 0.f : disc;
+                    q = (-qb - sqrtf(disc)) / qa;
+                    q = q < 1e-6f ? 1e-6f : (q > 1.f ? 1.f : q);
                 }
-            } else {
-                if (ok2) {
-                    const RT D = read_nat_r<T, RT>(s, parity, ib, ax, ay, az);
-                    const RT E = read_nat_r<T, RT>(s, parity, ib, bx, by, bz);
-                    const RT k = RT(1) / (q * (RT(2) * q + RT(1)));
-                    fn = k * A + (RT(2) * q - RT(1)) / q * D - (RT(2) * q - RT(1)) / (RT(2) * q + RT(1)) * E + k * mw;
-                } else if (ok1) {
-                    const RT D = read_nat_r<T, RT>(s, parity, ib, ax, ay, az);
-                    fn = (A + mw) / (RT(2) * q) + (RT(2) * q - RT(1)) / (RT(2) * q) * D;
+                const RT r0 = d0 + q * cx, r1 = d1 + q * cy, r2 = d2 + q * cz;
+                const RT uw0 = U0 + (Wy * r2 - Wz * r1);
+                const RT uw1 = U1 + (Wz * r0 - Wx * r2);
+                const RT uw2 = U2 + (Wx * r1 - Wy * r0);
+                const RT mw = mw6 * ((cx * uw0 + cy * uw1) + cz * uw2);
+                // the four nodes of the link
+                const uint32_t gx = gnode(g, ix, iy, iz);
+                const uint32_t gs = gnode(g, ix + cx, wrapi(iy + cy, g.NX), wrapi(iz + cz, g.NY));
+                uint32_t ga = 0, gb = 0;
+                if (ok1) ga = gnode(g, ix - cx, wrapi(iy - cy, g.NX), wrapi(iz - cz, g.NY));
+                if (ok2) gb = gnode(g, ix - 2 * cx, wrapi(iy - 2 * cy, g.NX), wrapi(iz - 2 * cz, g.NY));
+                const T* pA = parity ? Pib + gx : Pi + gs;
+                const RT A = pop_r<T, RT>(s, pA);
+                RT fn;
+                if (q < RT(0.5)) {
+                    if (ok2) {
+                        const RT B = pop_r<T, RT>(s, parity ? Pib + ga : Pi + gx);
+                        const RT C = pop_r<T, RT>(s, parity ? Pib + gb : Pi + ga);
+                        fn = q * (RT(1) + RT(2) * q) * A + (RT(1) - RT(4) * q * q) * B + q * (RT(2) * q - RT(1)) * C + mw;
+                    } else if (ok1) {
+                        const RT B = pop_r<T, RT>(s, parity ? Pib + ga : Pi + gx);
+                        fn = RT(2) * q * A + (RT(1) - RT(2) * q) * B + mw;
+                    } else {
+                        fn = A + mw;
+                    }
                 } else {
-                    fn = A + mw;
+                    if (ok2) {
+                        const RT D = pop_r<T, RT>(s, parity ? Pi + gx : Pib + ga);
+                        const RT E = pop_r<T, RT>(s, parity ? Pi + ga : Pib + gb);
+                        const RT k = RT(1) / (q * (RT(2) * q + RT(1)));
+                        fn = k * A + (RT(2) * q - RT(1)) / q * D - (RT(2) * q - RT(1)) / (RT(2) * q + RT(1)) * E + k * mw;
+                    } else if (ok1) {
+                        const RT D = pop_r<T, RT>(s, parity ? Pi + gx : Pib + ga);
+                        fn = (A + mw) / (RT(2) * q) + (RT(2) * q - RT(1)) / (RT(2) * q) * D;
+                    } else {
+                        fn = A + mw;
+                    }
                 }
+                put_r<T, RT>(s, const_cast<T*>(parity ? Pi + gs : Pib + gx), fn);
+                // Galilean-invariant momentum exchange
+                const RT sA = A + fn, dA = fn - A;
+                const RT p0 = cx * sA + uw0 * dA, p1 = cy * sA + uw1 * dA, p2 = cz * sA + uw2 * dA;
+                nacc[0] += p0; nacc[1] += p1; nacc[2] += p2;
+                nacc[3] += r1 * p2 - r2 * p1;
+                nacc[4] += r2 * p0 - r0 * p2;
+                nacc[5] += r0 * p1 - r1 * p0;
             }
-            write_nat_r<T, RT>(s, parity, ib, ix, iy, iz, fn);
-            // Galilean-invariant momentum exchange
-            const RT sA = A + fn, dA = fn - A;
-            const RT p0 = cx * sA + uw0 * dA, p1 = cy * sA + uw1 * dA, p2 = cz * sA + uw2 * dA;
-            nacc[0] += p0; nacc[1] += p1; nacc[2] += p2;
-            nacc[3] += r1 * p2 - r2 * p1;
-            nacc[4] += r2 * p0 - r0 * p2;
-            nacc[5] += r0 * p1 - r1 * p0;
         }
 #pragma unroll
         for (int k = 0; k < 6; ++k) acc[k] += (double)nacc[k];
+        __syncthreads();
+        if (threadIdx.x < Q - 1) cnt[threadIdx.x] = 0;
+        __syncthreads();
     }
     // per-sphere FP64 reduction: warp shuffles, then across warps
     __shared__ double sh[6][kPThreads / 32];
-    __shared__ unsigned shn[kPThreads / 32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int wid = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
         double v = acc[k];
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
         if (lane == 0) sh[k][wid] = v;
     }
-    for (int o = 16; o > 0; o >>= 1) nl += __shfl_down_sync(0xffffffffu, nl, o);
-    if (lane == 0) shn[wid] = nl;
     __syncthreads();
     if (threadIdx.x < 6) {
         double v = 0.0;
-        for (int w = 0; w < kPThreads / 32; ++w) v += sh[threadIdx.x][w];
+        for (int ww = 0; ww < kPThreads / 32; ++ww) v += sh[threadIdx.x][ww];
         if (threadIdx.x < 3) P.force[3 * p + threadIdx.x] = v;
         else P.torque[3 * p + threadIdx.x - 3] = v;
     }
-    if (threadIdx.x == 0) {
-        unsigned n = 0;
-        for (int w = 0; w < kPThreads / 32; ++w) n += shn[w];
-        atomicAdd(&P.counters[1], n);
-    }
+    if (threadIdx.x == 0) atomicAdd(&P.counters[1], nl);
+}
+
+// dynamic shared memory of k_ibb for spheres of radius R: the buckets and the
+// staged owner bytes of the largest bounding box plus its stencil margin
+size_t ibb_smem_bytes(double R) {
+    const int n = (int)std::floor(2.0 * (R + 1.5)) + 2 + 4;
+    return (size_t)kBucketBytes + (((size_t)n * n * n + 15) & ~(size_t)15);
 }
 
 __device__ __forceinline__ double repulse(double h, double zeta, double k0, double k1) {
@@ -585,6 +711,8 @@ __global__ void k_count_solid(const int* owner, size_t N, unsigned long long* ou
 
 }  // namespace
 
+size_t particles_smem_bytes(double R) { return ibb_smem_bytes(R); }
+
 cudaError_t particles_claim(const DeviceState& s, const DeviceParticles& P, cudaStream_t st) {
     if (P.npart == 0) return cudaSuccess;
     k_claim<<<P.npart, kPThreads, 0, st>>>(P, s.g, P.owner);
@@ -597,11 +725,22 @@ cudaError_t particles_after_step(const DeviceState& s, const DeviceParticles& P,
     if (P.npart == 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(P.counters, 0, 2 * sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
+    const size_t smem = ibb_smem_bytes(P.R);
     switch (s.prec) {
-        case LBM_PREC_FP64: k_ibb<double, double><<<P.npart, kPThreads, 0, st>>>(s, P, parity); break;
-        case LBM_PREC_FP32: k_ibb<float, float><<<P.npart, kPThreads, 0, st>>>(s, P, parity); break;
-        default: k_ibb<__half, float><<<P.npart, kPThreads, 0, st>>>(s, P, parity); break;
+        case LBM_PREC_FP64:
+            e = cudaFuncSetAttribute(k_ibb<double, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e == cudaSuccess) k_ibb<double, double><<<P.npart, kPThreads, smem, st>>>(s, P, parity);
+            break;
+        case LBM_PREC_FP32:
+            e = cudaFuncSetAttribute(k_ibb<float, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e == cudaSuccess) k_ibb<float, float><<<P.npart, kPThreads, smem, st>>>(s, P, parity);
+            break;
+        default:
+            e = cudaFuncSetAttribute(k_ibb<__half, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e == cudaSuccess) k_ibb<__half, float><<<P.npart, kPThreads, smem, st>>>(s, P, parity);
+            break;
     }
+    if (e != cudaSuccess) return e;
     k_repulsion<<<(P.npart + kRepTile - 1) / kRepTile, kRepTile, 0, st>>>(P, s.g);
     k_newton<<<(P.npart + 127) / 128, 128, 0, st>>>(P, s.g, s.cd.Fx, s.cd.Fy, s.cd.Fz, have_prev);
     k_release<<<P.npart, kPThreads, 0, st>>>(P, s.g, P.owner);
