@@ -300,236 +300,359 @@ __device__ __forceinline__ RT link_q(const double d[3], int cx, int cy, int cz, 
     }
 }
 
-constexpr int kBucket = 512;                           // links per direction bucket
-constexpr int kBucketBytes = (Q - 1) * kBucket * 4;
-
-// Interpolated bounce-back on every link of sphere blockIdx.x, after a step
-// that left the populations in orientation `parity`.
+// ---------------------------------------------------------------------------
+// Interpolated bounce-back.
 //
-// Staging: the owner values of the sphere's bounding box plus a two-node
-// stencil margin are loaded once into shared memory as one byte per node
-// (0 fluid, 1 this sphere, 2 another sphere, a node being refilled or beyond
-// a wall).  Phase 1 finds the links of a batch of box nodes (one node per
-// thread) from those bytes and appends them, with warp-aggregated counts, to
-// 18 per-direction buckets; when a bucket could overflow, or at the end,
-// phase 2 processes the buckets direction by direction with every lane on a
-// link of the same direction, so that the population gathers of a warp fall
-// on neighbouring streamwise addresses.
+// One CTA per sphere.  The owner values of the sphere's bounding box plus a
+// two-node stencil margin are staged once in shared memory as one byte per
+// node (0 fluid, 1 this sphere, 2 another sphere, a node being refilled or
+// beyond a wall), together with per-axis tables of the FP32 offset from the
+// sphere centre and of the node index.  Phase 1 walks the candidate nodes
+// (one per thread, streamwise fastest), finds their links from the staged
+// bytes and appends them, with warp-aggregated counts, to 18 per-direction
+// buckets.  Phase 2 cuts the buckets into chunks of 32 links of one direction
+// and deals the chunks to the warps, so that every lane of a warp works on the
+// same direction at neighbouring streamwise nodes.  A link that finds its
+// bucket full is processed at once by the thread that found it.
 //
 // With the AA orientation the six accesses of a link touch the four nodes
 // x_f + c_i (solid), x_f, x_f - c_i, x_f - 2c_i in the planes i and opp(i):
 // orientation 1 swaps the two planes and moves the slot-i accesses by -c_i
 // and the slot-opp(i) accesses by +c_i.
 //
-// RT: link arithmetic and q (FP64 for FP64 storage; FP32 for FP32/FP16
-// storage, where an FP64 q per link would cost more than the fluid step at
-// GB300's FP64 rate); force and torque are summed in FP64 per thread and per
-// sphere.
+// RT: link arithmetic and q (FP64 with correctly rounded operations for FP64
+// storage, bit-consistent with the oracle; FP32 with hardware reciprocals for
+// FP32/FP16 storage, where an FP64 q per link would cost more than the fluid
+// step at GB300's FP64 rate).  Force and torque are summed in FP64 per thread
+// and per sphere.
+
+// staged box of one sphere, in shared memory
+struct IbbBox {
+    int SA, SAB;                  // strides of the staged byte box
+    int A0;                       // staged streamwise index of candidate a = 0
+    const uint8_t* flag;          // [SC][SB][SA]
+    const float *tA, *tB, *tC;    // FP32 offset from the centre per staged index
+    const int *wA, *wB, *wC;      // node-index terms per staged index
+    const int* wZ;                // wrapped spanwise index per staged b (FP64 path)
+    int xlo;                      // wall-normal node of staged c = 0
+    float R2f;                    // R^2 in FP32
+};
+
+// per-direction constants (warp-uniform in phase 2)
 template <typename T, typename RT>
-__global__ void __launch_bounds__(kPThreads, sizeof(RT) == 8 ? 2 : 4) k_ibb(DeviceState s, DeviceParticles P, int parity) {
+struct IbbDir {
+    int i, cx, cy, cz, off;
+    RT fcx, fcy, fcz, mw6, qa, inv_qa;
+    const T* Pi;
+    const T* Pib;
+};
+template <typename T, typename RT>
+__device__ __forceinline__ IbbDir<T, RT> ibb_dir(const DeviceState& s, const IbbBox& B, int i) {
+    IbbDir<T, RT> d;
+    d.i = i;
+    d.cx = cx_rt(i); d.cy = cy_rt(i); d.cz = cz_rt(i);
+    d.off = d.cy + B.SA * d.cz + B.SAB * d.cx;
+    d.fcx = (RT)d.cx; d.fcy = (RT)d.cy; d.fcz = (RT)d.cz;
+    d.mw6 = (RT)(-6.0 * w_rt(i));
+    d.qa = (RT)(d.cx * d.cx + d.cy * d.cy + d.cz * d.cz);
+    d.inv_qa = d.qa == RT(1) ? RT(1) : RT(0.5);
+    d.Pi = plane<T>(s, i);
+    d.Pib = plane<T>(s, opp_rt(i));
+    return d;
+}
+
+struct IbbSphereVel { double U[3], W[3]; };
+
+// One link: staged coordinates (a, b, c) of the fluid node, direction d.i.
+// Adds the exchanged momentum and its moment to acc[6].
+template <typename T, typename RT>
+__device__ __forceinline__ void ibb_link(const DeviceState& s, const DeviceParticles& P, int p, int parity,
+                                         const IbbBox& B, const IbbDir<T, RT>& d, int a, int b, int c,
+                                         const RT (&UW)[6], RT (&acc)[6]) {
+    const int base = a + B.SA * b + B.SAB * c;
+    const bool ok1 = B.flag[base - d.off] == 0;
+    const bool ok2 = ok1 && B.flag[base - 2 * d.off] == 0;
+    const uint32_t gx = (uint32_t)(B.wA[a] + B.wB[b] + B.wC[c]);
+    const uint32_t gs = (uint32_t)(B.wA[a + d.cy] + B.wB[b + d.cz] + B.wC[c + d.cx]);
+    uint32_t ga = 0, gb = 0;
+    if (ok1) ga = (uint32_t)(B.wA[a - d.cy] + B.wB[b - d.cz] + B.wC[c - d.cx]);
+    if (ok2) gb = (uint32_t)(B.wA[a - 2 * d.cy] + B.wB[b - 2 * d.cz] + B.wC[c - 2 * d.cx]);
+    RT q, d0, d1, d2;
+    if constexpr (sizeof(RT) == 8) {
+        double dd[3];
+        offset(P, s.g, p, B.xlo + c, B.wA[a], B.wZ[b], dd);
+        q = link_q<double>(dd, d.cx, d.cy, d.cz, __dsub_rn(norm2_rn(dd), __dmul_rn(P.R, P.R)));
+        d0 = dd[0]; d1 = dd[1]; d2 = dd[2];
+    } else {
+        d0 = B.tC[c]; d1 = B.tA[a]; d2 = B.tB[b];
+        const float qc = d0 * d0 + d1 * d1 + d2 * d2 - B.R2f;
+        const float qb = d0 * d.fcx + d1 * d.fcy + d2 * d.fcz;
+        const float disc = qb * qb - qc * d.qa;
+        const float sq = disc > 0.f ? disc * rsqrtf(disc) : 0.f;
+        q = (-qb - sq) * d.inv_qa;
+        q = q < 1e-6f ? 1e-6f : (q > 1.f ? 1.f : q);
+    }
+    const RT r0 = d0 + q * d.fcx, r1 = d1 + q * d.fcy, r2 = d2 + q * d.fcz;
+    const RT uw0 = UW[0] + (UW[4] * r2 - UW[5] * r1);
+    const RT uw1 = UW[1] + (UW[5] * r0 - UW[3] * r2);
+    const RT uw2 = UW[2] + (UW[3] * r1 - UW[4] * r0);
+    const RT mw = d.mw6 * ((d.fcx * uw0 + d.fcy * uw1) + d.fcz * uw2);
+    const RT A = pop_r<T, RT>(s, parity ? d.Pib + gx : d.Pi + gs);
+    RT fn;
+    if (q < RT(0.5)) {
+        if (ok2) {
+            const RT Bv = pop_r<T, RT>(s, parity ? d.Pib + ga : d.Pi + gx);
+            const RT Cv = pop_r<T, RT>(s, parity ? d.Pib + gb : d.Pi + ga);
+            fn = q * (RT(1) + RT(2) * q) * A + (RT(1) - RT(4) * q * q) * Bv + q * (RT(2) * q - RT(1)) * Cv + mw;
+        } else if (ok1) {
+            const RT Bv = pop_r<T, RT>(s, parity ? d.Pib + ga : d.Pi + gx);
+            fn = RT(2) * q * A + (RT(1) - RT(2) * q) * Bv + mw;
+        } else {
+            fn = A + mw;
+        }
+    } else {
+        if (ok2) {
+            const RT D = pop_r<T, RT>(s, parity ? d.Pi + gx : d.Pib + ga);
+            const RT E = pop_r<T, RT>(s, parity ? d.Pi + ga : d.Pib + gb);
+            if constexpr (sizeof(RT) == 8) {
+                const RT k = RT(1) / (q * (RT(2) * q + RT(1)));
+                fn = k * A + (RT(2) * q - RT(1)) / q * D - (RT(2) * q - RT(1)) / (RT(2) * q + RT(1)) * E + k * mw;
+            } else {
+                const float t = 2.f * q + 1.f, k = __fdividef(1.f, q * t), m = 2.f * q - 1.f;
+                fn = k * (A + mw) + m * (t * k) * D - m * (q * k) * E;
+            }
+        } else if (ok1) {
+            const RT D = pop_r<T, RT>(s, parity ? d.Pi + gx : d.Pib + ga);
+            if constexpr (sizeof(RT) == 8) {
+                fn = (A + mw) / (RT(2) * q) + (RT(2) * q - RT(1)) / (RT(2) * q) * D;
+            } else {
+                const float h = __fdividef(1.f, 2.f * q);
+                fn = (A + mw) * h + (2.f * q - 1.f) * h * D;
+            }
+        } else {
+            fn = A + mw;
+        }
+    }
+    put_r<T, RT>(s, const_cast<T*>(parity ? d.Pi + gs : d.Pib + gx), fn);
+    // Galilean-invariant momentum exchange
+    const RT sA = A + fn, dA = fn - A;
+    const RT p0 = d.fcx * sA + uw0 * dA, p1 = d.fcy * sA + uw1 * dA, p2 = d.fcz * sA + uw2 * dA;
+    acc[0] += p0; acc[1] += p1; acc[2] += p2;
+    acc[3] += r1 * p2 - r2 * p1;
+    acc[4] += r2 * p0 - r0 * p2;
+    acc[5] += r0 * p1 - r1 * p0;
+}
+
+// a link that found its bucket full (rare: the buckets hold the links of a
+// whole sphere surface), processed by the thread that found it
+template <typename T, typename RT>
+__device__ __forceinline__ void ibb_link_cold(const DeviceState& s, const DeviceParticles& P, int p, int parity,
+                                           const IbbBox& B, int i, int a, int b, int c, const RT (&UW)[6],
+                                           RT (&acc)[6]) {
+    const IbbDir<T, RT> d = ibb_dir<T, RT>(s, B, i);
+    ibb_link<T, RT>(s, P, p, parity, B, d, a, b, c, UW, acc);
+}
+
+// shared-memory plan of k_ibb (bytes from the start of dynamic shared memory)
+struct IbbPlan { int bcap, nmax, SAmax, SBmax, flag_off, tab_off, bytes; };
+__host__ __device__ inline IbbPlan ibb_plan(double R) {
+    IbbPlan pl;
+    // links per direction: lattice lines crossing a sphere, <= pi R^2 sqrt(2)
+    // on average; a margin, rounded to whole warps
+    pl.bcap = ((int)(1.25 * 1.41421356 * 3.14159265 * R * R) + 64 + 31) & ~31;
+    pl.nmax = (int)floor(2.0 * (R + 1.5)) + 3;        // candidate nodes per axis
+    pl.SAmax = pl.nmax + 10;                            // + margin and 4-node alignment
+    pl.SBmax = pl.nmax + 4;
+    pl.flag_off = (Q - 1) * pl.bcap * 4;
+    pl.tab_off = pl.flag_off + ((pl.SAmax * pl.SBmax * pl.SBmax + 15) & ~15);
+    pl.bytes = pl.tab_off + (2 * pl.SAmax + 5 * pl.SBmax) * 4;
+    return pl;
+}
+
+template <typename T, typename RT>
+__global__ void __launch_bounds__(kPThreads, sizeof(RT) == 8 ? 2 : 4)
+    k_ibb(DeviceState s, DeviceParticles P, int parity, int vec4) {
     extern __shared__ __align__(16) unsigned char ibb_smem[];
-    uint32_t* bucket = reinterpret_cast<uint32_t*>(ibb_smem);     // [Q-1][kBucket] packed (a,b,c)
-    uint8_t* flag = ibb_smem + kBucketBytes;                        // staged owner bytes
     __shared__ int cnt[Q - 1];
+    __shared__ int cpre[Q];
     const Geometry& g = s.g;
     const int p = blockIdx.x;
     const double R = P.R;
-    const int* __restrict__ owner = P.owner;
+    IbbPlan pl = ibb_plan(R);
+    if (P.link_bucket > 0 && P.link_bucket < pl.bcap) pl.bcap = P.link_bucket;
+    uint32_t* bucket = reinterpret_cast<uint32_t*>(ibb_smem);       // [Q-1][bcap] packed (a,b,c)
+    uint8_t* flag = ibb_smem + pl.flag_off;
+    float* tA = reinterpret_cast<float*>(ibb_smem + pl.tab_off);
+    float* tB = tA + pl.SAmax;
+    float* tC = tB + pl.SBmax;
+    int* wA = reinterpret_cast<int*>(tC + pl.SBmax);
+    int* wB = wA + pl.SAmax;
+    int* wC = wB + pl.SBmax;
+    int* wZ = wC + pl.SBmax;
     const double ext = R + 1.5;
     const Range rx = box(P.pos[3 * p], ext, g.NZ, false);
     const Range ry = box(P.pos[3 * p + 1], ext, g.NX, true);
     const Range rz = box(P.pos[3 * p + 2], ext, g.NY, true);
-    const int SA = ry.n + 4, SB = rz.n + 4, SC = rx.n + 4, SAB = SA * SB;
+    // staged streamwise range starts on a multiple of 4 nodes (16-byte owner loads)
+    const int ga0 = (ry.lo - 2) & ~3;
+    const int SA = (ry.lo + ry.n + 2 - ga0 + 3) & ~3, SB = rz.n + 4, SC = rx.n + 4, SAB = SA * SB;
+    const int A0 = ry.lo - ga0;
+    const Centre cen = centre_of(P, p);
+    const int cix = (int)floor(cen.x), ciy = (int)floor(cen.y), ciz = (int)floor(cen.z);
     if (threadIdx.x < Q - 1) cnt[threadIdx.x] = 0;
-    {
-        BoxWalk w(threadIdx.x, blockDim.x, SA, SB, SC);
-        const int tot = SAB * SC;
-        for (int done = 0; done < tot; done += 4 * (int)blockDim.x) {
-            int o[4], li[4];
+    for (int t = threadIdx.x; t < SA; t += blockDim.x) {
+        tA[t] = (float)(ga0 + t - ciy) + (0.5f - (float)(cen.y - ciy));
+        wA[t] = wrapi(ga0 + t, g.NX);
+    }
+    for (int t = threadIdx.x; t < SB; t += blockDim.x) {
+        tB[t] = (float)(rz.lo - 2 + t - ciz) + (0.5f - (float)(cen.z - ciz));
+        wZ[t] = wrapi(rz.lo - 2 + t, g.NY);
+        wB[t] = wZ[t] * g.NX;
+    }
+    for (int t = threadIdx.x; t < SC; t += blockDim.x) {
+        tC[t] = (float)(rx.lo - 2 + t - cix) + (0.5f - (float)(cen.x - cix));
+        wC[t] = (rx.lo - 2 + t) * (g.NX * g.NY);
+    }
+    const int* __restrict__ owner = P.owner;
+    if (vec4) {
+        // four owner values per 16-byte load (NX is a multiple of 4)
+        const int qA = SA >> 2;
+        BoxWalk w(threadIdx.x, blockDim.x, qA, SB, SC);
+        const int tot = qA * SB * SC;
+        for (int done = 0; done < tot; done += 2 * (int)blockDim.x) {
+            int4 o[2];
+            int li[2];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < 2; ++u) {
                 li[u] = -1;
-                o[u] = -3;
+                o[u] = make_int4(-3, -3, -3, -3);
                 if (w.valid()) {
-                    li[u] = w.a + SA * w.b + SAB * w.c;
+                    li[u] = 4 * w.a + SA * w.b + SAB * w.c;
                     const int ix = rx.lo - 2 + w.c;
                     if (ix >= 0 && ix < g.NZ)
-                        o[u] = __ldg(owner + gnode(g, ix, wrapi(ry.lo - 2 + w.a, g.NX), wrapi(rz.lo - 2 + w.b, g.NY)));
+                        o[u] = __ldg(reinterpret_cast<const int4*>(
+                            owner + gnode(g, ix, wrapi(ga0 + 4 * w.a, g.NX), wrapi(rz.lo - 2 + w.b, g.NY))));
                     w.advance();
                 }
             }
 #pragma unroll
-            for (int u = 0; u < 4; ++u)
-                if (li[u] >= 0) flag[li[u]] = o[u] == -1 ? 0 : (o[u] == p ? 1 : 2);
+            for (int u = 0; u < 2; ++u) {
+                if (li[u] < 0) continue;
+                const int v[4] = {o[u].x, o[u].y, o[u].z, o[u].w};
+                uint32_t word = 0;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) word |= (uint32_t)(v[k] == -1 ? 0 : (v[k] == p ? 1 : 2)) << (8 * k);
+                *reinterpret_cast<uint32_t*>(flag + li[u]) = word;
+            }
+        }
+    } else {
+        BoxWalk w(threadIdx.x, blockDim.x, SA, SB, SC);
+        for (; w.valid(); w.advance()) {
+            const int ix = rx.lo - 2 + w.c;
+            int o = -3;
+            if (ix >= 0 && ix < g.NZ) o = __ldg(owner + gnode(g, ix, wrapi(ga0 + w.a, g.NX), wrapi(rz.lo - 2 + w.b, g.NY)));
+            flag[w.a + SA * w.b + SAB * w.c] = o == -1 ? 0 : (o == p ? 1 : 2);
         }
     }
-    // per-sphere constants of the link arithmetic
-    const Centre cen = centre_of(P, p);
+    IbbBox Bx;
+    Bx.SA = SA; Bx.SAB = SAB; Bx.A0 = A0; Bx.flag = flag;
+    Bx.tA = tA; Bx.tB = tB; Bx.tC = tC; Bx.wA = wA; Bx.wB = wB; Bx.wC = wC; Bx.wZ = wZ;
+    Bx.xlo = rx.lo - 2;
+    Bx.R2f = (float)(R * R);
+    RT UW[6];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { UW[k] = (RT)P.vel[3 * p + k]; UW[3 + k] = (RT)P.omg[3 * p + k]; }
     const float shell2 = (float)((R + 1.5) * (R + 1.5));
-    const int cix = (int)floor(cen.x), ciy = (int)floor(cen.y), ciz = (int)floor(cen.z);
-    const float hfx = 0.5f - (float)(cen.x - cix), hfy = 0.5f - (float)(cen.y - ciy), hfz = 0.5f - (float)(cen.z - ciz);
-    const float R2f = (float)(R * R);
-    const double R2 = __dmul_rn(R, R);
-    const RT U0 = (RT)P.vel[3 * p], U1 = (RT)P.vel[3 * p + 1], U2 = (RT)P.vel[3 * p + 2];
-    const RT Wx = (RT)P.omg[3 * p], Wy = (RT)P.omg[3 * p + 1], Wz = (RT)P.omg[3 * p + 2];
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const unsigned lt = (1u << lane) - 1u;
-    double acc[6] = {0, 0, 0, 0, 0, 0};
-    unsigned nl = 0;
+    RT acc[6] = {0, 0, 0, 0, 0, 0};
     __syncthreads();
-    const int total = rx.n * ry.n * rz.n;
-    const int rounds = (total + blockDim.x - 1) / blockDim.x;
-    BoxWalk w(threadIdx.x, blockDim.x, ry.n, rz.n, rx.n);
-    for (int round = 0; round < rounds; ++round) {
-        // phase 1: links of this thread's node, from the staged bytes
-        unsigned mask = 0;
-        uint32_t packed = 0;
-        if (w.valid()) {
-            const int base = (w.a + 2) + SA * (w.b + 2) + SAB * (w.c + 2);
-            packed = (uint32_t)w.a | ((uint32_t)w.b << 8) | ((uint32_t)w.c << 16);
-            if (flag[base] == 0 &&
-                dist2_fast(cen, g, rx.lo + w.c, wrapi(ry.lo + w.a, g.NX), wrapi(rz.lo + w.b, g.NY)) <= shell2) {
+    // phase 1: links of the candidate nodes, from the staged bytes
+    {
+        const int total = rx.n * ry.n * rz.n;
+        const int rounds = (total + blockDim.x - 1) / blockDim.x;
+        BoxWalk w(threadIdx.x, blockDim.x, ry.n, rz.n, rx.n);
+        for (int round = 0; round < rounds; ++round) {
+            unsigned mask = 0;
+            int a = 0, b = 0, c = 0;
+            if (w.valid()) {
+                a = w.a + A0; b = w.b + 2; c = w.c + 2;
+                const int base = a + SA * b + SAB * c;
+                if (flag[base] == 0 && tA[a] * tA[a] + tB[b] * tB[b] + tC[c] * tC[c] <= shell2) {
 #pragma unroll
-                for (int i = 1; i < Q; ++i)
-                    if (flag[base + CYf(i) + SA * CZf(i) + SAB * CXf(i)] == 1) mask |= 1u << i;
-            }
-            w.advance();
-        }
-        int over = 0;
-#pragma unroll
-        for (int i = 1; i < Q; ++i) {
-            const bool has = (mask >> i) & 1u;
-            const unsigned bal = __ballot_sync(0xffffffffu, has);
-            if (!bal) continue;
-            int b0 = 0;
-            if (lane == 0) {
-                b0 = atomicAdd(&cnt[i - 1], __popc(bal));
-                over |= b0 + __popc(bal) > kBucket - (int)blockDim.x;
-            }
-            b0 = __shfl_sync(0xffffffffu, b0, 0);
-            if (has) bucket[(i - 1) * kBucket + b0 + __popc(bal & lt)] = packed;
-        }
-        if (!__syncthreads_or(over) && round != rounds - 1) continue;
-        // phase 2: the buckets, one direction at a time
-        RT nacc[6] = {0, 0, 0, 0, 0, 0};
-#pragma unroll 1
-        for (int i = 1; i < Q; ++i) {
-            const int n = cnt[i - 1];
-            if (threadIdx.x == 0) nl += n;
-            const int cx = cx_rt(i), cy = cy_rt(i), cz = cz_rt(i), ib = opp_rt(i);
-            const int off = cy + SA * cz + SAB * cx;
-            const RT qa = (RT)(cx * cx + cy * cy + cz * cz);
-            const RT mw6 = RT(-6) * (RT)w_rt(i);
-            const T* __restrict__ Pi = plane<T>(s, i);
-            const T* __restrict__ Pib = plane<T>(s, ib);
-            for (int e = threadIdx.x; e < n; e += blockDim.x) {
-                const uint32_t v = bucket[(i - 1) * kBucket + e];
-                const int a = v & 255, b = (v >> 8) & 255, c = (v >> 16) & 255;
-                const int base = (a + 2) + SA * (b + 2) + SAB * (c + 2);
-                const bool ok1 = flag[base - off] == 0;
-                const bool ok2 = ok1 && flag[base - 2 * off] == 0;
-                const int ix = rx.lo + c, iy = wrapi(ry.lo + a, g.NX), iz = wrapi(rz.lo + b, g.NY);
-                RT q, d0, d1, d2;
-                if constexpr (sizeof(RT) == 8) {
-                    double d[3];
-                    offset(P, g, p, ix, iy, iz, d);
-                    q = link_q<double>(d, cx, cy, cz, __dsub_rn(norm2_rn(d), R2));
-                    d0 = d[0]; d1 = d[1]; d2 = d[2];
-                } else {
-                    // offsets from the integer part of the centre: exact
-                    // integers plus an FP32 fraction (no FP64 per link)
-                    int oy = iy - ciy, oz = iz - ciz;
-                    oy = oy >= g.NX / 2 ? oy - g.NX : (oy < -(g.NX / 2) ? oy + g.NX : oy);
-                    oz = oz >= g.NY / 2 ? oz - g.NY : (oz < -(g.NY / 2) ? oz + g.NY : oz);
-                    d0 = (float)(ix - cix) + hfx;
-                    d1 = (float)oy + hfy;
-                    d2 = (float)oz + hfz;
-                    const float qc = d0 * d0 + d1 * d1 + d2 * d2 - R2f;
-                    const float qb = d0 * cx + d1 * cy + d2 * cz;
-                    float disc = qb * qb - qa * qc;
-                    disc = disc < 0.f ? 0.f : disc;
-                    q = (-qb - sqrtf(disc)) / qa;
-                    q = q < 1e-6f ? 1e-6f : (q > 1.f ? 1.f : q);
+                    for (int i = 1; i < Q; ++i)
+                        if (flag[base + CYf(i) + SA * CZf(i) + SAB * CXf(i)] == 1) mask |= 1u << i;
                 }
-                const RT r0 = d0 + q * cx, r1 = d1 + q * cy, r2 = d2 + q * cz;
-                const RT uw0 = U0 + (Wy * r2 - Wz * r1);
-                const RT uw1 = U1 + (Wz * r0 - Wx * r2);
-                const RT uw2 = U2 + (Wx * r1 - Wy * r0);
-                const RT mw = mw6 * ((cx * uw0 + cy * uw1) + cz * uw2);
-                // the four nodes of the link
-                const uint32_t gx = gnode(g, ix, iy, iz);
-                const uint32_t gs = gnode(g, ix + cx, wrapi(iy + cy, g.NX), wrapi(iz + cz, g.NY));
-                uint32_t ga = 0, gb = 0;
-                if (ok1) ga = gnode(g, ix - cx, wrapi(iy - cy, g.NX), wrapi(iz - cz, g.NY));
-                if (ok2) gb = gnode(g, ix - 2 * cx, wrapi(iy - 2 * cy, g.NX), wrapi(iz - 2 * cz, g.NY));
-                const T* pA = parity ? Pib + gx : Pi + gs;
-                const RT A = pop_r<T, RT>(s, pA);
-                RT fn;
-                if (q < RT(0.5)) {
-                    if (ok2) {
-                        const RT B = pop_r<T, RT>(s, parity ? Pib + ga : Pi + gx);
-                        const RT C = pop_r<T, RT>(s, parity ? Pib + gb : Pi + ga);
-                        fn = q * (RT(1) + RT(2) * q) * A + (RT(1) - RT(4) * q * q) * B + q * (RT(2) * q - RT(1)) * C + mw;
-                    } else if (ok1) {
-                        const RT B = pop_r<T, RT>(s, parity ? Pib + ga : Pi + gx);
-                        fn = RT(2) * q * A + (RT(1) - RT(2) * q) * B + mw;
-                    } else {
-                        fn = A + mw;
-                    }
-                } else {
-                    if (ok2) {
-                        const RT D = pop_r<T, RT>(s, parity ? Pi + gx : Pib + ga);
-                        const RT E = pop_r<T, RT>(s, parity ? Pi + ga : Pib + gb);
-                        const RT k = RT(1) / (q * (RT(2) * q + RT(1)));
-                        fn = k * A + (RT(2) * q - RT(1)) / q * D - (RT(2) * q - RT(1)) / (RT(2) * q + RT(1)) * E + k * mw;
-                    } else if (ok1) {
-                        const RT D = pop_r<T, RT>(s, parity ? Pi + gx : Pib + ga);
-                        fn = (A + mw) / (RT(2) * q) + (RT(2) * q - RT(1)) / (RT(2) * q) * D;
-                    } else {
-                        fn = A + mw;
-                    }
+                w.advance();
+            }
+            const uint32_t packed = (uint32_t)a | ((uint32_t)b << 8) | ((uint32_t)c << 16);
+            if (!__any_sync(0xffffffffu, mask)) continue;
+#pragma unroll
+            for (int i = 1; i < Q; ++i) {
+                const bool has = (mask >> i) & 1u;
+                const unsigned bal = __ballot_sync(0xffffffffu, has);
+                if (!bal) continue;
+                int b0 = 0;
+                if (lane == 0) b0 = atomicAdd(&cnt[i - 1], __popc(bal));
+                b0 = __shfl_sync(0xffffffffu, b0, 0);
+                if (has) {
+                    const int pos = b0 + __popc(bal & lt);
+                    if (pos < pl.bcap) bucket[(i - 1) * pl.bcap + pos] = packed;
+                    else ibb_link_cold<T, RT>(s, P, p, parity, Bx, i, a, b, c, UW, acc);
                 }
-                put_r<T, RT>(s, const_cast<T*>(parity ? Pi + gs : Pib + gx), fn);
-                // Galilean-invariant momentum exchange
-                const RT sA = A + fn, dA = fn - A;
-                const RT p0 = cx * sA + uw0 * dA, p1 = cy * sA + uw1 * dA, p2 = cz * sA + uw2 * dA;
-                nacc[0] += p0; nacc[1] += p1; nacc[2] += p2;
-                nacc[3] += r1 * p2 - r2 * p1;
-                nacc[4] += r2 * p0 - r0 * p2;
-                nacc[5] += r0 * p1 - r1 * p0;
             }
         }
+    }
+    __syncthreads();
+    // chunks of 32 links per direction, prefix over the directions
+    if (wid == 0) {
+        const int n = lane < Q - 1 ? min(cnt[lane], pl.bcap) : 0;
+        int v = (n + 31) >> 5;
 #pragma unroll
-        for (int k = 0; k < 6; ++k) acc[k] += (double)nacc[k];
-        __syncthreads();
-        if (threadIdx.x < Q - 1) cnt[threadIdx.x] = 0;
-        __syncthreads();
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += u;
+        }
+        if (lane < Q - 1) cpre[lane + 1] = v;
+        if (lane == 0) cpre[0] = 0;
+    }
+    __syncthreads();
+    // phase 2: chunks dealt to the warps
+    {
+        const int nch = cpre[Q - 1];
+        int k = 0;
+        for (int ch = wid; ch < nch; ch += nw) {
+            while (ch >= cpre[k + 1]) ++k;
+            const int e = ((ch - cpre[k]) << 5) + lane;
+            if (e >= min(cnt[k], pl.bcap)) continue;
+            const IbbDir<T, RT> d = ibb_dir<T, RT>(s, Bx, k + 1);
+            const uint32_t v = bucket[k * pl.bcap + e];
+            ibb_link<T, RT>(s, P, p, parity, Bx, d, v & 255, (v >> 8) & 255, (v >> 16) & 255, UW, acc);
+        }
     }
     // per-sphere FP64 reduction: warp shuffles, then across warps
     __shared__ double sh[6][kPThreads / 32];
-    const int wid = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
-        double v = acc[k];
+        double v = (double)acc[k];
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
         if (lane == 0) sh[k][wid] = v;
     }
     __syncthreads();
     if (threadIdx.x < 6) {
         double v = 0.0;
-        for (int ww = 0; ww < kPThreads / 32; ++ww) v += sh[threadIdx.x][ww];
+        for (int ww = 0; ww < nw; ++ww) v += sh[threadIdx.x][ww];
         if (threadIdx.x < 3) P.force[3 * p + threadIdx.x] = v;
         else P.torque[3 * p + threadIdx.x - 3] = v;
     }
-    if (threadIdx.x == 0) atomicAdd(&P.counters[1], nl);
+    if (threadIdx.x == 0) {
+        unsigned nl = 0;
+        for (int i = 0; i < Q - 1; ++i) nl += (unsigned)cnt[i];
+        atomicAdd(&P.counters[1], nl);
+    }
 }
 
-// dynamic shared memory of k_ibb for spheres of radius R: the buckets and the
-// staged owner bytes of the largest bounding box plus its stencil margin
-size_t ibb_smem_bytes(double R) {
-    const int n = (int)std::floor(2.0 * (R + 1.5)) + 2 + 4;
-    return (size_t)kBucketBytes + (((size_t)n * n * n + 15) & ~(size_t)15);
-}
+size_t ibb_smem_bytes(double R) { return (size_t)ibb_plan(R).bytes; }
 
 __device__ __forceinline__ double repulse(double h, double zeta, double k0, double k1) {
     if (h >= zeta) return 0.0;
@@ -726,18 +849,20 @@ cudaError_t particles_after_step(const DeviceState& s, const DeviceParticles& P,
     cudaError_t e = cudaMemsetAsync(P.counters, 0, 2 * sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
     const size_t smem = ibb_smem_bytes(P.R);
+    // 16-byte owner loads need rows that start on 4-node boundaries
+    const int vec4 = (s.g.NX % 4 == 0 && ((uintptr_t)P.owner & 15) == 0) ? 1 : 0;
     switch (s.prec) {
         case LBM_PREC_FP64:
             e = cudaFuncSetAttribute(k_ibb<double, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e == cudaSuccess) k_ibb<double, double><<<P.npart, kPThreads, smem, st>>>(s, P, parity);
+            if (e == cudaSuccess) k_ibb<double, double><<<P.npart, kPThreads, smem, st>>>(s, P, parity, vec4);
             break;
         case LBM_PREC_FP32:
             e = cudaFuncSetAttribute(k_ibb<float, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e == cudaSuccess) k_ibb<float, float><<<P.npart, kPThreads, smem, st>>>(s, P, parity);
+            if (e == cudaSuccess) k_ibb<float, float><<<P.npart, kPThreads, smem, st>>>(s, P, parity, vec4);
             break;
         default:
             e = cudaFuncSetAttribute(k_ibb<__half, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e == cudaSuccess) k_ibb<__half, float><<<P.npart, kPThreads, smem, st>>>(s, P, parity);
+            if (e == cudaSuccess) k_ibb<__half, float><<<P.npart, kPThreads, smem, st>>>(s, P, parity, vec4);
             break;
     }
     if (e != cudaSuccess) return e;

@@ -52,6 +52,26 @@ def test_particles_fp64_match_oracle(pkg, orc, nsteps):
         assert rel(st[k], getattr(sp, k)) < 1e-10, k
 
 
+def test_link_bucket_overflow_path_matches_oracle(pkg, orc):
+    """32-entry link buckets: most links of a sphere take the path for a full
+    bucket, with the same results."""
+    shape = (24, 32, 22)
+    run, f0 = channel_with_spheres(orc, pkg, shape, POS)
+    sp = orc.Spheres(POS, radius=4.0, rho_ratio=2.0, vel=VEL)
+    fo, owner, links, refills = orc.particle_run(orc.params_from(run), sp, f0, 3)
+    with pkg.Lattice(run) as lat:
+        lat.upload_f(f0)
+        lat.set_particles(POS, radius=4.0, rho_ratio=2.0, vel=VEL, flags=pkg.PFLAG_SMALL_LINK_BUCKETS)
+        lat.step(3)
+        g = lat.download_f()
+        st = lat.particles()
+        _, nlinks, _ = lat.particle_counts()
+    assert nlinks == links[-1] and nlinks > 3 * 18 * 32
+    assert rel(g, fo) < 1e-10
+    for k in ("pos", "vel", "omg", "force", "torque"):
+        assert rel(st[k], getattr(sp, k)) < 1e-10, k
+
+
 def test_particle_diagnostics_mask_solid_nodes(pkg, orc):
     shape = (24, 32, 22)
     run, f0 = channel_with_spheres(orc, pkg, shape, POS)
