@@ -791,8 +791,9 @@ int lbm_particles_set(lbm_ctx* c, const lbm_particle_params* pp, const double* p
         return fail(LBM_ERR_INVALID_ARG, "bad sphere parameters");
     // the bounce-back kernel stages a sphere's bounding box in shared memory,
     // and the periodic spans must hold a sphere with its stencil reach
-    if (lbm::particles_smem_bytes(pp->radius) > 227u * 1024u)
-        return fail(LBM_ERR_INVALID_ARG, "sphere radius too large (at most 24 lattice units)");
+    const size_t smem = lbm::particles_smem_bytes(pp->radius);
+    if (smem == 0 || smem > 227u * 1024u)
+        return fail(LBM_ERR_INVALID_ARG, "sphere radius too large (at most 27 lattice units)");
     if (pp->npart > 0 && ((double)c->p.ny < 2.0 * pp->radius + 8.0 || (double)c->p.nz < 2.0 * pp->radius + 8.0))
         return fail(LBM_ERR_INVALID_ARG, "periodic span smaller than 2*radius + 8");
     for (int32_t k = 0; k < pp->npart; ++k) {
@@ -833,7 +834,6 @@ int lbm_particles_set(lbm_ctx* c, const lbm_particle_params* pp, const double* p
     CK(cudaMemsetAsync(P.owner, 0xff, c->s.N * sizeof(int), c->stream));   // -1: fluid
     P.npart = n;
     P.R = pp->radius; P.rho_ratio = pp->rho_ratio;
-    P.link_bucket = (pp->flags & LBM_PFLAG_SMALL_LINK_BUCKETS) ? 32 : 0;
     P.stf0 = pp->stf0; P.stf1 = pp->stf1; P.stf0_w = pp->stf0_w; P.stf1_w = pp->stf1_w; P.zeta = pp->zeta;
     c->pp = *pp;
     c->have_prev = 0;

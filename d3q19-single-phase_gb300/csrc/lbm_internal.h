@@ -48,7 +48,6 @@ struct DeviceParticles {
     uint32_t* refill_node;
     int* refill_part;
     unsigned* counters;               // [0] refills, [1] links, [3] overflow flag
-    int link_bucket;                  // > 0: cap of the per-direction link buckets
 };
 
 // Everything a step needs; built once per context.

@@ -304,16 +304,15 @@ __device__ __forceinline__ RT link_q(const double d[3], int cx, int cy, int cz, 
 // Interpolated bounce-back.
 //
 // One CTA per sphere.  The owner values of the sphere's bounding box plus a
-// two-node stencil margin are staged once in shared memory as one byte per
-// node (0 fluid, 1 this sphere, 2 another sphere, a node being refilled or
-// beyond a wall), together with per-axis tables of the FP32 offset from the
-// sphere centre and of the node index.  Phase 1 walks the candidate nodes
-// (one per thread, streamwise fastest), finds their links from the staged
-// bytes and appends them, with warp-aggregated counts, to 18 per-direction
-// buckets.  Phase 2 cuts the buckets into chunks of 32 links of one direction
-// and deals the chunks to the warps, so that every lane of a warp works on the
-// same direction at neighbouring streamwise nodes.  A link that finds its
-// bucket full is processed at once by the thread that found it.
+// two-node stencil margin are staged once in shared memory as two bit masks
+// per streamwise row (bit a: node owned by this sphere; node fluid), together
+// with per-axis tables of the FP32 offset from the sphere centre and of the
+// node index.  The links of direction c_i in row (b, c) are then one word
+// operation: fluid(b, c) & owned(b + c_iz, c + c_ix) shifted by c_iy.  The
+// work is cut into units (direction, wall-normal plane) dealt to the warps;
+// lane j takes the row b = j of the plane, and the set bits of the lanes are
+// streamed through a 64-entry queue per warp, so that every lane of a warp
+// processes a link, mostly of one direction at neighbouring streamwise nodes.
 //
 // With the AA orientation the six accesses of a link touch the four nodes
 // x_f + c_i (solid), x_f, x_f - c_i, x_f - 2c_i in the planes i and opp(i):
@@ -326,11 +325,40 @@ __device__ __forceinline__ RT link_q(const double d[3], int cx, int cy, int cz, 
 // step at GB300's FP64 rate).  Force and torque are summed in FP64 per thread
 // and per sphere.
 
+// bit a of the result = bit a + cy of x
+template <typename W>
+__device__ __forceinline__ W shift_a(W x, int cy) {
+    return cy > 0 ? (x >> 1) : (cy < 0 ? (x << 1) : x);
+}
+__device__ __forceinline__ int lowest_bit(uint32_t m) { return __ffs((int)m) - 1; }
+__device__ __forceinline__ int lowest_bit(unsigned long long m) { return __ffsll((long long)m) - 1; }
+
+// per-direction constants, from selects (no conversions)
+template <typename RT>
+struct IbbDir {
+    int cx, cy, cz, ib;
+    RT fcx, fcy, fcz, mw6, qa, inv_qa;
+};
+template <typename RT>
+__device__ __forceinline__ IbbDir<RT> ibb_dir(int i) {
+    IbbDir<RT> d;
+    d.cx = cx_rt(i); d.cy = cy_rt(i); d.cz = cz_rt(i); d.ib = opp_rt(i);
+    d.fcx = d.cx > 0 ? RT(1) : (d.cx < 0 ? RT(-1) : RT(0));
+    d.fcy = d.cy > 0 ? RT(1) : (d.cy < 0 ? RT(-1) : RT(0));
+    d.fcz = d.cz > 0 ? RT(1) : (d.cz < 0 ? RT(-1) : RT(0));
+    const bool axis = i <= 6;
+    d.mw6 = axis ? RT(-6.0 * W1) : RT(-6.0 * W2);
+    d.qa = axis ? RT(1) : RT(2);
+    d.inv_qa = axis ? RT(1) : RT(0.5);
+    return d;
+}
+
 // staged box of one sphere, in shared memory
+template <typename W>
 struct IbbBox {
-    int SA, SAB;                  // strides of the staged byte box
-    int A0;                       // staged streamwise index of candidate a = 0
-    const uint8_t* flag;          // [SC][SB][SA]
+    int SB;                       // row stride: row (b, c) at b + SB * c
+    const W* own;                 // bit a: owned by this sphere
+    const W* fluid;               // bit a: fluid
     const float *tA, *tB, *tC;    // FP32 offset from the centre per staged index
     const int *wA, *wB, *wC;      // node-index terms per staged index
     const int* wZ;                // wrapped spanwise index per staged b (FP64 path)
@@ -338,45 +366,22 @@ struct IbbBox {
     float R2f;                    // R^2 in FP32
 };
 
-// per-direction constants (warp-uniform in phase 2)
-template <typename T, typename RT>
-struct IbbDir {
-    int i, cx, cy, cz, off;
-    RT fcx, fcy, fcz, mw6, qa, inv_qa;
-    const T* Pi;
-    const T* Pib;
-};
-template <typename T, typename RT>
-__device__ __forceinline__ IbbDir<T, RT> ibb_dir(const DeviceState& s, const IbbBox& B, int i) {
-    IbbDir<T, RT> d;
-    d.i = i;
-    d.cx = cx_rt(i); d.cy = cy_rt(i); d.cz = cz_rt(i);
-    d.off = d.cy + B.SA * d.cz + B.SAB * d.cx;
-    d.fcx = (RT)d.cx; d.fcy = (RT)d.cy; d.fcz = (RT)d.cz;
-    d.mw6 = (RT)(-6.0 * w_rt(i));
-    d.qa = (RT)(d.cx * d.cx + d.cy * d.cy + d.cz * d.cz);
-    d.inv_qa = d.qa == RT(1) ? RT(1) : RT(0.5);
-    d.Pi = plane<T>(s, i);
-    d.Pib = plane<T>(s, opp_rt(i));
-    return d;
-}
-
-struct IbbSphereVel { double U[3], W[3]; };
-
-// One link: staged coordinates (a, b, c) of the fluid node, direction d.i.
+// One link: staged coordinates (a, b, c) of the fluid node, direction i.
 // Adds the exchanged momentum and its moment to acc[6].
-template <typename T, typename RT>
+template <typename T, typename RT, typename W>
 __device__ __forceinline__ void ibb_link(const DeviceState& s, const DeviceParticles& P, int p, int parity,
-                                         const IbbBox& B, const IbbDir<T, RT>& d, int a, int b, int c,
-                                         const RT (&UW)[6], RT (&acc)[6]) {
-    const int base = a + B.SA * b + B.SAB * c;
-    const bool ok1 = B.flag[base - d.off] == 0;
-    const bool ok2 = ok1 && B.flag[base - 2 * d.off] == 0;
+                                         const IbbBox<W>& B, int i, int a, int b, int c, const RT (&UW)[6],
+                                         RT (&acc)[6]) {
+    const IbbDir<RT> d = ibb_dir<RT>(i);
+    const bool ok1 = (B.fluid[(b - d.cz) + B.SB * (c - d.cx)] >> (a - d.cy)) & 1;
+    const bool ok2 = ok1 && ((B.fluid[(b - 2 * d.cz) + B.SB * (c - 2 * d.cx)] >> (a - 2 * d.cy)) & 1);
     const uint32_t gx = (uint32_t)(B.wA[a] + B.wB[b] + B.wC[c]);
     const uint32_t gs = (uint32_t)(B.wA[a + d.cy] + B.wB[b + d.cz] + B.wC[c + d.cx]);
     uint32_t ga = 0, gb = 0;
     if (ok1) ga = (uint32_t)(B.wA[a - d.cy] + B.wB[b - d.cz] + B.wC[c - d.cx]);
     if (ok2) gb = (uint32_t)(B.wA[a - 2 * d.cy] + B.wB[b - 2 * d.cz] + B.wC[c - 2 * d.cx]);
+    const T* Pi = plane<T>(s, i);
+    const T* Pib = plane<T>(s, d.ib);
     RT q, d0, d1, d2;
     if constexpr (sizeof(RT) == 8) {
         double dd[3];
@@ -397,23 +402,23 @@ __device__ __forceinline__ void ibb_link(const DeviceState& s, const DeviceParti
     const RT uw1 = UW[1] + (UW[5] * r0 - UW[3] * r2);
     const RT uw2 = UW[2] + (UW[3] * r1 - UW[4] * r0);
     const RT mw = d.mw6 * ((d.fcx * uw0 + d.fcy * uw1) + d.fcz * uw2);
-    const RT A = pop_r<T, RT>(s, parity ? d.Pib + gx : d.Pi + gs);
+    const RT A = pop_r<T, RT>(s, parity ? Pib + gx : Pi + gs);
     RT fn;
     if (q < RT(0.5)) {
         if (ok2) {
-            const RT Bv = pop_r<T, RT>(s, parity ? d.Pib + ga : d.Pi + gx);
-            const RT Cv = pop_r<T, RT>(s, parity ? d.Pib + gb : d.Pi + ga);
+            const RT Bv = pop_r<T, RT>(s, parity ? Pib + ga : Pi + gx);
+            const RT Cv = pop_r<T, RT>(s, parity ? Pib + gb : Pi + ga);
             fn = q * (RT(1) + RT(2) * q) * A + (RT(1) - RT(4) * q * q) * Bv + q * (RT(2) * q - RT(1)) * Cv + mw;
         } else if (ok1) {
-            const RT Bv = pop_r<T, RT>(s, parity ? d.Pib + ga : d.Pi + gx);
+            const RT Bv = pop_r<T, RT>(s, parity ? Pib + ga : Pi + gx);
             fn = RT(2) * q * A + (RT(1) - RT(2) * q) * Bv + mw;
         } else {
             fn = A + mw;
         }
     } else {
         if (ok2) {
-            const RT D = pop_r<T, RT>(s, parity ? d.Pi + gx : d.Pib + ga);
-            const RT E = pop_r<T, RT>(s, parity ? d.Pi + ga : d.Pib + gb);
+            const RT D = pop_r<T, RT>(s, parity ? Pi + gx : Pib + ga);
+            const RT E = pop_r<T, RT>(s, parity ? Pi + ga : Pib + gb);
             if constexpr (sizeof(RT) == 8) {
                 const RT k = RT(1) / (q * (RT(2) * q + RT(1)));
                 fn = k * A + (RT(2) * q - RT(1)) / q * D - (RT(2) * q - RT(1)) / (RT(2) * q + RT(1)) * E + k * mw;
@@ -422,7 +427,7 @@ __device__ __forceinline__ void ibb_link(const DeviceState& s, const DeviceParti
                 fn = k * (A + mw) + m * (t * k) * D - m * (q * k) * E;
             }
         } else if (ok1) {
-            const RT D = pop_r<T, RT>(s, parity ? d.Pi + gx : d.Pib + ga);
+            const RT D = pop_r<T, RT>(s, parity ? Pi + gx : Pib + ga);
             if constexpr (sizeof(RT) == 8) {
                 fn = (A + mw) / (RT(2) * q) + (RT(2) * q - RT(1)) / (RT(2) * q) * D;
             } else {
@@ -433,7 +438,7 @@ __device__ __forceinline__ void ibb_link(const DeviceState& s, const DeviceParti
             fn = A + mw;
         }
     }
-    put_r<T, RT>(s, const_cast<T*>(parity ? d.Pi + gs : d.Pib + gx), fn);
+    put_r<T, RT>(s, const_cast<T*>(parity ? Pi + gs : Pib + gx), fn);
     // Galilean-invariant momentum exchange
     const RT sA = A + fn, dA = fn - A;
     const RT p0 = d.fcx * sA + uw0 * dA, p1 = d.fcy * sA + uw1 * dA, p2 = d.fcz * sA + uw2 * dA;
@@ -443,201 +448,162 @@ __device__ __forceinline__ void ibb_link(const DeviceState& s, const DeviceParti
     acc[5] += r0 * p1 - r1 * p0;
 }
 
-// a link that found its bucket full (rare: the buckets hold the links of a
-// whole sphere surface), processed by the thread that found it
-template <typename T, typename RT>
-__device__ __forceinline__ void ibb_link_cold(const DeviceState& s, const DeviceParticles& P, int p, int parity,
-                                           const IbbBox& B, int i, int a, int b, int c, const RT (&UW)[6],
-                                           RT (&acc)[6]) {
-    const IbbDir<T, RT> d = ibb_dir<T, RT>(s, B, i);
-    ibb_link<T, RT>(s, P, p, parity, B, d, a, b, c, UW, acc);
-}
+constexpr int kIbbQueue = 64;         // link queue entries per warp
 
-// shared-memory plan of k_ibb (bytes from the start of dynamic shared memory)
-struct IbbPlan { int bcap, nmax, SAmax, SBmax, flag_off, tab_off, bytes; };
-__host__ __device__ inline IbbPlan ibb_plan(double R) {
+// shared-memory plan of k_ibb for spheres of radius R with row words of
+// wbits bits; bytes == 0 when the staged rows do not fit one word
+struct IbbPlan { int S, rows_off, tab_off, queue_off, bytes; };
+__host__ __device__ inline IbbPlan ibb_plan(double R, int wbits) {
     IbbPlan pl;
-    // links per direction: lattice lines crossing a sphere, <= pi R^2 sqrt(2)
-    // on average; a margin, rounded to whole warps
-    pl.bcap = ((int)(1.25 * 1.41421356 * 3.14159265 * R * R) + 64 + 31) & ~31;
-    pl.nmax = (int)floor(2.0 * (R + 1.5)) + 3;        // candidate nodes per axis
-    pl.SAmax = pl.nmax + 10;                            // + margin and 4-node alignment
-    pl.SBmax = pl.nmax + 4;
-    pl.flag_off = (Q - 1) * pl.bcap * 4;
-    pl.tab_off = pl.flag_off + ((pl.SAmax * pl.SBmax * pl.SBmax + 15) & ~15);
-    pl.bytes = pl.tab_off + (2 * pl.SAmax + 5 * pl.SBmax) * 4;
+    pl.S = (int)floor(2.0 * (R + 1.5)) + 3 + 4;         // staged nodes per axis, at most
+    const int wbytes = wbits / 8;
+    pl.rows_off = 0;
+    pl.tab_off = 2 * pl.S * pl.S * wbytes;
+    pl.queue_off = pl.tab_off + 7 * pl.S * 4;
+    pl.bytes = pl.S <= wbits ? pl.queue_off + (kPThreads / 32) * kIbbQueue * 4 : 0;
     return pl;
 }
 
-template <typename T, typename RT>
+template <typename T, typename RT, typename W>
 __global__ void __launch_bounds__(kPThreads, sizeof(RT) == 8 ? 2 : 4)
-    k_ibb(DeviceState s, DeviceParticles P, int parity, int vec4) {
+    k_ibb(DeviceState s, DeviceParticles P, int parity) {
     extern __shared__ __align__(16) unsigned char ibb_smem[];
-    __shared__ int cnt[Q - 1];
-    __shared__ int cpre[Q];
     const Geometry& g = s.g;
     const int p = blockIdx.x;
     const double R = P.R;
-    IbbPlan pl = ibb_plan(R);
-    if (P.link_bucket > 0 && P.link_bucket < pl.bcap) pl.bcap = P.link_bucket;
-    uint32_t* bucket = reinterpret_cast<uint32_t*>(ibb_smem);       // [Q-1][bcap] packed (a,b,c)
-    uint8_t* flag = ibb_smem + pl.flag_off;
-    float* tA = reinterpret_cast<float*>(ibb_smem + pl.tab_off);
-    float* tB = tA + pl.SAmax;
-    float* tC = tB + pl.SBmax;
-    int* wA = reinterpret_cast<int*>(tC + pl.SBmax);
-    int* wB = wA + pl.SAmax;
-    int* wC = wB + pl.SBmax;
-    int* wZ = wC + pl.SBmax;
+    const IbbPlan pl = ibb_plan(R, 8 * (int)sizeof(W));
     const double ext = R + 1.5;
     const Range rx = box(P.pos[3 * p], ext, g.NZ, false);
     const Range ry = box(P.pos[3 * p + 1], ext, g.NX, true);
     const Range rz = box(P.pos[3 * p + 2], ext, g.NY, true);
-    // staged streamwise range starts on a multiple of 4 nodes (16-byte owner loads)
-    const int ga0 = (ry.lo - 2) & ~3;
-    const int SA = (ry.lo + ry.n + 2 - ga0 + 3) & ~3, SB = rz.n + 4, SC = rx.n + 4, SAB = SA * SB;
-    const int A0 = ry.lo - ga0;
+    const int SA = ry.n + 4, SB = rz.n + 4, SC = rx.n + 4;
+    const int ya = ry.lo - 2, zb = rz.lo - 2, xc = rx.lo - 2;   // node of staged index 0
+    W* own = reinterpret_cast<W*>(ibb_smem + pl.rows_off);
+    W* fluid = own + pl.S * pl.S;
+    float* tA = reinterpret_cast<float*>(ibb_smem + pl.tab_off);
+    float* tB = tA + pl.S;
+    float* tC = tB + pl.S;
+    int* wA = reinterpret_cast<int*>(tC + pl.S);
+    int* wB = wA + pl.S;
+    int* wC = wB + pl.S;
+    int* wZ = wC + pl.S;
+    uint32_t* queue = reinterpret_cast<uint32_t*>(ibb_smem + pl.queue_off);
     const Centre cen = centre_of(P, p);
     const int cix = (int)floor(cen.x), ciy = (int)floor(cen.y), ciz = (int)floor(cen.z);
-    if (threadIdx.x < Q - 1) cnt[threadIdx.x] = 0;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int t = threadIdx.x; t < SA; t += blockDim.x) {
-        tA[t] = (float)(ga0 + t - ciy) + (0.5f - (float)(cen.y - ciy));
-        wA[t] = wrapi(ga0 + t, g.NX);
+        tA[t] = (float)(ya + t - ciy) + (0.5f - (float)(cen.y - ciy));
+        wA[t] = wrapi(ya + t, g.NX);
     }
     for (int t = threadIdx.x; t < SB; t += blockDim.x) {
-        tB[t] = (float)(rz.lo - 2 + t - ciz) + (0.5f - (float)(cen.z - ciz));
-        wZ[t] = wrapi(rz.lo - 2 + t, g.NY);
+        tB[t] = (float)(zb + t - ciz) + (0.5f - (float)(cen.z - ciz));
+        wZ[t] = wrapi(zb + t, g.NY);
         wB[t] = wZ[t] * g.NX;
     }
     for (int t = threadIdx.x; t < SC; t += blockDim.x) {
-        tC[t] = (float)(rx.lo - 2 + t - cix) + (0.5f - (float)(cen.x - cix));
-        wC[t] = (rx.lo - 2 + t) * (g.NX * g.NY);
+        tC[t] = (float)(xc + t - cix) + (0.5f - (float)(cen.x - cix));
+        wC[t] = (xc + t) * (g.NX * g.NY);
     }
-    const int* __restrict__ owner = P.owner;
-    if (vec4) {
-        // four owner values per 16-byte load (NX is a multiple of 4)
-        const int qA = SA >> 2;
-        BoxWalk w(threadIdx.x, blockDim.x, qA, SB, SC);
-        const int tot = qA * SB * SC;
-        for (int done = 0; done < tot; done += 2 * (int)blockDim.x) {
-            int4 o[2];
-            int li[2];
+    // staging: one warp per row, lane j holds nodes a = j (and j + 32)
+    {
+        const int* __restrict__ owner = P.owner;
+        const int nrows = SB * SC;
+        const int a0 = wrapi(ya + lane, g.NX);
+        const int a1 = sizeof(W) == 8 ? wrapi(ya + lane + 32, g.NX) : 0;
+        constexpr int U = 4;
+        for (int r0 = wid; r0 < nrows; r0 += U * nw) {
+            int o[U][2];
 #pragma unroll
-            for (int u = 0; u < 2; ++u) {
-                li[u] = -1;
-                o[u] = make_int4(-3, -3, -3, -3);
-                if (w.valid()) {
-                    li[u] = 4 * w.a + SA * w.b + SAB * w.c;
-                    const int ix = rx.lo - 2 + w.c;
-                    if (ix >= 0 && ix < g.NZ)
-                        o[u] = __ldg(reinterpret_cast<const int4*>(
-                            owner + gnode(g, ix, wrapi(ga0 + 4 * w.a, g.NX), wrapi(rz.lo - 2 + w.b, g.NY))));
-                    w.advance();
+            for (int u = 0; u < U; ++u) {
+                const int r = r0 + u * nw;
+                o[u][0] = o[u][1] = -3;
+                if (r < nrows) {
+                    const int b = r % SB, c = r / SB;
+                    const int ix = xc + c;
+                    if (ix >= 0 && ix < g.NZ) {
+                        const uint32_t rowbase = (uint32_t)g.NX * ((uint32_t)wrapi(zb + b, g.NY) + (uint32_t)g.NY * (uint32_t)ix);
+                        if (lane < SA) o[u][0] = __ldg(owner + rowbase + a0);
+                        if (sizeof(W) == 8 && lane + 32 < SA) o[u][1] = __ldg(owner + rowbase + a1);
+                    }
                 }
             }
 #pragma unroll
-            for (int u = 0; u < 2; ++u) {
-                if (li[u] < 0) continue;
-                const int v[4] = {o[u].x, o[u].y, o[u].z, o[u].w};
-                uint32_t word = 0;
-#pragma unroll
-                for (int k = 0; k < 4; ++k) word |= (uint32_t)(v[k] == -1 ? 0 : (v[k] == p ? 1 : 2)) << (8 * k);
-                *reinterpret_cast<uint32_t*>(flag + li[u]) = word;
+            for (int u = 0; u < U; ++u) {
+                const int r = r0 + u * nw;
+                const unsigned po = __ballot_sync(0xffffffffu, o[u][0] == p);
+                const unsigned fo = __ballot_sync(0xffffffffu, o[u][0] == -1);
+                W pw = (W)po, fw = (W)fo;
+                if constexpr (sizeof(W) == 8) {
+                    pw |= (W)__ballot_sync(0xffffffffu, o[u][1] == p) << 32;
+                    fw |= (W)__ballot_sync(0xffffffffu, o[u][1] == -1) << 32;
+                }
+                if (lane == 0 && r < nrows) {
+                    const int b = r % SB, c = r / SB;
+                    own[b + pl.S * c] = pw;
+                    fluid[b + pl.S * c] = fw;
+                }
             }
         }
-    } else {
-        BoxWalk w(threadIdx.x, blockDim.x, SA, SB, SC);
-        for (; w.valid(); w.advance()) {
-            const int ix = rx.lo - 2 + w.c;
-            int o = -3;
-            if (ix >= 0 && ix < g.NZ) o = __ldg(owner + gnode(g, ix, wrapi(ga0 + w.a, g.NX), wrapi(rz.lo - 2 + w.b, g.NY)));
-            flag[w.a + SA * w.b + SAB * w.c] = o == -1 ? 0 : (o == p ? 1 : 2);
-        }
     }
-    IbbBox Bx;
-    Bx.SA = SA; Bx.SAB = SAB; Bx.A0 = A0; Bx.flag = flag;
+    IbbBox<W> Bx;
+    Bx.SB = pl.S; Bx.own = own; Bx.fluid = fluid;
     Bx.tA = tA; Bx.tB = tB; Bx.tC = tC; Bx.wA = wA; Bx.wB = wB; Bx.wC = wC; Bx.wZ = wZ;
-    Bx.xlo = rx.lo - 2;
+    Bx.xlo = xc;
     Bx.R2f = (float)(R * R);
     RT UW[6];
 #pragma unroll
     for (int k = 0; k < 3; ++k) { UW[k] = (RT)P.vel[3 * p + k]; UW[3 + k] = (RT)P.omg[3 * p + k]; }
-    const float shell2 = (float)((R + 1.5) * (R + 1.5));
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const unsigned lt = (1u << lane) - 1u;
     RT acc[6] = {0, 0, 0, 0, 0, 0};
+    const unsigned lt = (1u << lane) - 1u;
+    uint32_t* q = queue + wid * kIbbQueue;
+    int head = 0, tail = 0;
     __syncthreads();
-    // phase 1: links of the candidate nodes, from the staged bytes
+    // units (direction i, plane c), lane j on row b = j + 2 of the plane
     {
-        const int total = rx.n * ry.n * rz.n;
-        const int rounds = (total + blockDim.x - 1) / blockDim.x;
-        BoxWalk w(threadIdx.x, blockDim.x, ry.n, rz.n, rx.n);
-        for (int round = 0; round < rounds; ++round) {
-            unsigned mask = 0;
-            int a = 0, b = 0, c = 0;
-            if (w.valid()) {
-                a = w.a + A0; b = w.b + 2; c = w.c + 2;
-                const int base = a + SA * b + SAB * c;
-                if (flag[base] == 0 && tA[a] * tA[a] + tB[b] * tB[b] + tC[c] * tC[c] <= shell2) {
-#pragma unroll
-                    for (int i = 1; i < Q; ++i)
-                        if (flag[base + CYf(i) + SA * CZf(i) + SAB * CXf(i)] == 1) mask |= 1u << i;
-                }
-                w.advance();
+        const W amask = (((W)1 << ry.n) - 1) << 2;      // candidate nodes a in [2, 2 + ry.n)
+        const int nunits = (Q - 1) * rx.n;
+        int i = 1 + wid / max(rx.n, 1), cc = wid % max(rx.n, 1);
+        for (int u = wid; u < nunits; u += nw) {
+            const int c = cc + 2, b = lane + 2;
+            W m = 0;
+            if (lane < rz.n) {
+                const int cx = cx_rt(i), cy = cy_rt(i), cz = cz_rt(i);
+                m = fluid[b + pl.S * c] & shift_a(own[(b + cz) + pl.S * (c + cx)], cy) & amask;
             }
-            const uint32_t packed = (uint32_t)a | ((uint32_t)b << 8) | ((uint32_t)c << 16);
-            if (!__any_sync(0xffffffffu, mask)) continue;
-#pragma unroll
-            for (int i = 1; i < Q; ++i) {
-                const bool has = (mask >> i) & 1u;
+            while (__any_sync(0xffffffffu, m != 0)) {
+                const bool has = m != 0;
+                int a = 0;
+                if (has) { a = lowest_bit(m); m &= m - 1; }
                 const unsigned bal = __ballot_sync(0xffffffffu, has);
-                if (!bal) continue;
-                int b0 = 0;
-                if (lane == 0) b0 = atomicAdd(&cnt[i - 1], __popc(bal));
-                b0 = __shfl_sync(0xffffffffu, b0, 0);
-                if (has) {
-                    const int pos = b0 + __popc(bal & lt);
-                    if (pos < pl.bcap) bucket[(i - 1) * pl.bcap + pos] = packed;
-                    else ibb_link_cold<T, RT>(s, P, p, parity, Bx, i, a, b, c, UW, acc);
+                if (has) q[(tail + __popc(bal & lt)) & (kIbbQueue - 1)] = (uint32_t)a | ((uint32_t)b << 8) | ((uint32_t)c << 16) | ((uint32_t)i << 24);
+                tail += __popc(bal);
+                if (tail - head >= 32) {
+                    __syncwarp();
+                    const uint32_t v = q[(head + lane) & (kIbbQueue - 1)];
+                    head += 32;
+                    __syncwarp();
+                    ibb_link<T, RT, W>(s, P, p, parity, Bx, v >> 24, v & 255, (v >> 8) & 255, (v >> 16) & 255, UW, acc);
                 }
             }
+            cc += nw;
+            while (cc >= rx.n) { cc -= rx.n; ++i; }
         }
-    }
-    __syncthreads();
-    // chunks of 32 links per direction, prefix over the directions
-    if (wid == 0) {
-        const int n = lane < Q - 1 ? min(cnt[lane], pl.bcap) : 0;
-        int v = (n + 31) >> 5;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int u = __shfl_up_sync(0xffffffffu, v, o);
-            if (lane >= o) v += u;
-        }
-        if (lane < Q - 1) cpre[lane + 1] = v;
-        if (lane == 0) cpre[0] = 0;
-    }
-    __syncthreads();
-    // phase 2: chunks dealt to the warps
-    {
-        const int nch = cpre[Q - 1];
-        int k = 0;
-        for (int ch = wid; ch < nch; ch += nw) {
-            while (ch >= cpre[k + 1]) ++k;
-            const int e = ((ch - cpre[k]) << 5) + lane;
-            if (e >= min(cnt[k], pl.bcap)) continue;
-            const IbbDir<T, RT> d = ibb_dir<T, RT>(s, Bx, k + 1);
-            const uint32_t v = bucket[k * pl.bcap + e];
-            ibb_link<T, RT>(s, P, p, parity, Bx, d, v & 255, (v >> 8) & 255, (v >> 16) & 255, UW, acc);
+        __syncwarp();
+        if (lane < tail - head) {
+            const uint32_t v = q[(head + lane) & (kIbbQueue - 1)];
+            ibb_link<T, RT, W>(s, P, p, parity, Bx, v >> 24, v & 255, (v >> 8) & 255, (v >> 16) & 255, UW, acc);
         }
     }
     // per-sphere FP64 reduction: warp shuffles, then across warps
     __shared__ double sh[6][kPThreads / 32];
+    __shared__ int shn[kPThreads / 32];
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
         double v = (double)acc[k];
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
         if (lane == 0) sh[k][wid] = v;
     }
+    if (lane == 0) shn[wid] = tail;
     __syncthreads();
     if (threadIdx.x < 6) {
         double v = 0.0;
@@ -647,12 +613,25 @@ __global__ void __launch_bounds__(kPThreads, sizeof(RT) == 8 ? 2 : 4)
     }
     if (threadIdx.x == 0) {
         unsigned nl = 0;
-        for (int i = 0; i < Q - 1; ++i) nl += (unsigned)cnt[i];
+        for (int ww = 0; ww < nw; ++ww) nl += (unsigned)shn[ww];
         atomicAdd(&P.counters[1], nl);
     }
 }
 
-size_t ibb_smem_bytes(double R) { return (size_t)ibb_plan(R).bytes; }
+template <typename T, typename RT, typename W>
+cudaError_t launch_ibb(const DeviceState& s, const DeviceParticles& P, int parity, size_t smem, cudaStream_t st) {
+    if (smem > 48 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(k_ibb<T, RT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    k_ibb<T, RT, W><<<P.npart, kPThreads, smem, st>>>(s, P, parity);
+    return cudaGetLastError();
+}
+
+size_t ibb_smem_bytes(double R) {
+    const IbbPlan p32 = ibb_plan(R, 32);
+    return (size_t)(p32.bytes ? p32.bytes : ibb_plan(R, 64).bytes);
+}
 
 __device__ __forceinline__ double repulse(double h, double zeta, double k0, double k1) {
     if (h >= zeta) return 0.0;
@@ -849,20 +828,19 @@ cudaError_t particles_after_step(const DeviceState& s, const DeviceParticles& P,
     cudaError_t e = cudaMemsetAsync(P.counters, 0, 2 * sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
     const size_t smem = ibb_smem_bytes(P.R);
-    // 16-byte owner loads need rows that start on 4-node boundaries
-    const int vec4 = (s.g.NX % 4 == 0 && ((uintptr_t)P.owner & 15) == 0) ? 1 : 0;
+    const bool w32 = ibb_plan(P.R, 32).bytes != 0;
     switch (s.prec) {
         case LBM_PREC_FP64:
-            e = cudaFuncSetAttribute(k_ibb<double, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e == cudaSuccess) k_ibb<double, double><<<P.npart, kPThreads, smem, st>>>(s, P, parity, vec4);
+            e = w32 ? launch_ibb<double, double, uint32_t>(s, P, parity, smem, st)
+                    : launch_ibb<double, double, unsigned long long>(s, P, parity, smem, st);
             break;
         case LBM_PREC_FP32:
-            e = cudaFuncSetAttribute(k_ibb<float, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e == cudaSuccess) k_ibb<float, float><<<P.npart, kPThreads, smem, st>>>(s, P, parity, vec4);
+            e = w32 ? launch_ibb<float, float, uint32_t>(s, P, parity, smem, st)
+                    : launch_ibb<float, float, unsigned long long>(s, P, parity, smem, st);
             break;
         default:
-            e = cudaFuncSetAttribute(k_ibb<__half, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e == cudaSuccess) k_ibb<__half, float><<<P.npart, kPThreads, smem, st>>>(s, P, parity, vec4);
+            e = w32 ? launch_ibb<__half, float, uint32_t>(s, P, parity, smem, st)
+                    : launch_ibb<__half, float, unsigned long long>(s, P, parity, smem, st);
             break;
     }
     if (e != cudaSuccess) return e;

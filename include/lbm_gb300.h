@@ -245,19 +245,13 @@ int lbm_load_flow(lbm_ctx* ctx, const char* path, int32_t kind,
  * (ix,iy,iz) (1-based) at (ix-1/2, iy-1/2, iz-1/2), as in macrovar. */
 typedef struct lbm_particle_params {
     int32_t npart;            /* number of spheres (npart, var_inc.f90:66)     */
-    int32_t flags;            /* LBM_PFLAG_* bits                              */
+    int32_t flags;            /* reserved, 0                                   */
     double  radius;           /* rad (var_inc.f90:67)                          */
     double  rho_ratio;        /* rhopart / rho0                                */
     double  stf0, stf1;       /* sphere-sphere repulsion (para.f90:357-358)    */
     double  stf0_w, stf1_w;   /* sphere-wall repulsion (para.f90:359-360)      */
     double  zeta;             /* repulsion range, lattice units                */
 } lbm_particle_params;
-
-/* lbm_particle_params.flags: cap the per-direction link buckets of the
- * bounce-back kernel at 32 entries, so that most links take the path for
- * links that find their bucket full (same results, slower; a check of that
- * path). */
-#define LBM_PFLAG_SMALL_LINK_BUCKETS 1
 
 /* Defaults of para.f90:339-379 for npart spheres of the given radius. */
 int lbm_particle_params_init(lbm_particle_params* pp, int32_t npart, double radius,

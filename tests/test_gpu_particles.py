@@ -52,21 +52,23 @@ def test_particles_fp64_match_oracle(pkg, orc, nsteps):
         assert rel(st[k], getattr(sp, k)) < 1e-10, k
 
 
-def test_link_bucket_overflow_path_matches_oracle(pkg, orc):
-    """32-entry link buckets: most links of a sphere take the path for a full
-    bucket, with the same results."""
-    shape = (24, 32, 22)
-    run, f0 = channel_with_spheres(orc, pkg, shape, POS)
-    sp = orc.Spheres(POS, radius=4.0, rho_ratio=2.0, vel=VEL)
+def test_large_sphere_64bit_rows_match_oracle(pkg, orc):
+    """Radius 12: the staged rows of the bounce-back kernel exceed 32 nodes and
+    take 64-bit words."""
+    shape = (32, 40, 40)
+    pos = np.array([[16.2, 19.7, 20.4]])
+    vel = np.array([[0.001, 0.004, -0.002]])
+    run, f0 = channel_with_spheres(orc, pkg, shape, pos)
+    sp = orc.Spheres(pos, radius=12.0, rho_ratio=2.0, vel=vel)
     fo, owner, links, refills = orc.particle_run(orc.params_from(run), sp, f0, 3)
     with pkg.Lattice(run) as lat:
         lat.upload_f(f0)
-        lat.set_particles(POS, radius=4.0, rho_ratio=2.0, vel=VEL, flags=pkg.PFLAG_SMALL_LINK_BUCKETS)
+        lat.set_particles(pos, radius=12.0, rho_ratio=2.0, vel=vel)
         lat.step(3)
         g = lat.download_f()
         st = lat.particles()
-        _, nlinks, _ = lat.particle_counts()
-    assert nlinks == links[-1] and nlinks > 3 * 18 * 32
+        _, nlinks, nref = lat.particle_counts()
+    assert nlinks == links[-1] and nref == refills[-1]
     assert rel(g, fo) < 1e-10
     for k in ("pos", "vel", "omg", "force", "torque"):
         assert rel(st[k], getattr(sp, k)) < 1e-10, k
