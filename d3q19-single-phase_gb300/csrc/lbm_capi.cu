@@ -144,6 +144,7 @@ int sync(lbm_ctx* c) {
         CK(cudaMemcpy(&flag, c->P.counters + 3, sizeof(unsigned), cudaMemcpyDeviceToHost));
         if (flag) {
             cudaMemset(c->P.counters + 3, 0, sizeof(unsigned));
+            if (flag & 2u) return fail(LBM_ERR_STATE, "non-finite or runaway sphere motion (velocity above 1 per step)");
             return fail(LBM_ERR_STATE, "refill list overflow: spheres moved too far in one step");
         }
     }
@@ -384,6 +385,8 @@ int lbm_destroy(lbm_ctx* c) {
     cudaFree(c->P.refill_node);
     cudaFree(c->P.refill_part);
     cudaFree(c->P.counters);
+    cudaFree(c->P.cell_count);
+    cudaFree(c->P.geom);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return LBM_OK;
@@ -807,6 +810,7 @@ int lbm_particles_set(lbm_ctx* c, const lbm_particle_params* pp, const double* p
     const int n = pp->npart;
     DeviceParticles& P = c->P;
     if (P.pos) { cudaFree(P.pos); P.pos = nullptr; }
+    if (P.geom) { cudaFree(P.geom); P.geom = nullptr; }
     if (!P.owner) CK(cudaMalloc(&P.owner, c->s.N * sizeof(int)));
     if (!P.counters) CK(cudaMalloc(&P.counters, 4 * sizeof(unsigned)));
     if (!c->d_count) CK(cudaMalloc(&c->d_count, sizeof(unsigned long long)));
@@ -821,19 +825,40 @@ int lbm_particles_set(lbm_ctx* c, const lbm_particle_params* pp, const double* p
         P.refill_cap = cap;
     }
     const size_t m = 3 * (size_t)std::max(n, 1);
-    CK(cudaMalloc(&P.pos, 8 * m * sizeof(double)));
+    CK(cudaMalloc(&P.pos, 9 * m * sizeof(double)));
     P.vel = P.pos + m; P.omg = P.vel + m; P.force = P.omg + m; P.torque = P.force + m;
-    P.fprev = P.torque + m; P.tprev = P.fprev + m; P.rep = P.tprev + m;
-    CK(cudaMemsetAsync(P.pos, 0, 8 * m * sizeof(double), c->stream));
+    P.fprev = P.torque + m; P.tprev = P.fprev + m; P.rep = P.tprev + m; P.pos_prev = P.rep + m;
+    CK(cudaMemsetAsync(P.pos, 0, 9 * m * sizeof(double), c->stream));
+    CK(cudaMalloc(&P.geom, (size_t)std::max(n, 1) * sizeof(SphereGeom)));
     if (n > 0) {
         CK(cudaMemcpyAsync(P.pos, pos, 3 * (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(P.pos_prev, pos, 3 * (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
         if (vel) CK(cudaMemcpyAsync(P.vel, vel, 3 * (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
         if (omg) CK(cudaMemcpyAsync(P.omg, omg, 3 * (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     }
     CK(cudaMemsetAsync(P.counters, 0, 4 * sizeof(unsigned), c->stream));
     CK(cudaMemsetAsync(P.owner, 0xff, c->s.N * sizeof(int), c->stream));   // -1: fluid
+    {
+        // repulsion cells at least one reach (2R + zeta) wide; three or more
+        // cells per periodic span, else the all-pairs search
+        const double reach = 2.0 * pp->radius + pp->zeta + 0.05;
+        const int ny = (int)std::floor((double)c->p.ny / reach), nz = (int)std::floor((double)c->p.nz / reach);
+        const int nx = std::max(1, (int)std::floor((double)c->p.nx / reach));
+        const long long ncell = (long long)nx * ny * nz;
+        cudaFree(P.cell_count);
+        P.cell_count = nullptr;
+        P.cell_list = nullptr;
+        P.ncell = 0;
+        if (n > 1 && ny >= 3 && nz >= 3 && ncell <= (1LL << 24)) {
+            CK(cudaMalloc(&P.cell_count, (size_t)ncell * (1 + kCellCap) * sizeof(int)));
+            P.cell_list = P.cell_count + ncell;
+            P.ncell = (int)ncell;
+            P.cell_nx = nx; P.cell_ny = ny; P.cell_nz = nz;
+        }
+    }
     P.npart = n;
     P.R = pp->radius; P.rho_ratio = pp->rho_ratio;
+    P.Rf = (float)pp->radius;
     P.stf0 = pp->stf0; P.stf1 = pp->stf1; P.stf0_w = pp->stf0_w; P.stf1_w = pp->stf1_w; P.zeta = pp->zeta;
     c->pp = *pp;
     c->have_prev = 0;

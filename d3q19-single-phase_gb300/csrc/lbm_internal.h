@@ -36,6 +36,16 @@ struct Geometry {
 };
 
 // Moving spheres on the device (all FP64 state, 3 values per sphere).
+// Per-sphere geometry in the forms the node kernels use, written once per
+// update of the positions (no FP64 in the kernels that read it).
+struct SphereGeom {
+    int ci[3];          // floor of the centre, reference axes
+    float h[3];         // 0.5 - (centre - ci): FP32 offset of node ci from the centre
+    float delta;        // displacement of the last update, rounded up
+    float U[3], W[3];   // velocity and angular velocity in FP32
+    float pad[3];
+};
+
 struct DeviceParticles {
     int npart;
     int refill_cap;
@@ -44,11 +54,19 @@ struct DeviceParticles {
     double *force, *torque;           // hydrodynamic part of the last step
     double *fprev, *tprev;            // total force/torque of the previous step
     double *rep;                      // repulsion of the current step
+    double *pos_prev;                 // centre before the last Newton-Euler update
+    SphereGeom* geom;                 // [npart]
+    float Rf;                         // radius in FP32
     int* owner;                       // per node: sphere id, -1 fluid, -2 pending refill
     uint32_t* refill_node;
     int* refill_part;
-    unsigned* counters;               // [0] refills, [1] links, [3] overflow flag
+    unsigned* counters;               // [0] refills, [1] links, [2] cell overflow, [3] refill overflow
+    // cell list of the repulsion (ncell == 0: all-pairs search)
+    int ncell, cell_nx, cell_ny, cell_nz;   // cells along reference x, y, z
+    int* cell_count;                        // [ncell]
+    int* cell_list;                         // [ncell][kCellCap] sphere ids
 };
+constexpr int kCellCap = 32;              // spheres per repulsion cell
 
 // Everything a step needs; built once per context.
 struct DeviceState {

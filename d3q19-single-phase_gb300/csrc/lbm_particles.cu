@@ -14,16 +14,20 @@
 //     step just taken; the momentum exchanged (Galilean-invariant form, Wen et
 //     al. 2014) is reduced per sphere with warp shuffles into FP64 force and
 //     torque;
-//  3. k_newton, one thread per sphere: soft-sphere repulsion and the FP64
-//     Newton-Euler update (second-order Adams-Bashforth);
-//  4. k_release / k_claim: node ownership follows the new positions; nodes
-//     that leave a sphere are queued;
+//  3. k_bin + k_repulsion_cells (a cell list; k_repulsion, all pairs, for
+//     small domains): soft-sphere repulsion summed in sphere-index order;
+//     k_newton, one thread per sphere: the FP64 Newton-Euler update
+//     (second-order Adams-Bashforth);
+//  4. k_shell<release>, then k_shell<claim>: node ownership follows the new
+//     positions along the thin shell swept by each surface; nodes that leave
+//     a sphere are queued;
 //  5. k_refill: queued nodes get the equilibrium at the wall velocity plus the
 //     non-equilibrium part of the fluid neighbour closest to the outward
 //     normal.
 // Geometry decisions (inside tests, q, the refill direction) use explicit
 // round-to-nearest FP64 operations so that they agree bit for bit with the
 // CPU oracle.
+#include <algorithm>
 #include <cmath>
 
 #include "lbm_internal.h"
@@ -157,6 +161,22 @@ __device__ __forceinline__ Range box(double c, double ext, int n, bool periodic)
     return r;
 }
 
+// Node range of a bounding box along one axis from the geometry record:
+// nodes whose centres lie within ext of the sphere centre, plus any node
+// within FP32 rounding of that (callers pass a margin in ext).
+__device__ __forceinline__ Range box_g(int ci, float h, float ext, int n, bool periodic) {
+    int a = ci + (int)floorf(-h - ext);
+    int b = ci + (int)ceilf(ext - h);
+    if (!periodic) {
+        if (a < 0) a = 0;
+        if (b > n - 1) b = n - 1;
+    }
+    Range r;
+    r.lo = a;
+    r.n = b >= a ? b - a + 1 : 0;
+    return r;
+}
+
 // GPU node index of reference indices (ix wall-normal, iy streamwise, iz spanwise)
 __device__ __forceinline__ uint32_t gnode(const Geometry& g, int ix, int iy, int iz) {
     return (uint32_t)iy + (uint32_t)g.NX * ((uint32_t)iz + (uint32_t)g.NY * (uint32_t)ix);
@@ -227,50 +247,99 @@ __device__ __forceinline__ void write_nat(const DeviceState& s, int parity, int 
 }
 
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kPThreads) k_claim(DeviceParticles P, Geometry g, int* owner) {
-    const int p = blockIdx.x;
-    const Range rx = box(P.pos[3 * p], P.R, g.NZ, false);
-    const Range ry = box(P.pos[3 * p + 1], P.R, g.NX, true);
-    const Range rz = box(P.pos[3 * p + 2], P.R, g.NY, true);
-    const Centre c = centre_of(P, p);
-    for (BoxWalk w(threadIdx.x, blockDim.x, ry.n, rz.n, rx.n); w.valid(); w.advance()) {
-        const int iy = wrapi(ry.lo + w.a, g.NX), iz = wrapi(rz.lo + w.b, g.NY), ix = rx.lo + w.c;
-        int in = inside_screen(dist2_fast(c, g, ix, iy, iz), P.R);
-        if (in < 0) {
-            double d[3];
-            offset(P, g, p, ix, iy, iz, d);
-            in = inside(d, P.R);
-        }
-        if (in) owner[gnode(g, ix, iy, iz)] = p;
-    }
-}
+// Ownership update along the thin shell swept by a sphere surface.  A node
+// owned by sphere p lies inside p's previous position, so within R + delta of
+// the new centre (delta: displacement of this step), and a node at less than
+// R - delta from the new centre was inside the previous sphere and is owned
+// already.  One warp per sphere; lane j takes (spanwise, wall-normal) rows of
+// the bounding box, intersects each row with that shell in FP32 (with a
+// margin far above the FP32 error) and decides the few nodes found by their
+// FP32 squared distance, or by the exact FP64 test of the oracle where that
+// lies within kInBand of R^2.  `full` claims every node inside (placement).
+constexpr int kShellWarps = 4;
+constexpr float kShellEps = 0.01f;
 
-__global__ void __launch_bounds__(kPThreads) k_release(DeviceParticles P, Geometry g, int* owner) {
-    const int p = blockIdx.x;
-    const Centre c = centre_of(P, p);
-    const double ext = P.R + 1.5;
-    const Range rx = box(P.pos[3 * p], ext, g.NZ, false);
-    const Range ry = box(P.pos[3 * p + 1], ext, g.NX, true);
-    const Range rz = box(P.pos[3 * p + 2], ext, g.NY, true);
-    for (BoxWalk w(threadIdx.x, blockDim.x, ry.n, rz.n, rx.n); w.valid(); w.advance()) {
-        const int iy = wrapi(ry.lo + w.a, g.NX), iz = wrapi(rz.lo + w.b, g.NY), ix = rx.lo + w.c;
-        const uint32_t n = gnode(g, ix, iy, iz);
-        if (owner[n] != p) continue;
-        int in = inside_screen(dist2_fast(c, g, ix, iy, iz), P.R);
-        if (in < 0) {
-            double d[3];
-            offset(P, g, p, ix, iy, iz, d);
-            in = inside(d, P.R);
+// FP32 squared distance error bound: node offsets are an exact integer plus
+// the FP32 fraction of the geometry record (error <= 2^-24 |d| + 2^-25 per
+// axis for |d| < 64), so |r2_f32 - r2| < 6e-7 r2 + 1e-5; the band is wider.
+__device__ __forceinline__ float in_band(float R2) { return 1e-5f * R2 + 1e-3f; }
+
+template <bool CLAIM>
+__global__ void __launch_bounds__(32 * kShellWarps) k_shell(DeviceParticles P, Geometry g, int* owner, int full) {
+    const int lane = threadIdx.x & 31;
+    const int p = blockIdx.x * kShellWarps + (threadIdx.x >> 5);
+    if (p >= P.npart) return;                       // whole warps leave together
+    const SphereGeom G = P.geom[p];
+    const float delta = full ? 0.f : G.delta;
+    const float Rf = P.Rf, R2 = Rf * Rf, band = in_band(R2);
+    float r_in, r_out;
+    if (CLAIM) {
+        r_in = full ? -1.f : Rf - delta - kShellEps;
+        r_out = Rf + kShellEps;
+    } else {
+        r_in = Rf - kShellEps;
+        r_out = Rf + delta + kShellEps;
+    }
+    const float ext = r_out + 1.f;
+    const Range rx = box_g(G.ci[0], G.h[0], ext, g.NZ, false);
+    const Range ry = box_g(G.ci[1], G.h[1], ext, g.NX, true);
+    const Range rz = box_g(G.ci[2], G.h[2], ext, g.NY, true);
+    const float yl0 = (float)(ry.lo - G.ci[1]) + G.h[1];    // offset of row node a = 0
+    const float ro2 = r_out * r_out, ri2 = r_in > 0.f ? r_in * r_in : -1.f;
+    const int nrows = rz.n * rx.n;
+    if (nrows <= 0) return;
+    // rows b + rz.n * c, lane-strided without a division per row
+    int b = lane % rz.n, c = lane / rz.n;
+    const int sb = 32 % rz.n, sc = 32 / rz.n;
+    for (int r = lane; r < nrows; r += 32) {
+        const float oz = (float)(rz.lo + b - G.ci[2]) + G.h[2], ox = (float)(rx.lo + c - G.ci[0]) + G.h[0];
+        const float rho2 = oz * oz + ox * ox;
+        if (rho2 <= ro2) {
+            const float hi = sqrtf(ro2 - rho2);
+            const float lo = rho2 < ri2 ? sqrtf(ri2 - rho2) : -1.f;
+            const int ix = rx.lo + c, iz = wrapi(rz.lo + b, g.NY);
+            // row nodes with |y| in [lo, hi]: one segment, or two around the hole
+            int s0[2], s1[2];
+            if (lo < 0.f) {
+                s0[0] = (int)ceilf(-hi - yl0); s1[0] = (int)floorf(hi - yl0);
+                s0[1] = 0; s1[1] = -1;
+            } else {
+                s0[0] = (int)ceilf(-hi - yl0); s1[0] = (int)floorf(-lo - yl0);
+                s0[1] = (int)ceilf(lo - yl0); s1[1] = (int)floorf(hi - yl0);
+            }
+            for (int k = 0; k < 2; ++k) {
+                const int a0 = max(s0[k], 0), a1 = min(s1[k], ry.n - 1);
+                for (int a = a0; a <= a1; ++a) {
+                    const float oy = (float)(ry.lo + a - G.ci[1]) + G.h[1];
+                    const float r2 = rho2 + oy * oy;
+                    const int iy = wrapi(ry.lo + a, g.NX);
+                    bool in;
+                    if (r2 < R2 - band) in = true;
+                    else if (r2 > R2 + band) in = false;
+                    else {
+                        double d[3];
+                        offset(P, g, p, ix, iy, iz, d);
+                        in = inside(d, P.R);
+                    }
+                    const uint32_t n = gnode(g, ix, iy, iz);
+                    if (CLAIM) {
+                        if (in) owner[n] = p;
+                    } else if (!in && owner[n] == p) {
+                        owner[n] = -2;
+                        const unsigned q = atomicAdd(&P.counters[0], 1u);
+                        if (q < (unsigned)P.refill_cap) {
+                            P.refill_node[q] = n;
+                            P.refill_part[q] = p;
+                        } else {
+                            atomicOr(&P.counters[3], 1u);      // refill list overflow
+                        }
+                    }
+                }
+            }
         }
-        if (in) continue;
-        owner[n] = -2;
-        const unsigned k = atomicAdd(&P.counters[0], 1u);
-        if (k < (unsigned)P.refill_cap) {
-            P.refill_node[k] = n;
-            P.refill_part[k] = p;
-        } else {
-            atomicExch(&P.counters[3], 1u);      // refill list overflow
-        }
+        b += sb;
+        c += sc;
+        if (b >= rz.n) { b -= rz.n; ++c; }
     }
 }
 
@@ -466,16 +535,15 @@ __host__ __device__ inline IbbPlan ibb_plan(double R, int wbits) {
 
 template <typename T, typename RT, typename W>
 __global__ void __launch_bounds__(kPThreads, sizeof(RT) == 8 ? 2 : 4)
-    k_ibb(DeviceState s, DeviceParticles P, int parity) {
+    k_ibb(DeviceState s, DeviceParticles P, int parity, IbbPlan pl) {
     extern __shared__ __align__(16) unsigned char ibb_smem[];
     const Geometry& g = s.g;
     const int p = blockIdx.x;
-    const double R = P.R;
-    const IbbPlan pl = ibb_plan(R, 8 * (int)sizeof(W));
-    const double ext = R + 1.5;
-    const Range rx = box(P.pos[3 * p], ext, g.NZ, false);
-    const Range ry = box(P.pos[3 * p + 1], ext, g.NX, true);
-    const Range rz = box(P.pos[3 * p + 2], ext, g.NY, true);
+    const SphereGeom G = P.geom[p];
+    const float ext = P.Rf + 1.5f;
+    const Range rx = box_g(G.ci[0], G.h[0], ext, g.NZ, false);
+    const Range ry = box_g(G.ci[1], G.h[1], ext, g.NX, true);
+    const Range rz = box_g(G.ci[2], G.h[2], ext, g.NY, true);
     const int SA = ry.n + 4, SB = rz.n + 4, SC = rx.n + 4;
     const int ya = ry.lo - 2, zb = rz.lo - 2, xc = rx.lo - 2;   // node of staged index 0
     W* own = reinterpret_cast<W*>(ibb_smem + pl.rows_off);
@@ -488,20 +556,19 @@ __global__ void __launch_bounds__(kPThreads, sizeof(RT) == 8 ? 2 : 4)
     int* wC = wB + pl.S;
     int* wZ = wC + pl.S;
     uint32_t* queue = reinterpret_cast<uint32_t*>(ibb_smem + pl.queue_off);
-    const Centre cen = centre_of(P, p);
-    const int cix = (int)floor(cen.x), ciy = (int)floor(cen.y), ciz = (int)floor(cen.z);
+    const int cix = G.ci[0], ciy = G.ci[1], ciz = G.ci[2];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int t = threadIdx.x; t < SA; t += blockDim.x) {
-        tA[t] = (float)(ya + t - ciy) + (0.5f - (float)(cen.y - ciy));
+        tA[t] = (float)(ya + t - ciy) + G.h[1];
         wA[t] = wrapi(ya + t, g.NX);
     }
     for (int t = threadIdx.x; t < SB; t += blockDim.x) {
-        tB[t] = (float)(zb + t - ciz) + (0.5f - (float)(cen.z - ciz));
+        tB[t] = (float)(zb + t - ciz) + G.h[2];
         wZ[t] = wrapi(zb + t, g.NY);
         wB[t] = wZ[t] * g.NX;
     }
     for (int t = threadIdx.x; t < SC; t += blockDim.x) {
-        tC[t] = (float)(xc + t - cix) + (0.5f - (float)(cen.x - cix));
+        tC[t] = (float)(xc + t - cix) + G.h[0];
         wC[t] = (xc + t) * (g.NX * g.NY);
     }
     // staging: one warp per row, lane j holds nodes a = j (and j + 32)
@@ -549,10 +616,18 @@ __global__ void __launch_bounds__(kPThreads, sizeof(RT) == 8 ? 2 : 4)
     Bx.SB = pl.S; Bx.own = own; Bx.fluid = fluid;
     Bx.tA = tA; Bx.tB = tB; Bx.tC = tC; Bx.wA = wA; Bx.wB = wB; Bx.wC = wC; Bx.wZ = wZ;
     Bx.xlo = xc;
-    Bx.R2f = (float)(R * R);
+    Bx.R2f = P.Rf * P.Rf;
     RT UW[6];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) { UW[k] = (RT)P.vel[3 * p + k]; UW[3 + k] = (RT)P.omg[3 * p + k]; }
+    for (int k = 0; k < 3; ++k) {
+        if constexpr (sizeof(RT) == 8) {
+            UW[k] = P.vel[3 * p + k];
+            UW[3 + k] = P.omg[3 * p + k];
+        } else {
+            UW[k] = G.U[k];
+            UW[3 + k] = G.W[k];
+        }
+    }
     RT acc[6] = {0, 0, 0, 0, 0, 0};
     const unsigned lt = (1u << lane) - 1u;
     uint32_t* q = queue + wid * kIbbQueue;
@@ -624,7 +699,7 @@ cudaError_t launch_ibb(const DeviceState& s, const DeviceParticles& P, int parit
         const cudaError_t e = cudaFuncSetAttribute(k_ibb<T, RT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    k_ibb<T, RT, W><<<P.npart, kPThreads, smem, st>>>(s, P, parity);
+    k_ibb<T, RT, W><<<P.npart, kPThreads, smem, st>>>(s, P, parity, ibb_plan(P.R, 8 * (int)sizeof(W)));
     return cudaGetLastError();
 }
 
@@ -692,6 +767,132 @@ __global__ void __launch_bounds__(kRepTile) k_repulsion(DeviceParticles P, Geome
     P.rep[3 * s] = rep[0]; P.rep[3 * s + 1] = rep[1]; P.rep[3 * s + 2] = rep[2];
 }
 
+// Cell of a sphere centre in the repulsion cell list (cells of equal width
+// along each axis, at least one reach wide).
+__device__ __forceinline__ int cell_of(const DeviceParticles& P, const Geometry& g, int s, int& cx, int& cy, int& cz) {
+    cx = min(P.cell_nx - 1, max(0, (int)(P.pos[3 * s] * P.cell_nx / g.NZ)));
+    cy = min(P.cell_ny - 1, max(0, (int)(P.pos[3 * s + 1] * P.cell_ny / g.NX)));
+    cz = min(P.cell_nz - 1, max(0, (int)(P.pos[3 * s + 2] * P.cell_nz / g.NY)));
+    return cx + P.cell_nx * (cy + P.cell_ny * cz);
+}
+
+__global__ void k_bin(DeviceParticles P, Geometry g) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= P.npart) return;
+    int cx, cy, cz;
+    const int cell = cell_of(P, g, s, cx, cy, cz);
+    const int k = atomicAdd(&P.cell_count[cell], 1);
+    if (k < kCellCap) P.cell_list[(size_t)cell * kCellCap + k] = s;
+    else atomicExch(&P.counters[2], 1u);
+}
+
+// exact FP64 pair term of spheres s and t (old positions), as the oracle
+__device__ __forceinline__ void pair_repulsion(const DeviceParticles& P, double L1, double L2, int s, int t,
+                                               double rep[3]) {
+    const double d0 = __dsub_rn(P.pos[3 * t], P.pos[3 * s]);
+    const double d1 = dmin_image(__dsub_rn(P.pos[3 * t + 1], P.pos[3 * s + 1]), L1);
+    const double d2 = dmin_image(__dsub_rn(P.pos[3 * t + 2], P.pos[3 * s + 2]), L2);
+    const double dd[3] = {d0, d1, d2};
+    const double dist = __dsqrt_rn(norm2_rn(dd));
+    const double fm = repulse(__dsub_rn(dist, 2.0 * P.R), P.zeta, P.stf0, P.stf1);
+    if (fm != 0.0 && dist > 0.0) {
+        rep[0] = __dsub_rn(rep[0], __ddiv_rn(__dmul_rn(fm, d0), dist));
+        rep[1] = __dsub_rn(rep[1], __ddiv_rn(__dmul_rn(fm, d1), dist));
+        rep[2] = __dsub_rn(rep[2], __ddiv_rn(__dmul_rn(fm, d2), dist));
+    }
+}
+
+// Repulsion from the cell list: one warp per sphere, lane k < 27 on one
+// neighbour cell.  Partners within reach (FP32 screen with a margin) are
+// collected, sorted by sphere id and summed in that order with the exact
+// FP64 pair term, so that the result is the oracle's index-ordered sum.  A
+// bin that overflowed at this step sends every sphere to the all-pairs scan.
+constexpr int kRepWarps = 8;
+constexpr int kRepMaxPartners = 64;
+__global__ void __launch_bounds__(32 * kRepWarps) k_repulsion_cells(DeviceParticles P, Geometry g) {
+    __shared__ int partners[kRepWarps][kRepMaxPartners];
+    __shared__ int npart_w[kRepWarps];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int s = blockIdx.x * kRepWarps + w;
+    if (s >= P.npart) return;                       // whole warps leave together
+    const double R = P.R;
+    const double L1 = (double)g.NX, L2 = (double)g.NY;
+    const float fL1 = (float)L1, fL2 = (float)L2;
+    const float reach = (float)(2.0 * R + P.zeta) + 0.01f;
+    const float reach2 = reach * reach;
+    const float fx0 = (float)P.pos[3 * s], fx1 = (float)P.pos[3 * s + 1], fx2 = (float)P.pos[3 * s + 2];
+    if (lane == 0) npart_w[w] = 0;
+    __syncwarp();
+    const bool all_pairs = *(volatile unsigned*)&P.counters[2] != 0;
+    auto consider = [&](int t) {
+        if (t == s) return;
+        float e0 = (float)P.pos[3 * t] - fx0, e1 = (float)P.pos[3 * t + 1] - fx1, e2 = (float)P.pos[3 * t + 2] - fx2;
+        e1 = e1 >= 0.5f * fL1 ? e1 - fL1 : (e1 < -0.5f * fL1 ? e1 + fL1 : e1);
+        e2 = e2 >= 0.5f * fL2 ? e2 - fL2 : (e2 < -0.5f * fL2 ? e2 + fL2 : e2);
+        if (e0 * e0 + e1 * e1 + e2 * e2 > reach2) return;
+        const int k = atomicAdd(&npart_w[w], 1);
+        if (k < kRepMaxPartners) partners[w][k] = t;
+    };
+    if (all_pairs) {
+        for (int t = lane; t < P.npart; t += 32) consider(t);
+    } else if (lane < 27) {
+        int cx, cy, cz;
+        cell_of(P, g, s, cx, cy, cz);
+        const int ox = lane % 3 - 1, oy = (lane / 3) % 3 - 1, oz = lane / 9 - 1;
+        const int nx = cx + ox;
+        if (nx >= 0 && nx < P.cell_nx) {
+            const int ny = (cy + oy + P.cell_ny) % P.cell_ny, nz = (cz + oz + P.cell_nz) % P.cell_nz;
+            const int cell = nx + P.cell_nx * (ny + P.cell_ny * nz);
+            const int n = min(P.cell_count[cell], kCellCap);
+            for (int k = 0; k < n; ++k) consider(P.cell_list[(size_t)cell * kCellCap + k]);
+        }
+    }
+    __syncwarp();
+    if (lane != 0) return;
+    const int n = npart_w[w];
+    double rep[3] = {0.0, 0.0, 0.0};
+    if (n <= kRepMaxPartners) {
+        int* list = partners[w];
+        for (int i = 1; i < n; ++i) {                // insertion sort by sphere id
+            const int v = list[i];
+            int j = i - 1;
+            while (j >= 0 && list[j] > v) { list[j + 1] = list[j]; --j; }
+            list[j + 1] = v;
+        }
+        for (int i = 0; i < n; ++i) pair_repulsion(P, L1, L2, s, list[i], rep);
+    } else {
+        for (int t = 0; t < P.npart; ++t)            // a crowd beyond the list: plain index order
+            if (t != s) pair_repulsion(P, L1, L2, s, t, rep);
+    }
+    const double xs0 = P.pos[3 * s];
+    const double hl = __dsub_rn(xs0, R), hu = __dsub_rn(__dsub_rn((double)g.NZ, xs0), R);
+    rep[0] = __dadd_rn(rep[0], repulse(hl, P.zeta, P.stf0_w, P.stf1_w));
+    rep[0] = __dsub_rn(rep[0], repulse(hu, P.zeta, P.stf0_w, P.stf1_w));
+    P.rep[3 * s] = rep[0]; P.rep[3 * s + 1] = rep[1]; P.rep[3 * s + 2] = rep[2];
+}
+
+// Geometry record of sphere s from its FP64 state; delta: displacement of
+// the update just made.
+__device__ __forceinline__ void write_geom(const DeviceParticles& P, int s, double delta) {
+    SphereGeom G;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const double c = P.pos[3 * s + a];
+        G.ci[a] = (int)floor(c);
+        G.h[a] = 0.5f - (float)(c - (double)G.ci[a]);
+        G.U[a] = (float)P.vel[3 * s + a];
+        G.W[a] = (float)P.omg[3 * s + a];
+        G.pad[a] = 0.f;
+    }
+    G.delta = __double2float_ru(delta);
+    P.geom[s] = G;
+}
+
+__global__ void k_geom(DeviceParticles P) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < P.npart) write_geom(P, s, 0.0);
+}
+
 // Newton-Euler update (second-order Adams-Bashforth, FP64); the body force
 // that drives the fluid also acts on the sphere volume.
 __global__ void k_newton(DeviceParticles P, Geometry g, double bfx, double bfy, double bfz, int have_prev) {
@@ -712,9 +913,24 @@ __global__ void k_newton(DeviceParticles P, Geometry g, double bfx, double bfy, 
         const double u1 = __dadd_rn(u0, __ddiv_rn(__dsub_rn(__dmul_rn(1.5, Ft), __dmul_rn(0.5, fp)), m));
         P.vel[3 * s + a] = u1;
         P.omg[3 * s + a] = __dadd_rn(P.omg[3 * s + a], __ddiv_rn(__dsub_rn(__dmul_rn(1.5, Tt), __dmul_rn(0.5, tp)), I));
+        P.pos_prev[3 * s + a] = P.pos[3 * s + a];
         P.pos[3 * s + a] = __dadd_rn(P.pos[3 * s + a], __dmul_rn(0.5, __dadd_rn(u0, u1)));
         P.fprev[3 * s + a] = Ft;
         P.tprev[3 * s + a] = Tt;
+    }
+    // a non-finite or runaway state (more than one lattice unit per step)
+    // stops the sphere where it was and is reported by the host
+    bool bad = false;
+    for (int a = 0; a < 3; ++a)
+        bad |= !(fabs(P.vel[3 * s + a]) <= 1.0) || !(fabs(P.pos[3 * s + a] - P.pos_prev[3 * s + a]) <= 1.0);
+    if (bad) {
+        for (int a = 0; a < 3; ++a) P.pos[3 * s + a] = P.pos_prev[3 * s + a];
+        atomicOr(&P.counters[3], 2u);
+    }
+    double disp2 = 0.0;
+    for (int a = 0; a < 3; ++a) {
+        const double d = P.pos[3 * s + a] - P.pos_prev[3 * s + a];
+        disp2 += d * d;
     }
     double y = P.pos[3 * s + 1], z = P.pos[3 * s + 2];
     if (y >= L1) y = __dsub_rn(y, L1);
@@ -723,6 +939,7 @@ __global__ void k_newton(DeviceParticles P, Geometry g, double bfx, double bfy, 
     else if (z < 0.0) z = __dadd_rn(z, L2);
     P.pos[3 * s + 1] = y;
     P.pos[3 * s + 2] = z;
+    write_geom(P, s, sqrt(disp2));
 }
 
 __device__ __forceinline__ void feq_dev(double rho, double ux, double uy, double uz, double* fe) {
@@ -735,12 +952,8 @@ __device__ __forceinline__ void feq_dev(double rho, double ux, double uy, double
     }
 }
 
-// Refilling of nodes queued by k_release that are still fluid (-2).
 template <typename T>
-__global__ void k_refill(DeviceState s, DeviceParticles P, int parity) {
-    const unsigned k = blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned cnt = min(P.counters[0], (unsigned)P.refill_cap);
-    if (k >= cnt) return;
+__device__ __forceinline__ void refill_node(const DeviceState& s, const DeviceParticles& P, int parity, unsigned k) {
     const Geometry& g = s.g;
     const uint32_t n = P.refill_node[k];
     const int* owner = P.owner;
@@ -795,12 +1008,20 @@ __global__ void k_refill(DeviceState s, DeviceParticles P, int parity) {
     for (int i = 0; i < Q; ++i) write_nat<T>(s, parity, i, ix, iy, iz, __dadd_rn(fe[i], __dsub_rn(gq[i], fn[i])));
 }
 
-__global__ void k_refill_done(DeviceParticles P) {
-    const unsigned k = blockIdx.x * blockDim.x + threadIdx.x;
+// Refilling of nodes queued by k_shell<release> that are still fluid (-2).
+template <typename T>
+__global__ void k_refill(DeviceState s, DeviceParticles P, int parity) {
     const unsigned cnt = min(P.counters[0], (unsigned)P.refill_cap);
-    if (k >= cnt) return;
-    const uint32_t n = P.refill_node[k];
-    if (P.owner[n] == -2) P.owner[n] = -1;
+    for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x)
+        refill_node<T>(s, P, parity, k);
+}
+
+__global__ void k_refill_done(DeviceParticles P) {
+    const unsigned cnt = min(P.counters[0], (unsigned)P.refill_cap);
+    for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x) {
+        const uint32_t n = P.refill_node[k];
+        if (P.owner[n] == -2) P.owner[n] = -1;
+    }
 }
 
 __global__ void k_count_solid(const int* owner, size_t N, unsigned long long* out) {
@@ -817,7 +1038,8 @@ size_t particles_smem_bytes(double R) { return ibb_smem_bytes(R); }
 
 cudaError_t particles_claim(const DeviceState& s, const DeviceParticles& P, cudaStream_t st) {
     if (P.npart == 0) return cudaSuccess;
-    k_claim<<<P.npart, kPThreads, 0, st>>>(P, s.g, P.owner);
+    k_geom<<<(P.npart + 127) / 128, 128, 0, st>>>(P);
+    k_shell<true><<<(P.npart + kShellWarps - 1) / kShellWarps, 32 * kShellWarps, 0, st>>>(P, s.g, P.owner, 1);
     return cudaGetLastError();
 }
 
@@ -844,11 +1066,20 @@ cudaError_t particles_after_step(const DeviceState& s, const DeviceParticles& P,
             break;
     }
     if (e != cudaSuccess) return e;
-    k_repulsion<<<(P.npart + kRepTile - 1) / kRepTile, kRepTile, 0, st>>>(P, s.g);
+    if (P.ncell > 0) {
+        e = cudaMemsetAsync(P.cell_count, 0, (size_t)P.ncell * sizeof(int), st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(P.counters + 2, 0, sizeof(unsigned), st);
+        if (e != cudaSuccess) return e;
+        k_bin<<<(P.npart + 255) / 256, 256, 0, st>>>(P, s.g);
+        k_repulsion_cells<<<(P.npart + kRepWarps - 1) / kRepWarps, 32 * kRepWarps, 0, st>>>(P, s.g);
+    } else {
+        k_repulsion<<<(P.npart + kRepTile - 1) / kRepTile, kRepTile, 0, st>>>(P, s.g);
+    }
     k_newton<<<(P.npart + 127) / 128, 128, 0, st>>>(P, s.g, s.cd.Fx, s.cd.Fy, s.cd.Fz, have_prev);
-    k_release<<<P.npart, kPThreads, 0, st>>>(P, s.g, P.owner);
-    k_claim<<<P.npart, kPThreads, 0, st>>>(P, s.g, P.owner);
-    const unsigned nb = (unsigned)((P.refill_cap + 255) / 256);
+    k_shell<false><<<(P.npart + kShellWarps - 1) / kShellWarps, 32 * kShellWarps, 0, st>>>(P, s.g, P.owner, 0);
+    k_shell<true><<<(P.npart + kShellWarps - 1) / kShellWarps, 32 * kShellWarps, 0, st>>>(P, s.g, P.owner, 0);
+    // refills: a few per sphere and step; a grid of 4 CTAs per SM strides the list
+    const unsigned nb = (unsigned)std::min<long long>((P.refill_cap + 255) / 256, 4LL * std::max(s.sm_count, 1));
     switch (s.prec) {
         case LBM_PREC_FP64: k_refill<double><<<nb, 256, 0, st>>>(s, P, parity); break;
         case LBM_PREC_FP32: k_refill<float><<<nb, 256, 0, st>>>(s, P, parity); break;
