@@ -356,7 +356,7 @@ def run_gpu(args, world, rank, local):
             "data": "synthetic (seeded Poiseuille + uniform noise initial state)",
             "config": {"workload": wname, "storage": prec, "nodes": N,
                        "grid_stream_span_wall": [cfg.stream, cfg.span, cfg.wall], "visc": cfg.visc,
-                       "ustar": cfg.ustar, "h": cfg.h, "mrt": "MRTtype 1 (para.f90)",
+                       "ustar": cfg.ustar, "h": cfg.h, "mrt": "MRTtype 1 (para.f90)" + (f", s16={cfg.s16} (sphere-laden)" if cfg.s16 else ""),
                        "l2": f"populations {N * 19 * BYTES[prec] / 1e9:.1f} GB >> 129 MB L2, no flush needed",
                        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
             "roofline": roof, "clocks": clocks, "gpu_launches": args.steps,
@@ -379,7 +379,8 @@ def accuracy_window(pkg, cfg, prec, steps, device, pos):
             lat.step(steps)
             d1 = lat.diag()
             part = lat.particles() if pos is not None else None
-            res[p] = (pkg.statistics(lat.profiles(), cfg.ustar), d1.rho_sum - d0.rho_sum, part)
+            res[p] = (pkg.statistics(lat.profiles(), cfg.ustar), d1.rho_sum - d0.rho_sum, part,
+                      d1.rho_sum / max(d1.nfluid, 1) - d0.rho_sum / max(d0.nfluid, 1))
     ref, lp = res["fp64"][0], res[prec][0]
     mref = ref["mean"][:, 1]
     out["steps"] = steps
@@ -389,6 +390,10 @@ def accuracy_window(pkg, cfg, prec, steps, device, pos):
     out["reynolds_stress_max_fp64"] = float(np.abs(sref).max())
     out["mass_drift_fp64"] = res["fp64"][1]
     out[f"mass_drift_{prec}"] = res[prec][1]
+    # with spheres the fluid node set changes as surfaces cover and uncover
+    # nodes; the mean density over the fluid nodes is the comparable figure
+    out["mean_density_drift_fp64"] = res["fp64"][3]
+    out[f"mean_density_drift_{prec}"] = res[prec][3]
     if pos is not None:
         a, b = res[prec][2], res["fp64"][2]
         fb = b["force"]

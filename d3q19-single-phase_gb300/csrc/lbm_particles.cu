@@ -66,35 +66,6 @@ __device__ __forceinline__ int opp_rt(int i) {
 }
 __device__ __forceinline__ double w_rt(int i) { return i == 0 ? W0 : (i <= 6 ? W1 : W2); }
 
-// Walk a bounding box with a stride of blockDim.x nodes without integer
-// division per node; callers put the streamwise (contiguous) axis first so
-// that the lanes of a warp touch neighbouring addresses.
-struct BoxWalk {
-    int a, b, c, na, nb, nc;
-    int sa, sb, sc;                       // the stride in mixed radix (na, nb)
-    __device__ __forceinline__ BoxWalk(int t, int step, int na_, int nb_, int nc_) : na(na_), nb(nb_), nc(nc_) {
-        if (na <= 0 || nb <= 0) { a = b = 0; c = nc; sa = sb = sc = 0; return; }
-        a = t % na;
-        const int r = t / na;
-        b = r % nb;
-        c = r / nb;
-        sa = step % na;
-        const int rs = step / na;
-        sb = rs % nb;
-        sc = rs / nb;
-    }
-    __device__ __forceinline__ bool valid() const { return c < nc; }
-    __device__ __forceinline__ void advance() {
-        a += sa;
-        int carry = 0;
-        if (a >= na) { a -= na; carry = 1; }
-        b += sb + carry;
-        carry = 0;
-        if (b >= nb) { b -= nb; carry = 1; }
-        c += sc + carry;
-    }
-};
-
 __device__ __forceinline__ double dmin_image(double d, double L) {
     if (d >= 0.5 * L) d = __dsub_rn(d, L);
     else if (d < -0.5 * L) d = __dadd_rn(d, L);
@@ -114,52 +85,11 @@ __device__ __forceinline__ double norm2_rn(const double d[3]) {
 }
 __device__ __forceinline__ bool inside(const double d[3], double R) { return norm2_rn(d) <= __dmul_rn(R, R); }
 
-// Inside test screened in FP32 (node and centre coordinates rounded to FP32,
-// error well below the band); only nodes within the band around the surface
-// get the exact FP64 test, which is the one the oracle uses.
-struct Centre { double x, y, z; float fx, fy, fz; };
-__device__ __forceinline__ Centre centre_of(const DeviceParticles& P, int p) {
-    Centre c;
-    c.x = P.pos[3 * p]; c.y = P.pos[3 * p + 1]; c.z = P.pos[3 * p + 2];
-    c.fx = (float)c.x; c.fy = (float)c.y; c.fz = (float)c.z;
-    return c;
-}
-__device__ __forceinline__ float fmin_image(float d, float L) {
-    return d >= 0.5f * L ? d - L : (d < -0.5f * L ? d + L : d);
-}
-__device__ __forceinline__ float dist2_fast(const Centre& c, const Geometry& g, int ix, int iy, int iz) {
-    const float x = ((float)ix + 0.5f) - c.fx;
-    const float y = fmin_image(((float)iy + 0.5f) - c.fy, (float)g.NX);
-    const float z = fmin_image(((float)iz + 0.5f) - c.fz, (float)g.NY);
-    return x * x + y * y + z * z;
-}
-// 1 inside, 0 outside, -1 undecided (needs the exact FP64 test)
-__device__ __forceinline__ int inside_screen(float r2, double R) {
-    const float R2 = (float)(R * R);
-    const float band = 1e-3f * R2 + 0.05f;
-    return r2 < R2 - band ? 1 : (r2 > R2 + band ? 0 : -1);
-}
-
 // periodic wrap of an index within one period of [0, n) (all callers stay
 // within [-n, 2n): box edges and stencils reach at most R + 3 nodes out)
 __device__ __forceinline__ int wrapi(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
 
-// node-index range of a bounding box along one axis (same rule as the oracle)
 struct Range { int lo, n; };
-__device__ __forceinline__ Range box(double c, double ext, int n, bool periodic) {
-    int a = (int)floor(__dsub_rn(__dsub_rn(c, ext), 0.5));
-    int b = (int)ceil(__dsub_rn(__dadd_rn(c, ext), 0.5));
-    if (periodic) {
-        if (b - a + 1 >= n) { a = 0; b = n - 1; }
-    } else {
-        if (a < 0) a = 0;
-        if (b > n - 1) b = n - 1;
-    }
-    Range r;
-    r.lo = a;
-    r.n = b >= a ? b - a + 1 : 0;
-    return r;
-}
 
 // Node range of a bounding box along one axis from the geometry record:
 // nodes whose centres lie within ext of the sphere centre, plus any node
@@ -255,7 +185,10 @@ __device__ __forceinline__ void write_nat(const DeviceState& s, int parity, int 
 // the bounding box, intersects each row with that shell in FP32 (with a
 // margin far above the FP32 error) and decides the few nodes found by their
 // FP32 squared distance, or by the exact FP64 test of the oracle where that
-// lies within kInBand of R^2.  `full` claims every node inside (placement).
+// lies within in_band() of R^2.  `full` claims every node inside (placement).
+// Claims take the highest sphere index (atomicMax), the oracle's outcome of
+// claiming in index order where spheres overlap; nodes that a sphere released
+// inside another one are claimed by k_reclaim.
 constexpr int kShellWarps = 4;
 constexpr float kShellEps = 0.01f;
 
@@ -323,7 +256,7 @@ __global__ void __launch_bounds__(32 * kShellWarps) k_shell(DeviceParticles P, G
                     }
                     const uint32_t n = gnode(g, ix, iy, iz);
                     if (CLAIM) {
-                        if (in) owner[n] = p;
+                        if (in) atomicMax(owner + n, p);        // the highest index among overlapping spheres
                     } else if (!in && owner[n] == p) {
                         owner[n] = -2;
                         const unsigned q = atomicAdd(&P.counters[0], 1u);
@@ -402,133 +335,171 @@ __device__ __forceinline__ W shift_a(W x, int cy) {
 __device__ __forceinline__ int lowest_bit(uint32_t m) { return __ffs((int)m) - 1; }
 __device__ __forceinline__ int lowest_bit(unsigned long long m) { return __ffsll((long long)m) - 1; }
 
-// per-direction constants, from selects (no conversions)
-template <typename RT>
+// per-direction constants (a shared-memory table built once per CTA)
 struct IbbDir {
-    int cx, cy, cz, ib;
-    RT fcx, fcy, fcz, mw6, qa, inv_qa;
+    float fcx, fcy, fcz, mw6;     // c_i as floats, -6 w_i
+    float qa, inv_qa;             // |c_i|^2 and its inverse
+    int packed;                   // (cx+1) | (cy+1) << 2 | (cz+1) << 4 | opp(i) << 8
+    int pad;
 };
-template <typename RT>
-__device__ __forceinline__ IbbDir<RT> ibb_dir(int i) {
-    IbbDir<RT> d;
-    d.cx = cx_rt(i); d.cy = cy_rt(i); d.cz = cz_rt(i); d.ib = opp_rt(i);
-    d.fcx = d.cx > 0 ? RT(1) : (d.cx < 0 ? RT(-1) : RT(0));
-    d.fcy = d.cy > 0 ? RT(1) : (d.cy < 0 ? RT(-1) : RT(0));
-    d.fcz = d.cz > 0 ? RT(1) : (d.cz < 0 ? RT(-1) : RT(0));
-    const bool axis = i <= 6;
-    d.mw6 = axis ? RT(-6.0 * W1) : RT(-6.0 * W2);
-    d.qa = axis ? RT(1) : RT(2);
-    d.inv_qa = axis ? RT(1) : RT(0.5);
-    return d;
-}
 
 // staged box of one sphere, in shared memory
 template <typename W>
 struct IbbBox {
-    int SB;                       // row stride: row (b, c) at b + SB * c
+    int S;                        // row stride: row (b, c) at b + S * c
     const W* own;                 // bit a: owned by this sphere
     const W* fluid;               // bit a: fluid
+    const int* rowIdx;            // node-index term of row (b, c)
     const float *tA, *tB, *tC;    // FP32 offset from the centre per staged index
-    const int *wA, *wB, *wC;      // node-index terms per staged index
-    const int* wZ;                // wrapped spanwise index per staged b (FP64 path)
+    const int* wA;                // wrapped streamwise node per staged a
+    const int* wZ;                // wrapped spanwise node per staged b (FP64 path)
+    const IbbDir* dir;            // [Q]
     int xlo;                      // wall-normal node of staged c = 0
     float R2f;                    // R^2 in FP32
 };
 
-// One link: staged coordinates (a, b, c) of the fluid node, direction i.
-// Adds the exchanged momentum and its moment to acc[6].
+// A link between its gathers and its finish: geometry, wall velocity and the
+// populations read.
+template <typename T, typename RT>
+struct IbbLink {
+    RT q, x0, x1, x2, fcx, fcy, fcz, uw0, uw1, uw2, mw, A, X, Y;
+    T* w;                         // storage of the returning population
+    bool ok1, ok2;
+};
+
+// Gathers of one link: entry (a, b, c, i) = staged coordinates of the fluid
+// node and the direction.  X and Y are the interpolation partners: (B, C) at
+// x_f, x_f - c_i in direction i for q < 1/2, (D, E) at x_f - c_i, x_f - 2c_i
+// in direction opp(i) otherwise.
 template <typename T, typename RT, typename W>
-__device__ __forceinline__ void ibb_link(const DeviceState& s, const DeviceParticles& P, int p, int parity,
-                                         const IbbBox<W>& B, int i, int a, int b, int c, const RT (&UW)[6],
-                                         RT (&acc)[6]) {
-    const IbbDir<RT> d = ibb_dir<RT>(i);
-    const bool ok1 = (B.fluid[(b - d.cz) + B.SB * (c - d.cx)] >> (a - d.cy)) & 1;
-    const bool ok2 = ok1 && ((B.fluid[(b - 2 * d.cz) + B.SB * (c - 2 * d.cx)] >> (a - 2 * d.cy)) & 1);
-    const uint32_t gx = (uint32_t)(B.wA[a] + B.wB[b] + B.wC[c]);
-    const uint32_t gs = (uint32_t)(B.wA[a + d.cy] + B.wB[b + d.cz] + B.wC[c + d.cx]);
+__device__ __forceinline__ IbbLink<T, RT> ibb_gather(const DeviceState& s, const DeviceParticles& P, int p,
+                                                     int parity, const IbbBox<W>& B, uint32_t v, const RT (&UW)[6]) {
+    IbbLink<T, RT> L;
+    const int a = v & 255, b = (v >> 8) & 255, c = (v >> 16) & 255, i = (int)(v >> 24);
+    const IbbDir D = B.dir[i];
+    const int cx = (D.packed & 3) - 1, cy = ((D.packed >> 2) & 3) - 1, cz = ((D.packed >> 4) & 3) - 1;
+    const int ib = D.packed >> 8;
+    const int dr = cz + B.S * cx;                      // row offset of c_i
+    const int r0 = b + B.S * c;
+    L.ok1 = (B.fluid[r0 - dr] >> (a - cy)) & 1;
+    L.ok2 = L.ok1 && ((B.fluid[r0 - 2 * dr] >> (a - 2 * cy)) & 1);
+    const uint32_t gx = (uint32_t)(B.wA[a] + B.rowIdx[r0]);
+    const uint32_t gs = (uint32_t)(B.wA[a + cy] + B.rowIdx[r0 + dr]);
     uint32_t ga = 0, gb = 0;
-    if (ok1) ga = (uint32_t)(B.wA[a - d.cy] + B.wB[b - d.cz] + B.wC[c - d.cx]);
-    if (ok2) gb = (uint32_t)(B.wA[a - 2 * d.cy] + B.wB[b - 2 * d.cz] + B.wC[c - 2 * d.cx]);
+    if (L.ok1) ga = (uint32_t)(B.wA[a - cy] + B.rowIdx[r0 - dr]);
+    if (L.ok2) gb = (uint32_t)(B.wA[a - 2 * cy] + B.rowIdx[r0 - 2 * dr]);
     const T* Pi = plane<T>(s, i);
-    const T* Pib = plane<T>(s, d.ib);
-    RT q, d0, d1, d2;
+    const T* Pib = plane<T>(s, ib);
+    RT d0, d1, d2;
     if constexpr (sizeof(RT) == 8) {
         double dd[3];
         offset(P, s.g, p, B.xlo + c, B.wA[a], B.wZ[b], dd);
-        q = link_q<double>(dd, d.cx, d.cy, d.cz, __dsub_rn(norm2_rn(dd), __dmul_rn(P.R, P.R)));
+        L.q = link_q<double>(dd, cx, cy, cz, __dsub_rn(norm2_rn(dd), __dmul_rn(P.R, P.R)));
         d0 = dd[0]; d1 = dd[1]; d2 = dd[2];
+        L.fcx = cx; L.fcy = cy; L.fcz = cz;
     } else {
+        L.fcx = D.fcx; L.fcy = D.fcy; L.fcz = D.fcz;
         d0 = B.tC[c]; d1 = B.tA[a]; d2 = B.tB[b];
         const float qc = d0 * d0 + d1 * d1 + d2 * d2 - B.R2f;
-        const float qb = d0 * d.fcx + d1 * d.fcy + d2 * d.fcz;
-        const float disc = qb * qb - qc * d.qa;
+        const float qb = d0 * L.fcx + d1 * L.fcy + d2 * L.fcz;
+        const float disc = qb * qb - qc * D.qa;
         const float sq = disc > 0.f ? disc * rsqrtf(disc) : 0.f;
-        q = (-qb - sq) * d.inv_qa;
-        q = q < 1e-6f ? 1e-6f : (q > 1.f ? 1.f : q);
+        float q = (-qb - sq) * D.inv_qa;
+        L.q = q < 1e-6f ? 1e-6f : (q > 1.f ? 1.f : q);
     }
-    const RT r0 = d0 + q * d.fcx, r1 = d1 + q * d.fcy, r2 = d2 + q * d.fcz;
-    const RT uw0 = UW[0] + (UW[4] * r2 - UW[5] * r1);
-    const RT uw1 = UW[1] + (UW[5] * r0 - UW[3] * r2);
-    const RT uw2 = UW[2] + (UW[3] * r1 - UW[4] * r0);
-    const RT mw = d.mw6 * ((d.fcx * uw0 + d.fcy * uw1) + d.fcz * uw2);
-    const RT A = pop_r<T, RT>(s, parity ? Pib + gx : Pi + gs);
-    RT fn;
-    if (q < RT(0.5)) {
-        if (ok2) {
-            const RT Bv = pop_r<T, RT>(s, parity ? Pib + ga : Pi + gx);
-            const RT Cv = pop_r<T, RT>(s, parity ? Pib + gb : Pi + ga);
-            fn = q * (RT(1) + RT(2) * q) * A + (RT(1) - RT(4) * q * q) * Bv + q * (RT(2) * q - RT(1)) * Cv + mw;
-        } else if (ok1) {
-            const RT Bv = pop_r<T, RT>(s, parity ? Pib + ga : Pi + gx);
-            fn = RT(2) * q * A + (RT(1) - RT(2) * q) * Bv + mw;
-        } else {
-            fn = A + mw;
-        }
-    } else {
-        if (ok2) {
-            const RT D = pop_r<T, RT>(s, parity ? Pi + gx : Pib + ga);
-            const RT E = pop_r<T, RT>(s, parity ? Pi + ga : Pib + gb);
-            if constexpr (sizeof(RT) == 8) {
-                const RT k = RT(1) / (q * (RT(2) * q + RT(1)));
-                fn = k * A + (RT(2) * q - RT(1)) / q * D - (RT(2) * q - RT(1)) / (RT(2) * q + RT(1)) * E + k * mw;
-            } else {
-                const float t = 2.f * q + 1.f, k = __fdividef(1.f, q * t), m = 2.f * q - 1.f;
-                fn = k * (A + mw) + m * (t * k) * D - m * (q * k) * E;
-            }
-        } else if (ok1) {
-            const RT D = pop_r<T, RT>(s, parity ? Pi + gx : Pib + ga);
-            if constexpr (sizeof(RT) == 8) {
-                fn = (A + mw) / (RT(2) * q) + (RT(2) * q - RT(1)) / (RT(2) * q) * D;
-            } else {
-                const float h = __fdividef(1.f, 2.f * q);
-                fn = (A + mw) * h + (2.f * q - 1.f) * h * D;
-            }
-        } else {
-            fn = A + mw;
-        }
-    }
-    put_r<T, RT>(s, const_cast<T*>(parity ? Pi + gs : Pib + gx), fn);
-    // Galilean-invariant momentum exchange
-    const RT sA = A + fn, dA = fn - A;
-    const RT p0 = d.fcx * sA + uw0 * dA, p1 = d.fcy * sA + uw1 * dA, p2 = d.fcz * sA + uw2 * dA;
-    acc[0] += p0; acc[1] += p1; acc[2] += p2;
-    acc[3] += r1 * p2 - r2 * p1;
-    acc[4] += r2 * p0 - r0 * p2;
-    acc[5] += r0 * p1 - r1 * p0;
+    L.x0 = d0 + L.q * L.fcx; L.x1 = d1 + L.q * L.fcy; L.x2 = d2 + L.q * L.fcz;
+    L.uw0 = UW[0] + (UW[4] * L.x2 - UW[5] * L.x1);
+    L.uw1 = UW[1] + (UW[5] * L.x0 - UW[3] * L.x2);
+    L.uw2 = UW[2] + (UW[3] * L.x1 - UW[4] * L.x0);
+    RT mw6;
+    if constexpr (sizeof(RT) == 8) mw6 = -6.0 * (i <= 6 ? W1 : W2);
+    else mw6 = D.mw6;
+    L.mw = mw6 * ((L.fcx * L.uw0 + L.fcy * L.uw1) + L.fcz * L.uw2);
+    const bool near = L.q < RT(0.5);
+    const T* pX = near ? (parity ? Pib + ga : Pi + gx) : (parity ? Pi + gx : Pib + ga);
+    const T* pY = near ? (parity ? Pib + gb : Pi + ga) : (parity ? Pi + ga : Pib + gb);
+    L.w = const_cast<T*>(parity ? Pi + gs : Pib + gx);
+    L.A = pop_r<T, RT>(s, parity ? Pib + gx : Pi + gs);
+    L.X = L.ok1 ? pop_r<T, RT>(s, pX) : RT(0);
+    L.Y = L.ok2 ? pop_r<T, RT>(s, pY) : RT(0);
+    return L;
 }
 
-constexpr int kIbbQueue = 64;         // link queue entries per warp
+// Interpolation, the returning population and the exchanged momentum and its
+// moment (added to acc[6]).
+template <typename T, typename RT>
+__device__ __forceinline__ void ibb_finish(const DeviceState& s, const IbbLink<T, RT>& L, RT (&acc)[6]) {
+    const RT q = L.q, A = L.A, mw = L.mw;
+    RT fn;
+    if (q < RT(0.5)) {
+        if (L.ok2) fn = q * (RT(1) + RT(2) * q) * A + (RT(1) - RT(4) * q * q) * L.X + q * (RT(2) * q - RT(1)) * L.Y + mw;
+        else if (L.ok1) fn = RT(2) * q * A + (RT(1) - RT(2) * q) * L.X + mw;
+        else fn = A + mw;
+    } else {
+        if (L.ok2) {
+            if constexpr (sizeof(RT) == 8) {
+                const RT k = RT(1) / (q * (RT(2) * q + RT(1)));
+                fn = k * A + (RT(2) * q - RT(1)) / q * L.X - (RT(2) * q - RT(1)) / (RT(2) * q + RT(1)) * L.Y + k * mw;
+            } else {
+                const float t = 2.f * q + 1.f, k = __fdividef(1.f, q * t), m = 2.f * q - 1.f;
+                fn = k * (A + mw) + m * (t * k) * L.X - m * (q * k) * L.Y;
+            }
+        } else if (L.ok1) {
+            if constexpr (sizeof(RT) == 8) {
+                fn = (A + mw) / (RT(2) * q) + (RT(2) * q - RT(1)) / (RT(2) * q) * L.X;
+            } else {
+                const float h = __fdividef(1.f, 2.f * q);
+                fn = (A + mw) * h + (2.f * q - 1.f) * h * L.X;
+            }
+        } else {
+            fn = A + mw;
+        }
+    }
+    put_r<T, RT>(s, L.w, fn);
+    // Galilean-invariant momentum exchange
+    const RT sA = A + fn, dA = fn - A;
+    const RT p0 = L.fcx * sA + L.uw0 * dA, p1 = L.fcy * sA + L.uw1 * dA, p2 = L.fcz * sA + L.uw2 * dA;
+    acc[0] += p0; acc[1] += p1; acc[2] += p2;
+    acc[3] += L.x1 * p2 - L.x2 * p1;
+    acc[4] += L.x2 * p0 - L.x0 * p2;
+    acc[5] += L.x0 * p1 - L.x1 * p0;
+}
+
+template <typename T, typename RT, typename W>
+__device__ __forceinline__ void ibb_link(const DeviceState& s, const DeviceParticles& P, int p, int parity,
+                                         const IbbBox<W>& B, uint32_t v, const RT (&UW)[6], RT (&acc)[6]) {
+    const IbbLink<T, RT> L = ibb_gather<T, RT, W>(s, P, p, parity, B, v, UW);
+    ibb_finish<T, RT>(s, L, acc);
+}
+
+// two links per lane: both gathers in flight before either finish
+template <typename T, typename RT, typename W>
+__device__ __forceinline__ void ibb_link2(const DeviceState& s, const DeviceParticles& P, int p, int parity,
+                                          const IbbBox<W>& B, uint32_t v1, uint32_t v2, const RT (&UW)[6],
+                                          RT (&acc)[6]) {
+    const IbbLink<T, RT> L1 = ibb_gather<T, RT, W>(s, P, p, parity, B, v1, UW);
+    const IbbLink<T, RT> L2 = ibb_gather<T, RT, W>(s, P, p, parity, B, v2, UW);
+    ibb_finish<T, RT>(s, L1, acc);
+    ibb_finish<T, RT>(s, L2, acc);
+}
+
+constexpr int kIbbQueue = 256;        // link queue entries per warp (a power of 2)
 
 // shared-memory plan of k_ibb for spheres of radius R with row words of
 // wbits bits; bytes == 0 when the staged rows do not fit one word
-struct IbbPlan { int S, rows_off, tab_off, queue_off, bytes; };
+struct IbbPlan { int S, own_off, fluid_off, row_off, tab_off, dir_off, list_off, queue_off, bytes; };
 __host__ __device__ inline IbbPlan ibb_plan(double R, int wbits) {
     IbbPlan pl;
     pl.S = (int)floor(2.0 * (R + 1.5)) + 3 + 4;         // staged nodes per axis, at most
-    const int wbytes = wbits / 8;
-    pl.rows_off = 0;
-    pl.tab_off = 2 * pl.S * pl.S * wbytes;
-    pl.queue_off = pl.tab_off + 7 * pl.S * 4;
+    const int SS = pl.S * pl.S, wb = wbits / 8;
+    pl.own_off = 0;
+    pl.fluid_off = pl.own_off + SS * wb;
+    pl.row_off = pl.fluid_off + SS * wb;
+    pl.tab_off = pl.row_off + SS * 4;
+    pl.dir_off = pl.tab_off + 5 * pl.S * 4;
+    pl.dir_off = (pl.dir_off + 15) & ~15;
+    pl.list_off = pl.dir_off + Q * (int)sizeof(IbbDir);
+    pl.queue_off = (pl.list_off + SS * 2 + 15) & ~15;
     pl.bytes = pl.S <= wbits ? pl.queue_off + (kPThreads / 32) * kIbbQueue * 4 : 0;
     return pl;
 }
@@ -537,6 +508,7 @@ template <typename T, typename RT, typename W>
 __global__ void __launch_bounds__(kPThreads, sizeof(RT) == 8 ? 2 : 4)
     k_ibb(DeviceState s, DeviceParticles P, int parity, IbbPlan pl) {
     extern __shared__ __align__(16) unsigned char ibb_smem[];
+    __shared__ int nact;
     const Geometry& g = s.g;
     const int p = blockIdx.x;
     const SphereGeom G = P.geom[p];
@@ -544,59 +516,74 @@ __global__ void __launch_bounds__(kPThreads, sizeof(RT) == 8 ? 2 : 4)
     const Range rx = box_g(G.ci[0], G.h[0], ext, g.NZ, false);
     const Range ry = box_g(G.ci[1], G.h[1], ext, g.NX, true);
     const Range rz = box_g(G.ci[2], G.h[2], ext, g.NY, true);
-    const int SA = ry.n + 4, SB = rz.n + 4, SC = rx.n + 4;
+    const int SA = ry.n + 4, SB = rz.n + 4, SC = rx.n + 4, S = pl.S;
     const int ya = ry.lo - 2, zb = rz.lo - 2, xc = rx.lo - 2;   // node of staged index 0
-    W* own = reinterpret_cast<W*>(ibb_smem + pl.rows_off);
-    W* fluid = own + pl.S * pl.S;
+    W* own = reinterpret_cast<W*>(ibb_smem + pl.own_off);
+    W* fluid = reinterpret_cast<W*>(ibb_smem + pl.fluid_off);
+    int* rowIdx = reinterpret_cast<int*>(ibb_smem + pl.row_off);
     float* tA = reinterpret_cast<float*>(ibb_smem + pl.tab_off);
-    float* tB = tA + pl.S;
-    float* tC = tB + pl.S;
-    int* wA = reinterpret_cast<int*>(tC + pl.S);
-    int* wB = wA + pl.S;
-    int* wC = wB + pl.S;
-    int* wZ = wC + pl.S;
+    float* tB = tA + S;
+    float* tC = tB + S;
+    int* wA = reinterpret_cast<int*>(tC + S);
+    int* wZ = wA + S;
+    IbbDir* dir = reinterpret_cast<IbbDir*>(ibb_smem + pl.dir_off);
+    uint16_t* rowlist = reinterpret_cast<uint16_t*>(ibb_smem + pl.list_off);
     uint32_t* queue = reinterpret_cast<uint32_t*>(ibb_smem + pl.queue_off);
-    const int cix = G.ci[0], ciy = G.ci[1], ciz = G.ci[2];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int NXY = g.NX * g.NY;
+    if (threadIdx.x == 0) nact = 0;
     for (int t = threadIdx.x; t < SA; t += blockDim.x) {
-        tA[t] = (float)(ya + t - ciy) + G.h[1];
+        tA[t] = (float)(ya + t - G.ci[1]) + G.h[1];
         wA[t] = wrapi(ya + t, g.NX);
     }
     for (int t = threadIdx.x; t < SB; t += blockDim.x) {
-        tB[t] = (float)(zb + t - ciz) + G.h[2];
+        tB[t] = (float)(zb + t - G.ci[2]) + G.h[2];
         wZ[t] = wrapi(zb + t, g.NY);
-        wB[t] = wZ[t] * g.NX;
     }
-    for (int t = threadIdx.x; t < SC; t += blockDim.x) {
-        tC[t] = (float)(xc + t - cix) + G.h[0];
-        wC[t] = (xc + t) * (g.NX * g.NY);
+    for (int t = threadIdx.x; t < SC; t += blockDim.x) tC[t] = (float)(xc + t - G.ci[0]) + G.h[0];
+    for (int t = threadIdx.x; t < SB * SC; t += blockDim.x) {
+        const int b = t % SB, c = t / SB;
+        rowIdx[b + S * c] = wrapi(zb + b, g.NY) * g.NX + (xc + c) * NXY;
     }
+    if (threadIdx.x < Q) {
+        const int i = threadIdx.x;
+        IbbDir d;
+        const int cx = cx_rt(i), cy = cy_rt(i), cz = cz_rt(i);
+        d.fcx = (float)cx; d.fcy = (float)cy; d.fcz = (float)cz;
+        d.mw6 = (float)(-6.0 * w_rt(i));
+        d.qa = (float)(cx * cx + cy * cy + cz * cz);
+        d.inv_qa = d.qa == 1.f ? 1.f : 0.5f;
+        d.packed = (cx + 1) | ((cy + 1) << 2) | ((cz + 1) << 4) | (opp_rt(i) << 8);
+        d.pad = 0;
+        dir[i] = d;
+    }
+    __syncthreads();                                     // the staging reads wZ
     // staging: one warp per row, lane j holds nodes a = j (and j + 32)
     {
         const int* __restrict__ owner = P.owner;
         const int nrows = SB * SC;
         const int a0 = wrapi(ya + lane, g.NX);
         const int a1 = sizeof(W) == 8 ? wrapi(ya + lane + 32, g.NX) : 0;
-        constexpr int U = 4;
+        int b = wid % SB, c = wid / SB;                  // row r = b + SB * c, r += nw
+        const int sb = nw % SB, sc = nw / SB;
+        constexpr int U = 8;                             // rows in flight per warp
         for (int r0 = wid; r0 < nrows; r0 += U * nw) {
-            int o[U][2];
+            int o[U][2], rb[U], rc[U];
 #pragma unroll
             for (int u = 0; u < U; ++u) {
-                const int r = r0 + u * nw;
+                rb[u] = b; rc[u] = c;
                 o[u][0] = o[u][1] = -3;
-                if (r < nrows) {
-                    const int b = r % SB, c = r / SB;
-                    const int ix = xc + c;
-                    if (ix >= 0 && ix < g.NZ) {
-                        const uint32_t rowbase = (uint32_t)g.NX * ((uint32_t)wrapi(zb + b, g.NY) + (uint32_t)g.NY * (uint32_t)ix);
-                        if (lane < SA) o[u][0] = __ldg(owner + rowbase + a0);
-                        if (sizeof(W) == 8 && lane + 32 < SA) o[u][1] = __ldg(owner + rowbase + a1);
-                    }
+                const int ix = xc + c;
+                if (r0 + u * nw < nrows && ix >= 0 && ix < g.NZ) {
+                    const uint32_t rowbase = (uint32_t)g.NX * (uint32_t)wZ[b] + (uint32_t)NXY * (uint32_t)ix;
+                    if (lane < SA) o[u][0] = __ldg(owner + rowbase + a0);
+                    if (sizeof(W) == 8 && lane + 32 < SA) o[u][1] = __ldg(owner + rowbase + a1);
                 }
+                b += sb; c += sc;
+                if (b >= SB) { b -= SB; ++c; }
             }
 #pragma unroll
             for (int u = 0; u < U; ++u) {
-                const int r = r0 + u * nw;
                 const unsigned po = __ballot_sync(0xffffffffu, o[u][0] == p);
                 const unsigned fo = __ballot_sync(0xffffffffu, o[u][0] == -1);
                 W pw = (W)po, fw = (W)fo;
@@ -604,17 +591,36 @@ __global__ void __launch_bounds__(kPThreads, sizeof(RT) == 8 ? 2 : 4)
                     pw |= (W)__ballot_sync(0xffffffffu, o[u][1] == p) << 32;
                     fw |= (W)__ballot_sync(0xffffffffu, o[u][1] == -1) << 32;
                 }
-                if (lane == 0 && r < nrows) {
-                    const int b = r % SB, c = r / SB;
-                    own[b + pl.S * c] = pw;
-                    fluid[b + pl.S * c] = fw;
+                if (lane == 0 && r0 + u * nw < nrows) {
+                    own[rb[u] + S * rc[u]] = pw;
+                    fluid[rb[u] + S * rc[u]] = fw;
                 }
             }
         }
     }
+    __syncthreads();
+    // rows that can hold links: (b, c) within R + 1.5 of the centre
+    {
+        const float lim = ext * ext + 0.01f;
+        const int nr = rz.n * rx.n;
+        for (int t0 = wid * 32; t0 < nr; t0 += 32 * nw) {
+            const int t = t0 + lane;
+            bool keep = false;
+            int b = 0, c = 0;
+            if (t < nr) {
+                b = 2 + t % rz.n; c = 2 + t / rz.n;
+                keep = tB[b] * tB[b] + tC[c] * tC[c] <= lim;
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, keep);
+            int base = 0;
+            if (lane == 0 && bal) base = atomicAdd(&nact, __popc(bal));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (keep) rowlist[base + __popc(bal & ((1u << lane) - 1u))] = (uint16_t)(b | (c << 8));
+        }
+    }
     IbbBox<W> Bx;
-    Bx.SB = pl.S; Bx.own = own; Bx.fluid = fluid;
-    Bx.tA = tA; Bx.tB = tB; Bx.tC = tC; Bx.wA = wA; Bx.wB = wB; Bx.wC = wC; Bx.wZ = wZ;
+    Bx.S = S; Bx.own = own; Bx.fluid = fluid; Bx.rowIdx = rowIdx;
+    Bx.tA = tA; Bx.tB = tB; Bx.tC = tC; Bx.wA = wA; Bx.wZ = wZ; Bx.dir = dir;
     Bx.xlo = xc;
     Bx.R2f = P.Rf * P.Rf;
     RT UW[6];
@@ -633,41 +639,76 @@ __global__ void __launch_bounds__(kPThreads, sizeof(RT) == 8 ? 2 : 4)
     uint32_t* q = queue + wid * kIbbQueue;
     int head = 0, tail = 0;
     __syncthreads();
-    // units (direction i, plane c), lane j on row b = j + 2 of the plane
+    // units (direction i, chunk of 32 rows); lane j on row 32 k + j
     {
         const W amask = (((W)1 << ry.n) - 1) << 2;      // candidate nodes a in [2, 2 + ry.n)
-        const int nunits = (Q - 1) * rx.n;
-        int i = 1 + wid / max(rx.n, 1), cc = wid % max(rx.n, 1);
+        const int na = nact;
+        const int nch = (na + 31) >> 5;
+        const int nunits = (Q - 1) * nch;
         for (int u = wid; u < nunits; u += nw) {
-            const int c = cc + 2, b = lane + 2;
+            const int i = 1 + u / nch, k = u - (i - 1) * nch;
+            const int rr = (k << 5) + lane;
             W m = 0;
-            if (lane < rz.n) {
-                const int cx = cx_rt(i), cy = cy_rt(i), cz = cz_rt(i);
-                m = fluid[b + pl.S * c] & shift_a(own[(b + cz) + pl.S * (c + cx)], cy) & amask;
+            int b = 0, c = 0;
+            if (rr < na) {
+                const int rc = rowlist[rr];
+                b = rc & 255; c = rc >> 8;
+                const int pk = dir[i].packed;
+                const int cx = (pk & 3) - 1, cy = ((pk >> 2) & 3) - 1, cz = ((pk >> 4) & 3) - 1;
+                m = fluid[b + S * c] & shift_a(own[(b + cz) + S * (c + cx)], cy) & amask;
             }
-            while (__any_sync(0xffffffffu, m != 0)) {
-                const bool has = m != 0;
-                int a = 0;
-                if (has) { a = lowest_bit(m); m &= m - 1; }
-                const unsigned bal = __ballot_sync(0xffffffffu, has);
-                if (has) q[(tail + __popc(bal & lt)) & (kIbbQueue - 1)] = (uint32_t)a | ((uint32_t)b << 8) | ((uint32_t)c << 16) | ((uint32_t)i << 24);
-                tail += __popc(bal);
-                if (tail - head >= 32) {
-                    __syncwarp();
-                    const uint32_t v = q[(head + lane) & (kIbbQueue - 1)];
-                    head += 32;
-                    __syncwarp();
-                    ibb_link<T, RT, W>(s, P, p, parity, Bx, v >> 24, v & 255, (v >> 8) & 255, (v >> 16) & 255, UW, acc);
+            // append the set bits of all lanes (a prefix over the lanes)
+            const int n = __popc(m);
+            int incl = n;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            const int tot = __shfl_sync(0xffffffffu, incl, 31);
+            if (tot == 0) continue;
+            if (tail - head + tot <= kIbbQueue) {
+                int pos = tail + incl - n;
+                const uint32_t hi = ((uint32_t)b << 8) | ((uint32_t)c << 16) | ((uint32_t)i << 24);
+                while (m) {
+                    q[(pos++) & (kIbbQueue - 1)] = (uint32_t)lowest_bit(m) | hi;
+                    m &= m - 1;
+                }
+                tail += tot;
+            } else {
+                // more links than the queue has room for: one bit per lane at a time
+                while (__any_sync(0xffffffffu, m != 0)) {
+                    const bool has = m != 0;
+                    int a = 0;
+                    if (has) { a = lowest_bit(m); m &= m - 1; }
+                    const unsigned bal = __ballot_sync(0xffffffffu, has);
+                    if (has) q[(tail + __popc(bal & lt)) & (kIbbQueue - 1)] = (uint32_t)a | ((uint32_t)b << 8) | ((uint32_t)c << 16) | ((uint32_t)i << 24);
+                    tail += __popc(bal);
+                    if (tail - head >= 32) {
+                        __syncwarp();
+                        const uint32_t v = q[(head + lane) & (kIbbQueue - 1)];
+                        head += 32;
+                        __syncwarp();
+                        ibb_link<T, RT, W>(s, P, p, parity, Bx, v, UW, acc);
+                    }
                 }
             }
-            cc += nw;
-            while (cc >= rx.n) { cc -= rx.n; ++i; }
+            while (tail - head >= 64) {
+                __syncwarp();
+                const uint32_t v1 = q[(head + lane) & (kIbbQueue - 1)];
+                const uint32_t v2 = q[(head + 32 + lane) & (kIbbQueue - 1)];
+                head += 64;
+                __syncwarp();
+                ibb_link2<T, RT, W>(s, P, p, parity, Bx, v1, v2, UW, acc);
+            }
         }
         __syncwarp();
-        if (lane < tail - head) {
+        if (tail - head >= 32) {
             const uint32_t v = q[(head + lane) & (kIbbQueue - 1)];
-            ibb_link<T, RT, W>(s, P, p, parity, Bx, v >> 24, v & 255, (v >> 8) & 255, (v >> 16) & 255, UW, acc);
+            head += 32;
+            ibb_link<T, RT, W>(s, P, p, parity, Bx, v, UW, acc);
         }
+        if (lane < tail - head) ibb_link<T, RT, W>(s, P, p, parity, Bx, q[(head + lane) & (kIbbQueue - 1)], UW, acc);
     }
     // per-sphere FP64 reduction: warp shuffles, then across warps
     __shared__ double sh[6][kPThreads / 32];
@@ -869,6 +910,63 @@ __global__ void __launch_bounds__(32 * kRepWarps) k_repulsion_cells(DevicePartic
     rep[0] = __dadd_rn(rep[0], repulse(hl, P.zeta, P.stf0_w, P.stf1_w));
     rep[0] = __dsub_rn(rep[0], repulse(hu, P.zeta, P.stf0_w, P.stf1_w));
     P.rep[3 * s] = rep[0]; P.rep[3 * s + 1] = rep[1]; P.rep[3 * s + 2] = rep[2];
+}
+
+// Nodes released at this step that lie inside another sphere (overlapping
+// spheres) are claimed by the highest-index sphere containing them, as the
+// oracle's claim of every inside node does.  The candidates come from the
+// cell list binned before the update (a centre moves less than two nodes per
+// step, within one cell), or from all spheres when there is no cell list or a
+// bin overflowed.
+__global__ void k_reclaim(DeviceParticles P, Geometry g, int* owner) {
+    const unsigned cnt = min(P.counters[0], (unsigned)P.refill_cap);
+    const bool all = P.ncell == 0 || *(volatile unsigned*)&P.counters[2] != 0;
+    const float R2 = P.Rf * P.Rf, band = in_band(R2), reach2 = (P.Rf + 0.1f) * (P.Rf + 0.1f);
+    for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x) {
+        const uint32_t n = P.refill_node[k];
+        const int iy = (int)(n % (uint32_t)g.NX);
+        const int iz = (int)((n / (uint32_t)g.NX) % (uint32_t)g.NY);
+        const int ix = (int)(n / g.NXY);
+        int best = -1;
+        auto test = [&](int t) {
+            if (t <= best) return;
+            const SphereGeom G = P.geom[t];
+            int dy = iy - G.ci[1], dz = iz - G.ci[2];             // periodic image first, in integers
+            dy = dy > g.NX / 2 ? dy - g.NX : (dy < -(g.NX / 2) ? dy + g.NX : dy);
+            dz = dz > g.NY / 2 ? dz - g.NY : (dz < -(g.NY / 2) ? dz + g.NY : dz);
+            const float ox = (float)(ix - G.ci[0]) + G.h[0];
+            const float oy = (float)dy + G.h[1];
+            const float oz = (float)dz + G.h[2];
+            const float r2 = ox * ox + oy * oy + oz * oz;
+            if (r2 > reach2) return;
+            bool in;
+            if (r2 < R2 - band) in = true;
+            else if (r2 > R2 + band) in = false;
+            else {
+                double d[3];
+                offset(P, g, t, ix, iy, iz, d);
+                in = inside(d, P.R);
+            }
+            if (in) best = t;
+        };
+        if (all) {
+            for (int t = 0; t < P.npart; ++t) test(t);
+        } else {
+            const int cx = min(P.cell_nx - 1, (int)((ix + 0.5) * P.cell_nx / g.NZ));
+            const int cy = min(P.cell_ny - 1, (int)((iy + 0.5) * P.cell_ny / g.NX));
+            const int cz = min(P.cell_nz - 1, (int)((iz + 0.5) * P.cell_nz / g.NY));
+            for (int k3 = 0; k3 < 27; ++k3) {
+                const int nx = cx + k3 % 3 - 1;
+                if (nx < 0 || nx >= P.cell_nx) continue;
+                const int ny = (cy + (k3 / 3) % 3 - 1 + P.cell_ny) % P.cell_ny;
+                const int nz = (cz + k3 / 9 - 1 + P.cell_nz) % P.cell_nz;
+                const int cell = nx + P.cell_nx * (ny + P.cell_ny * nz);
+                const int m = min(P.cell_count[cell], kCellCap);
+                for (int j = 0; j < m; ++j) test(P.cell_list[(size_t)cell * kCellCap + j]);
+            }
+        }
+        if (best >= 0) atomicMax(owner + n, best);
+    }
 }
 
 // Geometry record of sphere s from its FP64 state; delta: displacement of
@@ -1078,6 +1176,7 @@ cudaError_t particles_after_step(const DeviceState& s, const DeviceParticles& P,
     k_newton<<<(P.npart + 127) / 128, 128, 0, st>>>(P, s.g, s.cd.Fx, s.cd.Fy, s.cd.Fz, have_prev);
     k_shell<false><<<(P.npart + kShellWarps - 1) / kShellWarps, 32 * kShellWarps, 0, st>>>(P, s.g, P.owner, 0);
     k_shell<true><<<(P.npart + kShellWarps - 1) / kShellWarps, 32 * kShellWarps, 0, st>>>(P, s.g, P.owner, 0);
+    k_reclaim<<<std::max(1, 2 * s.sm_count), 256, 0, st>>>(P, s.g, P.owner);
     // refills: a few per sphere and step; a grid of 4 CTAs per SM strides the list
     const unsigned nb = (unsigned)std::min<long long>((P.refill_cap + 255) / 256, 4LL * std::max(s.sm_count, 1));
     switch (s.prec) {

@@ -16,6 +16,7 @@
 //   nx ny nz          lattice, reference axes (wall-normal, streamwise, spanwise)
 //   visc ustar h      viscosity, friction velocity, half height (force = ustar^2/h)
 //   mrt               MRT rate set 1/2/3 (para.f90:110-141)
+//   s16               rate of the third-order odd moments, overriding the set
 //   precision         fp64 | fp32 | fp16
 //   steps ndiag nstat main-loop length and output cadence
 //   uc amp seed       initial Poiseuille centreline, noise amplitude, seed
@@ -111,6 +112,7 @@ int main(int argc, char** argv) {
 
     lbm_params p;
     check(lbm_params_init(&p, nx, ny, nz, mrt, visc, force, prec), "lbm_params_init");
+    if (g_args.count("s16")) p.s16 = argd("s16", p.s16);
     lbm_ctx* ctx = nullptr;
     check(lbm_create(&p, &ctx), "lbm_create");
 

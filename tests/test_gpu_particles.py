@@ -99,6 +99,32 @@ def test_repulsion_cell_list_matches_oracle(pkg, orc):
     assert rel(free.vel[:5], sp.vel[:5]) > 1e-3
 
 
+def test_overlapping_spheres_ownership_matches_oracle(pkg, orc):
+    """Two overlapping spheres driven apart: nodes in the overlap belong to the
+    higher index, and the nodes that sphere 1 leaves inside sphere 0 are
+    claimed by sphere 0 (the oracle claims every inside node in index
+    order)."""
+    shape = (24, 48, 40)
+    pos = np.array([[12.0, 20.0, 20.0], [12.3, 25.0, 20.5], [12.0, 38.0, 8.0]])
+    vel = np.array([[0.0, -0.06, 0.0], [0.0, 0.06, 0.0], [0.0, 0.0, 0.0]])
+    run, f0 = channel_with_spheres(orc, pkg, shape, pos)
+    sp = orc.Spheres(pos, radius=4.0, rho_ratio=1e6, vel=vel)
+    fo, owner, links, refills = orc.particle_run(orc.params_from(run), sp, f0, 30)
+    assert sum(refills) > 0
+    with pkg.Lattice(run) as lat:
+        lat.upload_f(f0)
+        lat.set_particles(pos, radius=4.0, rho_ratio=1e6, vel=vel)
+        lat.step(30)
+        g = lat.download_f()
+        st = lat.particles()
+        nsolid, nlinks, _ = lat.particle_counts()
+        rho, _, _, _ = lat.macrovar()
+    assert nsolid == int((owner >= 0).sum()) and nlinks == links[-1]
+    assert rel(g, fo) < 1e-10
+    for k in ("pos", "vel", "omg", "force", "torque"):
+        assert rel(st[k], getattr(sp, k)) < 1e-10, k
+
+
 def test_particle_diagnostics_mask_solid_nodes(pkg, orc):
     shape = (24, 32, 22)
     run, f0 = channel_with_spheres(orc, pkg, shape, POS)
