@@ -38,6 +38,7 @@ PRECISIONS = {"fp64": PREC_FP64, "fp32": PREC_FP32, "fp16": PREC_FP16}
 MRT_STABLE, MRT_LBGK, MRT_LOWDISS = 1, 2, 3
 PROFILE_COLS = 12
 FLAG_SIMPLE_STEP = 1
+PFLAG_Q_FP64 = 1
 PROFILE_NAMES = ("ux", "uy", "uz", "uxuz", "uxuy", "uyuz", "uxux", "uyuy", "uzuz", "rho", "rhorho", "count")
 
 # Every symbol include/lbm_gb300.h declares.

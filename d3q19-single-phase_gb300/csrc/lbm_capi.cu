@@ -859,6 +859,7 @@ int lbm_particles_set(lbm_ctx* c, const lbm_particle_params* pp, const double* p
     P.npart = n;
     P.R = pp->radius; P.rho_ratio = pp->rho_ratio;
     P.Rf = (float)pp->radius;
+    P.q_fp64 = (pp->flags & LBM_PFLAG_Q_FP64) ? 1 : 0;
     P.stf0 = pp->stf0; P.stf1 = pp->stf1; P.stf0_w = pp->stf0_w; P.stf1_w = pp->stf1_w; P.zeta = pp->zeta;
     c->pp = *pp;
     c->have_prev = 0;

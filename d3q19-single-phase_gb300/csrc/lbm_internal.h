@@ -56,6 +56,7 @@ struct DeviceParticles {
     double *rep;                      // repulsion of the current step
     double *pos_prev;                 // centre before the last Newton-Euler update
     SphereGeom* geom;                 // [npart]
+    int q_fp64;                       // FP64 link fractions for FP32/FP16 storage
     float Rf;                         // radius in FP32
     int* owner;                       // per node: sphere id, -1 fluid, -2 pending refill
     uint32_t* refill_node;

@@ -371,7 +371,7 @@ struct IbbLink {
 // node and the direction.  X and Y are the interpolation partners: (B, C) at
 // x_f, x_f - c_i in direction i for q < 1/2, (D, E) at x_f - c_i, x_f - 2c_i
 // in direction opp(i) otherwise.
-template <typename T, typename RT, typename W>
+template <typename T, typename RT, typename W, bool Q64>
 __device__ __forceinline__ IbbLink<T, RT> ibb_gather(const DeviceState& s, const DeviceParticles& P, int p,
                                                      int parity, const IbbBox<W>& B, uint32_t v, const RT (&UW)[6]) {
     IbbLink<T, RT> L;
@@ -400,12 +400,18 @@ __device__ __forceinline__ IbbLink<T, RT> ibb_gather(const DeviceState& s, const
     } else {
         L.fcx = D.fcx; L.fcy = D.fcy; L.fcz = D.fcz;
         d0 = B.tC[c]; d1 = B.tA[a]; d2 = B.tB[b];
-        const float qc = d0 * d0 + d1 * d1 + d2 * d2 - B.R2f;
-        const float qb = d0 * L.fcx + d1 * L.fcy + d2 * L.fcz;
-        const float disc = qb * qb - qc * D.qa;
-        const float sq = disc > 0.f ? disc * rsqrtf(disc) : 0.f;
-        float q = (-qb - sq) * D.inv_qa;
-        L.q = q < 1e-6f ? 1e-6f : (q > 1.f ? 1.f : q);
+        if constexpr (Q64) {
+            double dd[3];
+            offset(P, s.g, p, B.xlo + c, B.wA[a], B.wZ[b], dd);
+            L.q = (float)link_q<double>(dd, cx, cy, cz, __dsub_rn(norm2_rn(dd), __dmul_rn(P.R, P.R)));
+        } else {
+            const float qc = d0 * d0 + d1 * d1 + d2 * d2 - B.R2f;
+            const float qb = d0 * L.fcx + d1 * L.fcy + d2 * L.fcz;
+            const float disc = qb * qb - qc * D.qa;
+            const float sq = disc > 0.f ? disc * rsqrtf(disc) : 0.f;
+            float q = (-qb - sq) * D.inv_qa;
+            L.q = q < 1e-6f ? 1e-6f : (q > 1.f ? 1.f : q);
+        }
     }
     L.x0 = d0 + L.q * L.fcx; L.x1 = d1 + L.q * L.fcy; L.x2 = d2 + L.q * L.fcz;
     L.uw0 = UW[0] + (UW[4] * L.x2 - UW[5] * L.x1);
@@ -465,20 +471,20 @@ __device__ __forceinline__ void ibb_finish(const DeviceState& s, const IbbLink<T
     acc[5] += L.x0 * p1 - L.x1 * p0;
 }
 
-template <typename T, typename RT, typename W>
+template <typename T, typename RT, typename W, bool Q64>
 __device__ __forceinline__ void ibb_link(const DeviceState& s, const DeviceParticles& P, int p, int parity,
                                          const IbbBox<W>& B, uint32_t v, const RT (&UW)[6], RT (&acc)[6]) {
-    const IbbLink<T, RT> L = ibb_gather<T, RT, W>(s, P, p, parity, B, v, UW);
+    const IbbLink<T, RT> L = ibb_gather<T, RT, W, Q64>(s, P, p, parity, B, v, UW);
     ibb_finish<T, RT>(s, L, acc);
 }
 
 // two links per lane: both gathers in flight before either finish
-template <typename T, typename RT, typename W>
+template <typename T, typename RT, typename W, bool Q64>
 __device__ __forceinline__ void ibb_link2(const DeviceState& s, const DeviceParticles& P, int p, int parity,
                                           const IbbBox<W>& B, uint32_t v1, uint32_t v2, const RT (&UW)[6],
                                           RT (&acc)[6]) {
-    const IbbLink<T, RT> L1 = ibb_gather<T, RT, W>(s, P, p, parity, B, v1, UW);
-    const IbbLink<T, RT> L2 = ibb_gather<T, RT, W>(s, P, p, parity, B, v2, UW);
+    const IbbLink<T, RT> L1 = ibb_gather<T, RT, W, Q64>(s, P, p, parity, B, v1, UW);
+    const IbbLink<T, RT> L2 = ibb_gather<T, RT, W, Q64>(s, P, p, parity, B, v2, UW);
     ibb_finish<T, RT>(s, L1, acc);
     ibb_finish<T, RT>(s, L2, acc);
 }
@@ -504,7 +510,7 @@ __host__ __device__ inline IbbPlan ibb_plan(double R, int wbits) {
     return pl;
 }
 
-template <typename T, typename RT, typename W>
+template <typename T, typename RT, typename W, bool Q64>
 __global__ void __launch_bounds__(kPThreads, sizeof(RT) == 8 ? 2 : 4)
     k_ibb(DeviceState s, DeviceParticles P, int parity, IbbPlan pl) {
     extern __shared__ __align__(16) unsigned char ibb_smem[];
@@ -689,7 +695,7 @@ __global__ void __launch_bounds__(kPThreads, sizeof(RT) == 8 ? 2 : 4)
                         const uint32_t v = q[(head + lane) & (kIbbQueue - 1)];
                         head += 32;
                         __syncwarp();
-                        ibb_link<T, RT, W>(s, P, p, parity, Bx, v, UW, acc);
+                        ibb_link<T, RT, W, Q64>(s, P, p, parity, Bx, v, UW, acc);
                     }
                 }
             }
@@ -699,16 +705,16 @@ __global__ void __launch_bounds__(kPThreads, sizeof(RT) == 8 ? 2 : 4)
                 const uint32_t v2 = q[(head + 32 + lane) & (kIbbQueue - 1)];
                 head += 64;
                 __syncwarp();
-                ibb_link2<T, RT, W>(s, P, p, parity, Bx, v1, v2, UW, acc);
+                ibb_link2<T, RT, W, Q64>(s, P, p, parity, Bx, v1, v2, UW, acc);
             }
         }
         __syncwarp();
         if (tail - head >= 32) {
             const uint32_t v = q[(head + lane) & (kIbbQueue - 1)];
             head += 32;
-            ibb_link<T, RT, W>(s, P, p, parity, Bx, v, UW, acc);
+            ibb_link<T, RT, W, Q64>(s, P, p, parity, Bx, v, UW, acc);
         }
-        if (lane < tail - head) ibb_link<T, RT, W>(s, P, p, parity, Bx, q[(head + lane) & (kIbbQueue - 1)], UW, acc);
+        if (lane < tail - head) ibb_link<T, RT, W, Q64>(s, P, p, parity, Bx, q[(head + lane) & (kIbbQueue - 1)], UW, acc);
     }
     // per-sphere FP64 reduction: warp shuffles, then across warps
     __shared__ double sh[6][kPThreads / 32];
@@ -734,14 +740,20 @@ __global__ void __launch_bounds__(kPThreads, sizeof(RT) == 8 ? 2 : 4)
     }
 }
 
-template <typename T, typename RT, typename W>
-cudaError_t launch_ibb(const DeviceState& s, const DeviceParticles& P, int parity, size_t smem, cudaStream_t st) {
+template <typename T, typename RT, typename W, bool Q64>
+cudaError_t launch_ibb_q(const DeviceState& s, const DeviceParticles& P, int parity, size_t smem, cudaStream_t st) {
     if (smem > 48 * 1024) {
-        const cudaError_t e = cudaFuncSetAttribute(k_ibb<T, RT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        const cudaError_t e = cudaFuncSetAttribute(k_ibb<T, RT, W, Q64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    k_ibb<T, RT, W><<<P.npart, kPThreads, smem, st>>>(s, P, parity, ibb_plan(P.R, 8 * (int)sizeof(W)));
+    k_ibb<T, RT, W, Q64><<<P.npart, kPThreads, smem, st>>>(s, P, parity, ibb_plan(P.R, 8 * (int)sizeof(W)));
     return cudaGetLastError();
+}
+template <typename T, typename RT, typename W>
+cudaError_t launch_ibb(const DeviceState& s, const DeviceParticles& P, int parity, size_t smem, cudaStream_t st) {
+    // FP64 storage computes q in FP64 anyway
+    if (sizeof(RT) == 4 && P.q_fp64) return launch_ibb_q<T, RT, W, true>(s, P, parity, smem, st);
+    return launch_ibb_q<T, RT, W, false>(s, P, parity, smem, st);
 }
 
 size_t ibb_smem_bytes(double R) {

@@ -245,13 +245,19 @@ int lbm_load_flow(lbm_ctx* ctx, const char* path, int32_t kind,
  * (ix,iy,iz) (1-based) at (ix-1/2, iy-1/2, iz-1/2), as in macrovar. */
 typedef struct lbm_particle_params {
     int32_t npart;            /* number of spheres (npart, var_inc.f90:66)     */
-    int32_t flags;            /* reserved, 0                                   */
+    int32_t flags;            /* LBM_PFLAG_* bits                              */
     double  radius;           /* rad (var_inc.f90:67)                          */
     double  rho_ratio;        /* rhopart / rho0                                */
     double  stf0, stf1;       /* sphere-sphere repulsion (para.f90:357-358)    */
     double  stf0_w, stf1_w;   /* sphere-wall repulsion (para.f90:359-360)      */
     double  zeta;             /* repulsion range, lattice units                */
 } lbm_particle_params;
+
+/* lbm_particle_params.flags: compute the boundary-link fractions q in FP64
+ * for FP32/FP16 storage too (default: FP32 from the FP64 centre split into an
+ * exact integer part and an FP32 fraction, |dq| < 1e-5; FP64 q costs about
+ * 20 FP64 operations per link at GB300's 1/64 FP64 rate). */
+#define LBM_PFLAG_Q_FP64 1
 
 /* Defaults of para.f90:339-379 for npart spheres of the given radius. */
 int lbm_particle_params_init(lbm_particle_params* pp, int32_t npart, double radius,

@@ -125,6 +125,27 @@ def test_overlapping_spheres_ownership_matches_oracle(pkg, orc):
         assert rel(st[k], getattr(sp, k)) < 1e-10, k
 
 
+@pytest.mark.parametrize("prec", ["fp32", "fp16"])
+def test_fp64_link_fractions_option(pkg, orc, prec):
+    """LBM_PFLAG_Q_FP64: the FP32 link fractions (exact integer offsets plus an
+    FP32 fraction) and FP64 ones give the same run to within the storage
+    rounding, and both follow the FP64 path."""
+    shape = (32, 64, 32)
+    pos = pkg.place_spheres(*shape, 6, 4.0, gap=2.0, wall_gap=1.0, seed=13)
+    res = {}
+    for tag, p, flags in (("ref", "fp64", 0), ("q32", prec, 0), ("q64", prec, pkg.PFLAG_Q_FP64)):
+        run, f0 = channel_with_spheres(orc, pkg, shape, pos, force=1e-5, precision=p)
+        with pkg.Lattice(run) as lat:
+            lat.upload_f(f0)
+            lat.set_particles(pos, radius=4.0, rho_ratio=2.0, flags=flags)
+            lat.step(40)
+            res[tag] = lat.particles()
+    tol = 1e-4 if prec == "fp32" else 3e-2
+    for tag in ("q32", "q64"):
+        assert rel(res[tag]["force"], res["ref"]["force"]) < tol, tag
+    assert rel(res["q32"]["force"], res["q64"]["force"]) < tol
+
+
 def test_particle_diagnostics_mask_solid_nodes(pkg, orc):
     shape = (24, 32, 22)
     run, f0 = channel_with_spheres(orc, pkg, shape, POS)
