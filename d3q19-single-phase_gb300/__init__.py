@@ -49,7 +49,9 @@ EXPORTS = (
     "lbm_step_count", "lbm_prerelax", "lbm_macrovar", "lbm_diag", "lbm_profiles", "lbm_avedensity",
     "lbm_save_flow", "lbm_load_flow", "lbm_profiles_noalloc", "lbm_particle_params_init",
     "lbm_particles_place", "lbm_particles_set", "lbm_particles_get", "lbm_particle_counts",
-    "lbm_timing_enable", "lbm_timing_get",
+    "lbm_timing_enable", "lbm_timing_get", "lbm_strain",
+    "lbm_mlp_create", "lbm_mlp_destroy", "lbm_mlp_get", "lbm_mlp_set", "lbm_mlp_set_data", "lbm_mlp_train",
+    "lbm_mlp_gradient", "lbm_mlp_predict",
 )
 
 
@@ -107,6 +109,7 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
         raise RuntimeError(f"{p} is missing: build it with __graft_entry__.build() (needs nvcc)")
     lib = ctypes.CDLL(str(p))
     dp = ctypes.POINTER(ctypes.c_double)
+    fp = ctypes.POINTER(ctypes.c_float)
     ctx = ctypes.c_void_p
     sig = {
         "lbm_strerror": (ctypes.c_char_p, [ctypes.c_int]),
@@ -132,6 +135,15 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
         "lbm_prerelax": (ctypes.c_int, [ctx, dp, dp, dp, ctypes.c_double, ctypes.c_int32,
                                         ctypes.POINTER(ctypes.c_int32), dp]),
         "lbm_macrovar": (ctypes.c_int, [ctx, dp, dp, dp, dp]),
+        "lbm_strain": (ctypes.c_int, [ctx, dp, dp]),
+        "lbm_mlp_create": (ctypes.c_int, [ctypes.POINTER(ctx), ctypes.c_uint64, ctypes.c_int32]),
+        "lbm_mlp_destroy": (ctypes.c_int, [ctx]),
+        "lbm_mlp_get": (ctypes.c_int, [ctx, fp, fp]),
+        "lbm_mlp_set": (ctypes.c_int, [ctx, fp, fp]),
+        "lbm_mlp_set_data": (ctypes.c_int, [ctx, fp, fp, ctypes.c_int64, ctypes.c_int32]),
+        "lbm_mlp_train": (ctypes.c_int, [ctx, ctypes.c_int32, ctypes.c_int32, ctypes.c_float, ctypes.c_int32, fp]),
+        "lbm_mlp_gradient": (ctypes.c_int, [ctx, ctypes.c_int32, ctypes.POINTER(ctypes.c_double), fp]),
+        "lbm_mlp_predict": (ctypes.c_int, [ctx, fp, ctypes.c_int64, fp]),
         "lbm_diag": (ctypes.c_int, [ctx, ctypes.POINTER(LBMStats)]),
         "lbm_profiles": (ctypes.c_int, [ctx, dp]),
         "lbm_profiles_noalloc": (ctypes.c_int, [ctx, dp]),
@@ -170,6 +182,82 @@ def _dptr(a: np.ndarray | None):
     if a is None:
         return None
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _fptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+MLP_IN, MLP_PARAMS, MLP_NORM = 7, 1345, 14
+MLP_FP32 = 1
+
+
+class ClosureNet:
+    """The learned LES closure's eddy-viscosity network (``lbm_mlp_*``):
+    7 features -> 32 -> 32 -> nu_t / nu, trained on the GPU."""
+
+    def __init__(self, seed: int = 0, device: int = 0):
+        self.lib = load_library()
+        self._m = ctypes.c_void_p()
+        _check(self.lib, self.lib.lbm_mlp_create(ctypes.byref(self._m), seed, device), "lbm_mlp_create")
+
+    def close(self) -> None:
+        if self._m:
+            self.lib.lbm_mlp_destroy(self._m)
+            self._m = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _call(self, name, *args):
+        _check(self.lib, getattr(self.lib, name)(self._m, *args), name)
+
+    def get(self) -> tuple[np.ndarray, np.ndarray]:
+        p = np.empty(MLP_PARAMS, dtype=np.float32)
+        n = np.empty(MLP_NORM, dtype=np.float32)
+        self._call("lbm_mlp_get", _fptr(p), _fptr(n))
+        return p, n
+
+    def set(self, params=None, norm=None) -> None:
+        p = None if params is None else np.ascontiguousarray(params, dtype=np.float32).reshape(MLP_PARAMS)
+        n = None if norm is None else np.ascontiguousarray(norm, dtype=np.float32).reshape(MLP_NORM)
+        self._call("lbm_mlp_set", _fptr(p), _fptr(n))
+
+    def set_data(self, X, y, set_norm: bool = True) -> None:
+        X = np.ascontiguousarray(X, dtype=np.float32).reshape(-1, MLP_IN)
+        y = np.ascontiguousarray(y, dtype=np.float32).reshape(-1)
+        if len(X) != len(y):
+            raise ValueError("X and y differ in length")
+        self._data = (X, y)
+        self._call("lbm_mlp_set_data", _fptr(X), _fptr(y), len(X), int(set_norm))
+
+    def train(self, steps: int, batch: int = 65536, lr: float = 1e-3, fp32: bool = False) -> np.ndarray:
+        losses = np.empty(max(steps, 1), dtype=np.float32)
+        self._call("lbm_mlp_train", steps, batch, lr, MLP_FP32 if fp32 else 0, _fptr(losses))
+        return losses[:steps]
+
+    def gradient(self, fp32: bool = False) -> tuple[float, np.ndarray]:
+        loss = ctypes.c_double()
+        g = np.empty(MLP_PARAMS, dtype=np.float32)
+        self._call("lbm_mlp_gradient", MLP_FP32 if fp32 else 0, ctypes.byref(loss), _fptr(g))
+        return loss.value, g
+
+    def predict(self, X) -> np.ndarray:
+        X = np.ascontiguousarray(X, dtype=np.float32).reshape(-1, MLP_IN)
+        out = np.empty(len(X), dtype=np.float32)
+        self._call("lbm_mlp_predict", _fptr(X), len(X), _fptr(out))
+        return out
 
 
 # --------------------------------------------------------------------------
@@ -407,6 +495,12 @@ class Lattice:
         outs = [np.empty(self.shape, dtype=np.float64, order="F") for _ in range(4)]
         self._call("lbm_macrovar", *map(_dptr, outs))
         return tuple(outs)
+
+    def strain(self) -> tuple[np.ndarray, np.ndarray]:
+        """S_ij S_ij per node by the two methods of sijstat01 (moments, populations)."""
+        outs = [np.empty(self.shape, dtype=np.float64, order="F") for _ in range(2)]
+        self._call("lbm_strain", *map(_dptr, outs))
+        return outs[0], outs[1]
 
     def diag(self) -> LBMStats:
         st = LBMStats()

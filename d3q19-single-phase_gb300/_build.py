@@ -27,7 +27,8 @@ NVCC_FLAGS = [
     "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
     "--expt-relaxed-constexpr",
 ]
-SOURCES = ["lbm_step.cu", "lbm_step_tma.cu", "lbm_fields.cu", "lbm_particles.cu", "lbm_capi.cu", "lbm_noalloc.cu"]
+SOURCES = ["lbm_step.cu", "lbm_step_tma.cu", "lbm_fields.cu", "lbm_particles.cu", "lbm_capi.cu", "lbm_noalloc.cu",
+           "lbm_mlp.cu"]
 
 
 def nvcc() -> str:

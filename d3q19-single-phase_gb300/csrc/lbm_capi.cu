@@ -578,6 +578,24 @@ int lbm_macrovar(lbm_ctx* c, double* rho, double* ux, double* uy, double* uz) {
     return sync(c);
 }
 
+int lbm_strain(lbm_ctx* c, double* m1, double* m2) {
+    if (check_ctx(c)) return LBM_ERR_INVALID_ARG;
+    if (!m1 && !m2) return LBM_OK;
+    if (int rc = set_device(c)) return rc;
+    const int k = chunk_planes(c, 2);
+    const size_t pp = plane_nodes(c->p);
+    for (int z0 = 0; z0 < c->p.nz; z0 += k) {
+        const int nzc = std::min(k, c->p.nz - z0);
+        const size_t n = (size_t)nzc * pp;
+        double* d1 = m1 ? c->d_stage : nullptr;
+        double* d2 = m2 ? c->d_stage + n : nullptr;
+        CK(launch_strain(c->s, c->parity, d1, d2, z0, nzc, c->stream));
+        if (m1) CK(cudaMemcpyAsync(m1 + (size_t)z0 * pp, d1, n * 8, cudaMemcpyDeviceToHost, c->stream));
+        if (m2) CK(cudaMemcpyAsync(m2 + (size_t)z0 * pp, d2, n * 8, cudaMemcpyDeviceToHost, c->stream));
+    }
+    return sync(c);
+}
+
 int lbm_profiles(lbm_ctx* c, double* out) {
     if (check_ctx(c) || !out) return fail(LBM_ERR_INVALID_ARG, "null argument");
     if (int rc = set_device(c)) return rc;

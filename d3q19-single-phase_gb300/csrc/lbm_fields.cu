@@ -2,6 +2,7 @@
 // f(0:18,nx,ny,nz) and the device SoA storage, equilibrium initialisation,
 // macroscopic fields and FP64 reductions for the diagnostics.
 #include "lbm_internal.h"
+#include "lbm_strain.cuh"
 
 namespace lbm {
 
@@ -231,6 +232,53 @@ __global__ void k_macro(DeviceState s, int parity, double* rho, double* ux, doub
     if (uz) uz[o] = c;
 }
 
+// Strain rate from the non-equilibrium part of the populations, the two ways
+// of sijstat01 (saveload.f90:2320-2432), FP64 per node, natural orientation,
+// reference axes (x wall-normal):
+//  method 1 (moment space, Yu et al. 2006, Appendix; saveload.f90:2322-2380):
+//    the non-equilibrium parts of e, 3p_xx, p_ww, p_xy, p_yz, p_xz scaled by
+//    the rates that relax them (s1, s9) give S_ij directly;
+//  method 2 (population space, saveload.f90:2385-2432): S_ab =
+//    (3 / 2 tau) sum_i c_ia c_ib (f_i - f_i^eq) with the incompressible
+//    equilibrium of initial.f90:26-44.
+// Outputs S_ij S_ij of both; solid nodes give 0 (the reference masks them).
+template <typename T>
+__global__ void k_strain(DeviceState s, int parity, double* __restrict__ m1, double* __restrict__ m2, int z0) {
+    const RefNode r = ref_node(s.g, z0);
+    if (!r.ok) return;
+    const size_t o = ref_lin(s.g, r.ix, r.iy, r.iz - z0);
+    const int own = s.owner ? s.owner[gpu_lin(s.g, r.ix, r.iy, r.iz)] : -1;
+    if (own >= 0) {
+        if (m1) m1[o] = 0.0;
+        if (m2) m2[o] = 0.0;
+        return;
+    }
+    double f[Q];
+    gather_natural<T>(s, parity, r.iy, r.iz, r.ix, f);
+    const double F[3] = {(double)s.cd.Fx, (double)s.cd.Fy, (double)s.cd.Fz};
+    double rho, ux, uy, uz;
+    macro_of<double>(f, F, rho, ux, uy, uz);
+    const double s1 = (double)s.cd.ke * 2394.0, s9 = (double)s.cd.kp * 36.0;
+    if (m1) {
+        double S6[6];
+        strain_from_moments(f, rho, ux, uy, uz, s1, s9, S6);
+        m1[o] = S6[0] * S6[0] + S6[1] * S6[1] + S6[2] * S6[2] + 2.0 * (S6[3] * S6[3] + S6[4] * S6[4] + S6[5] * S6[5]);
+    }
+    if (m2) {
+        const double usq = 1.5 * (ux * ux + uy * uy + uz * uz);
+        double a[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+        for (int i = 1; i < Q; ++i) {
+            const double cu = CXf(i) * ux + CYf(i) * uy + CZf(i) * uz;
+            const double fn = f[i] - weight(i) * (rho + 3.0 * cu + 4.5 * cu * cu - usq);
+            a[0] += fn * (CXf(i) * CXf(i)); a[1] += fn * (CYf(i) * CYf(i)); a[2] += fn * (CZf(i) * CZf(i));
+            a[3] += fn * (CXf(i) * CYf(i)); a[4] += fn * (CYf(i) * CZf(i)); a[5] += fn * (CZf(i) * CXf(i));
+        }
+        const double k = 1.5 * s9;                       // 1.5 / tau
+        m2[o] = (a[0] * a[0] + a[1] * a[1] + a[2] * a[2] + 2.0 * (a[3] * a[3] + a[4] * a[4] + a[5] * a[5])) * k * k;
+    }
+}
+
 __global__ void k_ref_to_gpu_vec(Geometry g, size_t N, const double* __restrict__ ux,
                                  const double* __restrict__ uy, const double* __restrict__ uz,
                                  double* __restrict__ uf, int z0) {
@@ -401,6 +449,11 @@ cudaError_t launch_init_channel(const DeviceState& s, double uc, double amp, uin
 cudaError_t launch_macro(const DeviceState& s, int parity, double* rho, double* ux, double* uy,
                          double* uz, int z0, int nzc, cudaStream_t st) {
     LBM_DISPATCH(s.prec, (k_macro<T><<<ref_grid(s.g, nzc, kBx), kBx, 0, st>>>(s, parity, rho, ux, uy, uz, z0)))
+}
+
+cudaError_t launch_strain(const DeviceState& s, int parity, double* m1, double* m2, int z0, int nzc,
+                          cudaStream_t st) {
+    LBM_DISPATCH(s.prec, (k_strain<T><<<ref_grid(s.g, nzc, kBx), kBx, 0, st>>>(s, parity, m1, m2, z0)))
 }
 
 cudaError_t launch_ref_to_gpu_vec(const DeviceState& s, const double* ux, const double* uy,

@@ -115,6 +115,8 @@ cudaError_t launch_macro(const DeviceState& s, int parity, double* rho,
                          double* ux, double* uy, double* uz, int z0, int nzc,
                          cudaStream_t st);
 // velocity (nx*ny*nz*3 doubles, reference layout chunk) to GPU-layout frozen u
+cudaError_t launch_strain(const DeviceState& s, int parity, double* m1, double* m2, int z0, int nzc,
+                          cudaStream_t st);
 cudaError_t launch_ref_to_gpu_vec(const DeviceState& s, const double* ux,
                                   const double* uy, const double* uz,
                                   double* uf, int z0, int nzc, cudaStream_t st);

@@ -1,0 +1,61 @@
+// The per-node eddy-viscosity network of the learned LES closure:
+// 7 inputs -> 32 -> 32 -> 1, SiLU hidden layers, softplus output (nu_t / nu
+// >= 0).  Shared by the training kernels (lbm_mlp.cu) and the LES collision
+// that evaluates it per node with the weights in shared memory.
+//
+// Parameter vector (FP32, kMlpParams floats): W1[7][32] (row = input), b1[32],
+// W2[32][32] (row = input), b2[32], w3[32], b3.  Inputs are standardised with
+// a per-feature mean and inverse standard deviation (norm[0..6], norm[7..13])
+// before the first layer.
+#pragma once
+
+#include <cmath>
+
+namespace lbm {
+
+constexpr int kMlpIn = 7;
+constexpr int kMlpH = 32;
+constexpr int kOffW1 = 0;
+constexpr int kOffB1 = kOffW1 + kMlpIn * kMlpH;
+constexpr int kOffW2 = kOffB1 + kMlpH;
+constexpr int kOffB2 = kOffW2 + kMlpH * kMlpH;
+constexpr int kOffW3 = kOffB2 + kMlpH;
+constexpr int kOffB3 = kOffW3 + kMlpH;
+constexpr int kMlpParams = kOffB3 + 1;          // 1345
+constexpr int kMlpNorm = 2 * kMlpIn;
+
+__host__ __device__ inline float mlp_sigmoid(float x) { return 1.f / (1.f + expf(-x)); }
+__host__ __device__ inline float mlp_silu(float x) { return x * mlp_sigmoid(x); }
+// d silu / dx = s (1 + x (1 - s)), s = sigmoid(x)
+__host__ __device__ inline float mlp_silu_grad(float x) {
+    const float s = mlp_sigmoid(x);
+    return s * (1.f + x * (1.f - s));
+}
+__host__ __device__ inline float mlp_softplus(float x) { return x > 20.f ? x : log1pf(expf(x)); }
+
+// Forward pass of one sample; x: raw features, P: parameters, norm: mean and
+// inverse std.  Returns nu_t / nu.
+__host__ __device__ inline float mlp_infer(const float* P, const float* norm, const float* x) {
+    float xn[kMlpIn];
+#pragma unroll
+    for (int i = 0; i < kMlpIn; ++i) xn[i] = (x[i] - norm[i]) * norm[kMlpIn + i];
+    float h1[kMlpH];                                 // registers: every index is a constant
+#pragma unroll
+    for (int j = 0; j < kMlpH; ++j) {
+        float z = P[kOffB1 + j];
+#pragma unroll
+        for (int i = 0; i < kMlpIn; ++i) z += xn[i] * P[kOffW1 + i * kMlpH + j];
+        h1[j] = mlp_silu(z);
+    }
+    float z3 = P[kOffB3];
+#pragma unroll 2
+    for (int j = 0; j < kMlpH; ++j) {
+        float z = P[kOffB2 + j];
+#pragma unroll
+        for (int i = 0; i < kMlpH; ++i) z += h1[i] * P[kOffW2 + i * kMlpH + j];
+        z3 += mlp_silu(z) * P[kOffW3 + j];
+    }
+    return mlp_softplus(z3);
+}
+
+}  // namespace lbm

@@ -195,6 +195,13 @@ int lbm_macrovar(lbm_ctx* ctx, double* rho, double* ux, double* uy,
 /* Global fluid-node diagnostics (diag) computed on the device in FP64. */
 int lbm_diag(lbm_ctx* ctx, lbm_stats* st);
 
+/* S_ij S_ij of the strain rate from the non-equilibrium populations, per
+ * node, both methods of sijstat01 (saveload.f90:2320-2432): m1 from the
+ * non-equilibrium moments (Yu et al. 2006), m2 from f - f^eq in population
+ * space.  Host arrays of nx*ny*nz doubles in the reference layout (either may
+ * be NULL); solid nodes give 0. */
+int lbm_strain(lbm_ctx* ctx, double* sij2_m1, double* sij2_m2);
+
 /* Plane sums for statistc/statistc2: out[LBM_PROFILE_COLS*nx], column-major
  * (column c of plane ix at out[c + LBM_PROFILE_COLS*(ix-1)]). FP64. */
 int lbm_profiles(lbm_ctx* ctx, double* out);
@@ -280,6 +287,39 @@ int lbm_particles_get(lbm_ctx* ctx, double* pos, double* vel, double* omg,
 /* Solid node count, boundary links and refilled nodes of the last step. */
 int lbm_particle_counts(lbm_ctx* ctx, int64_t* nsolid, int64_t* nlinks,
                         int64_t* nrefill);
+
+/* ---- Learned LES closure (no reference counterpart) --------------------
+ * A per-node network maps 7 features of the resolved strain (from the
+ * non-equilibrium moments) and the wall distance to nu_t / nu >= 0:
+ * 7 -> 32 -> 32 -> 1, SiLU hidden layers, softplus output.  Parameters (FP32):
+ * W1[7][32] (row = input), b1[32], W2[32][32], b2[32], w3[32], b3; inputs are
+ * standardised with norm[0..6] (mean) and norm[7..13] (1 / std).  Training
+ * runs on the GPU: forward, backward (BF16 tensor-core GEMMs with FP32
+ * accumulation, or FP32 with LBM_MLP_FP32) and Adam on the FP32 master
+ * weights; loss = mean squared error of nu_t / nu. */
+#define LBM_MLP_IN 7
+#define LBM_MLP_HIDDEN 32
+#define LBM_MLP_PARAMS 1345
+#define LBM_MLP_NORM 14
+#define LBM_MLP_FP32 1          /* flags: FP32 FMA products instead of BF16 tensor cores */
+typedef struct lbm_mlp lbm_mlp;
+/* Glorot-uniform weights from the seed, zero biases, identity normalisation. */
+int lbm_mlp_create(lbm_mlp** m, uint64_t seed, int32_t device);
+int lbm_mlp_destroy(lbm_mlp* m);
+/* params: LBM_MLP_PARAMS floats, norm: LBM_MLP_NORM floats (either may be
+ * NULL).  Setting the parameters restarts the Adam state. */
+int lbm_mlp_get(lbm_mlp* m, float* params, float* norm);
+int lbm_mlp_set(lbm_mlp* m, const float* params, const float* norm);
+/* Training set: X[n][7] raw features, y[n] targets nu_t / nu (host FP32);
+ * set_norm != 0 takes the normalisation from the mean and std of X. */
+int lbm_mlp_set_data(lbm_mlp* m, const float* X, const float* y, int64_t n, int32_t set_norm);
+/* `steps` Adam steps (beta 0.9/0.999, eps 1e-8) on random batches of `batch`
+ * samples; losses (may be NULL) receives each step's batch loss. */
+int lbm_mlp_train(lbm_mlp* m, int32_t steps, int32_t batch, float lr, int32_t flags, float* losses);
+/* Loss and gradient of the mean loss over the whole training set. */
+int lbm_mlp_gradient(lbm_mlp* m, int32_t flags, double* loss, float* grad);
+/* nu_t / nu for X[n][7] (FP32 forward pass, the one the LES collision runs). */
+int lbm_mlp_predict(lbm_mlp* m, const float* X, int64_t n, float* out);
 
 #ifdef __cplusplus
 }

@@ -296,3 +296,120 @@ def particle_run(p: OrcParams, sp: Spheres, f: np.ndarray, nsteps: int, owner=No
         links.append(nl.value)
         refills.append(nr.value)
     return f, owner, links, refills
+
+
+# ---- strain rate from the non-equilibrium populations (sijstat01) -----------
+def strain_sij2(p: OrcParams, f: np.ndarray, s1: float, s9: float):
+    """S_ij S_ij per node by the two methods of sijstat01, in FP64, written
+    with the reference's own sums (saveload.f90:2322-2380, population order
+    of para.f90) so that it checks the GPU's lattice-vector formulation:
+    method 1 from the non-equilibrium moments (Yu et al. 2006), method 2 from
+    f - f^eq (saveload.f90:2385-2432).  f: (19, nx, ny, nz) deviations."""
+    rho, ux, uy, uz = macrovar(p, f)
+    ux2, uy2, uz2 = ux * ux, uy * uy, uz * uz
+    eqm1 = -11.0 * rho + 19.0 * (ux2 + uy2 + uz2)           # :2337-2342
+    eqm6 = 2.0 * ux2 - uy2 - uz2
+    eqm8 = uy2 - uz2
+    eqm10, eqm11, eqm12 = ux * uy, uy * uz, ux * uz
+    sum1 = f[1:7].sum(axis=0)                                # :2344-2355
+    sum2 = f[7:19].sum(axis=0)
+    sum6 = f[1] + f[2]
+    sum7 = f[3] + f[4] + f[5] + f[6]
+    sum8 = f[7:15].sum(axis=0)
+    sum9 = f[15:19].sum(axis=0)
+    sum10 = f[3] + f[4] - f[5] - f[6]
+    sum11 = f[7] + f[8] + f[9] + f[10] - f[11] - f[12] - f[13] - f[14]
+    evlm1 = -30.0 * f[0] - 11.0 * sum1 + 8.0 * sum2          # :2357-2362 (coef2, coef3, coef5)
+    evlm6 = 2.0 * sum6 - sum7 + sum8 - 2.0 * sum9
+    evlm8 = sum10 + sum11
+    evlm10 = f[7] - f[8] - f[9] + f[10]
+    evlm11 = f[15] - f[16] - f[17] + f[18]
+    evlm12 = f[11] - f[12] - f[13] + f[14]
+    n1 = s1 * (evlm1 - eqm1)                                 # :2364-2369
+    n9 = s9 * (evlm6 - eqm6)
+    n11 = s9 * (evlm8 - eqm8)
+    n13 = s9 * (evlm10 - eqm10)
+    n14 = s9 * (evlm11 - eqm11)
+    n15 = s9 * (evlm12 - eqm12)
+    sxx = -(n1 + 19.0 * n9) / 38.0                           # :2371-2376
+    syy = -(2.0 * n1 - 19.0 * (n9 - 3.0 * n11)) / 76.0
+    szz = -(2.0 * n1 - 19.0 * (n9 + 3.0 * n11)) / 76.0
+    sxy, syz, szx = -1.5 * n13, -1.5 * n14, -1.5 * n15
+    m1 = sxx**2 + syy**2 + szz**2 + 2.0 * (sxy**2 + syz**2 + szx**2)
+    usqr = 1.5 * (ux2 + uy2 + uz2)                            # :2385-2397
+    a = np.zeros((6,) + rho.shape)
+    for i in range(1, Q):
+        cu = CX[i] * ux + CY[i] * uy + CZ[i] * uz
+        fn = f[i] - W[i] * (rho + 3.0 * cu + 4.5 * cu * cu - usqr)
+        a[0] += fn * CX[i] * CX[i]
+        a[1] += fn * CY[i] * CY[i]
+        a[2] += fn * CZ[i] * CZ[i]
+        a[3] += fn * CX[i] * CY[i]
+        a[4] += fn * CY[i] * CZ[i]
+        a[5] += fn * CZ[i] * CX[i]
+    m2 = (a[0]**2 + a[1]**2 + a[2]**2 + 2.0 * (a[3]**2 + a[4]**2 + a[5]**2)) * (1.5 * s9) ** 2
+    return m1, m2
+
+
+# ---- learned LES closure network (no reference counterpart) -----------------
+MLP_IN, MLP_H = 7, 32
+MLP_PARAMS = MLP_IN * MLP_H + MLP_H + MLP_H * MLP_H + MLP_H + MLP_H + 1
+
+
+def mlp_unpack(p):
+    """(W1[7][32], b1, W2[32][32], b2, w3, b3) views of the parameter vector,
+    in the C ABI's order (W rows are inputs)."""
+    p = np.asarray(p, dtype=np.float64)
+    o = 0
+    W1 = p[o:o + MLP_IN * MLP_H].reshape(MLP_IN, MLP_H); o += MLP_IN * MLP_H
+    b1 = p[o:o + MLP_H]; o += MLP_H
+    W2 = p[o:o + MLP_H * MLP_H].reshape(MLP_H, MLP_H); o += MLP_H * MLP_H
+    b2 = p[o:o + MLP_H]; o += MLP_H
+    w3 = p[o:o + MLP_H]; o += MLP_H
+    return W1, b1, W2, b2, w3, p[o]
+
+
+def _sigmoid(x):
+    return 1.0 / (1.0 + np.exp(-x))
+
+
+def mlp_forward(p, norm, X):
+    """nu_t / nu for raw features X[n][7] in FP64 (the network of lbm_mlp.cuh)."""
+    W1, b1, W2, b2, w3, b3 = mlp_unpack(p)
+    norm = np.asarray(norm, dtype=np.float64)
+    xn = (np.asarray(X, dtype=np.float64) - norm[:MLP_IN]) * norm[MLP_IN:]
+    z1 = xn @ W1 + b1
+    h1 = z1 * _sigmoid(z1)
+    z2 = h1 @ W2 + b2
+    h2 = z2 * _sigmoid(z2)
+    z3 = h2 @ w3 + b3
+    return np.where(z3 > 20.0, z3, np.log1p(np.exp(np.minimum(z3, 20.0)))), (xn, z1, h1, z2, h2, z3)
+
+
+def mlp_loss_grad(p, norm, X, y):
+    """Mean squared error of nu_t / nu and its analytic gradient, FP64."""
+    out, (xn, z1, h1, z2, h2, z3) = mlp_forward(p, norm, X)
+    W1, b1, W2, b2, w3, b3 = mlp_unpack(p)
+    n = len(y)
+    diff = out - np.asarray(y, dtype=np.float64)
+    loss = float(np.mean(diff * diff))
+    dz3 = 2.0 * diff * _sigmoid(z3) / n
+    dsilu = lambda z: _sigmoid(z) * (1.0 + z * (1.0 - _sigmoid(z)))
+    dw3 = h2.T @ dz3
+    db3 = dz3.sum()
+    dz2 = np.outer(dz3, w3) * dsilu(z2)
+    dW2 = h1.T @ dz2
+    db2 = dz2.sum(axis=0)
+    dz1 = (dz2 @ W2.T) * dsilu(z1)
+    dW1 = xn.T @ dz1
+    db1 = dz1.sum(axis=0)
+    g = np.concatenate([dW1.ravel(), db1, dW2.ravel(), db2, dw3, [db3]])
+    return loss, g
+
+
+def mlp_adam(p, g, m, v, t, lr, b1=0.9, b2=0.999, eps=1e-8):
+    """One Adam step (Kingma & Ba 2015) on FP64 copies; returns (p, m, v)."""
+    m = b1 * m + (1 - b1) * g
+    v = b2 * v + (1 - b2) * g * g
+    p = p - lr * (m / (1 - b1**t)) / (np.sqrt(v / (1 - b2**t)) + eps)
+    return p, m, v

@@ -1,0 +1,103 @@
+"""GPU parity of the learned-closure path: strain from the non-equilibrium
+populations (both methods of sijstat01), through the C ABI, against the FP64
+oracle."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from test_oracle import random_f, stable_rates
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+@pytest.mark.parametrize("shape", [(12, 16, 10), (7, 9, 5)])
+def test_strain_fp64_matches_oracle(pkg, orc, shape):
+    nx, ny, nz = shape
+    run = pkg.RunParams(nx=nx, ny=ny, nz=nz, visc=0.01, force_y=1e-5, mrt_type=1,
+                        precision=pkg.PRECISIONS["fp64"])
+    f0 = random_f(orc, shape, seed=4)
+    p = orc.params_from(run)
+    f3 = orc.run(p, f0, 3)[0]                 # a state with a non-equilibrium part
+    r = run.rates()
+    m1o, m2o = orc.strain_sij2(p, f3, r["s1"], r["s9"])
+    with pkg.Lattice(run) as lat:
+        lat.upload_f(f0)
+        lat.step(3)
+        m1, m2 = lat.strain()
+    assert rel(m1, m1o) < 1e-10 and rel(m2, m2o) < 1e-10
+
+
+def test_strain_masks_solid_nodes(pkg, orc):
+    shape = (24, 32, 22)
+    run = pkg.RunParams(nx=shape[0], ny=shape[1], nz=shape[2], visc=0.02, force_y=2e-6, mrt_type=1,
+                        precision=pkg.PRECISIONS["fp32"])
+    pos = np.array([[12.0, 16.0, 11.0]])
+    with pkg.Lattice(run) as lat:
+        lat.init_channel(0.04, 0.05, 3)
+        lat.set_particles(pos, radius=4.0, rho_ratio=2.0)
+        lat.step(4)
+        m1, m2 = lat.strain()
+        rho = lat.macrovar()[0]
+    solid = rho == 2.0
+    assert solid.sum() > 200
+    assert (m1[solid] == 0).all() and (m2[solid] == 0).all()
+    assert (m1[~solid] > 0).mean() > 0.99
+
+
+def net_and_data(orc, n=1000, seed=0):
+    rng = np.random.default_rng(seed)
+    p = rng.normal(0, 0.3, orc.MLP_PARAMS).astype(np.float32)
+    norm = np.concatenate([rng.normal(0, 0.5, 7), rng.uniform(0.5, 2.0, 7)]).astype(np.float32)
+    X = rng.normal(0, 1, (n, 7)).astype(np.float32)
+    y = rng.uniform(0, 3, n).astype(np.float32)
+    return p, norm, X, y
+
+
+def test_mlp_gradient_matches_oracle(pkg, orc):
+    """Full-set loss and gradient: FP32 products to FP32 rounding, BF16
+    tensor-core products to BF16 rounding (8-bit mantissa)."""
+    p, norm, X, y = net_and_data(orc)
+    lo, go = orc.mlp_loss_grad(p.astype(np.float64), norm.astype(np.float64), X, y)
+    with pkg.ClosureNet(seed=1) as net:
+        net.set(p, norm)
+        net.set_data(X, y, set_norm=False)
+        l32, g32 = net.gradient(fp32=True)
+        l16, g16 = net.gradient(fp32=False)
+    assert abs(l32 - lo) < 1e-5 * lo
+    assert np.abs(g32 - go).max() < 1e-4 * np.abs(go).max()
+    assert abs(l16 - lo) < 2e-2 * lo
+    assert np.abs(g16 - go).max() < 3e-2 * np.abs(go).max()
+    # the tensor-core gradient points the same way
+    assert float(g16 @ go) / (np.linalg.norm(g16) * np.linalg.norm(go)) > 0.999
+
+
+def test_mlp_predict_matches_oracle(pkg, orc):
+    p, norm, X, _ = net_and_data(orc, n=3000, seed=2)
+    want, _ = orc.mlp_forward(p.astype(np.float64), norm.astype(np.float64), X)
+    with pkg.ClosureNet() as net:
+        net.set(p, norm)
+        got = net.predict(X)
+    assert np.abs(got - want).max() < 1e-5 * max(1.0, np.abs(want).max())
+
+
+@pytest.mark.parametrize("fp32", [True, False])
+def test_mlp_training_fits_a_smooth_target(pkg, orc, fp32):
+    rng = np.random.default_rng(5)
+    X = rng.normal(0, 1, (20000, 7)).astype(np.float32)
+    y = np.log1p(np.exp(0.8 * X[:, 0] - 0.5 * X[:, 3] + 0.3 * np.sin(2 * X[:, 6]))).astype(np.float32)
+    with pkg.ClosureNet(seed=7) as net:
+        net.set_data(X, y)
+        l0, _ = net.gradient(fp32=True)
+        losses = net.train(400, batch=4096, lr=3e-3, fp32=fp32)
+        l1, _ = net.gradient(fp32=True)
+        p, norm = net.get()
+    assert np.isfinite(losses).all()
+    assert l1 < 0.05 * l0
+    # the GPU's weights reproduce the loss in the oracle
+    lo, _ = orc.mlp_loss_grad(p.astype(np.float64), norm.astype(np.float64), X, y)
+    assert abs(lo - l1) < 1e-3 * max(lo, 1e-12) + 1e-7

@@ -1,0 +1,38 @@
+"""CPU checks of the oracle's strain rate (sijstat01's two methods): both give
+the analytic S_ij S_ij of a laminar Poiseuille flow, and agree with each
+other on a developed channel."""
+from __future__ import annotations
+
+import numpy as np
+
+from test_oracle import stable_rates
+
+
+def test_poiseuille_strain_both_methods(orc):
+    nx, ny, nz = 16, 4, 4
+    visc, g = 0.1, 1e-5
+    rates = stable_rates(visc)
+    p = orc.params(rates, (0.0, g, 0.0))
+    zero = np.zeros((nx, ny, nz), order="F")
+    f = orc.initpop(zero, zero, zero)
+    f = orc.run(p, f, 4000)[0]
+    m1, m2 = orc.strain_sij2(p, f, rates["s1"], rates["s9"])
+    x = np.arange(nx) + 0.5                   # node centres, walls at 0 and nx
+    dudx = g / (2 * visc) * (nx - 2 * x)      # u = g x (nx - x) / (2 visc)
+    exact = 0.5 * dudx**2                     # S_xy = S_yx = du/dx / 2
+    for m in (m1, m2):
+        prof = m.mean(axis=(1, 2))
+        assert np.abs(prof - exact).max() < 2e-2 * exact.max()
+    assert np.abs(m1 - m2).max() < 2e-2 * exact.max()
+
+
+def test_strain_zero_at_equilibrium(orc):
+    rng = np.random.default_rng(1)
+    shape = (6, 5, 4)
+    u = [rng.uniform(-0.02, 0.02, shape) for _ in range(3)]
+    f = orc.initpop(*u)
+    p = orc.params(stable_rates(0.05))
+    m1, m2 = orc.strain_sij2(p, f, 1.5, 1.2)
+    # equilibrium populations carry no non-equilibrium part (up to the F/2 of
+    # a zero force) -- both measures vanish to rounding
+    assert np.abs(m1).max() < 1e-24 and np.abs(m2).max() < 1e-24
