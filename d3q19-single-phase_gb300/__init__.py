@@ -51,7 +51,7 @@ EXPORTS = (
     "lbm_particles_place", "lbm_particles_set", "lbm_particles_get", "lbm_particle_counts",
     "lbm_timing_enable", "lbm_timing_get", "lbm_strain",
     "lbm_mlp_create", "lbm_mlp_destroy", "lbm_mlp_get", "lbm_mlp_set", "lbm_mlp_set_data", "lbm_mlp_train",
-    "lbm_mlp_gradient", "lbm_mlp_predict",
+    "lbm_mlp_gradient", "lbm_mlp_predict", "lbm_les_set", "lbm_les_nut", "lbm_les_training_data",
 )
 
 
@@ -144,6 +144,9 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
         "lbm_mlp_train": (ctypes.c_int, [ctx, ctypes.c_int32, ctypes.c_int32, ctypes.c_float, ctypes.c_int32, fp]),
         "lbm_mlp_gradient": (ctypes.c_int, [ctx, ctypes.c_int32, ctypes.POINTER(ctypes.c_double), fp]),
         "lbm_mlp_predict": (ctypes.c_int, [ctx, fp, ctypes.c_int64, fp]),
+        "lbm_les_set": (ctypes.c_int, [ctx, fp, fp, ctypes.c_double, ctypes.c_double]),
+        "lbm_les_nut": (ctypes.c_int, [ctx, dp]),
+        "lbm_les_training_data": (ctypes.c_int, [ctx, ctypes.c_int32, ctypes.c_double, ctypes.c_double, fp, fp, dp]),
         "lbm_diag": (ctypes.c_int, [ctx, ctypes.POINTER(LBMStats)]),
         "lbm_profiles": (ctypes.c_int, [ctx, dp]),
         "lbm_profiles_noalloc": (ctypes.c_int, [ctx, dp]),
@@ -495,6 +498,31 @@ class Lattice:
         outs = [np.empty(self.shape, dtype=np.float64, order="F") for _ in range(4)]
         self._call("lbm_macrovar", *map(_dptr, outs))
         return tuple(outs)
+
+    def les_set(self, params=None, norm=None, ustar: float = 0.0, h: float = 0.0) -> None:
+        """Fuse the closure network into the collision (None: plain MRT)."""
+        if params is None:
+            self._call("lbm_les_set", None, None, 0.0, 0.0)
+            return
+        p = np.ascontiguousarray(params, dtype=np.float32).reshape(MLP_PARAMS)
+        n = np.ascontiguousarray(norm, dtype=np.float32).reshape(MLP_NORM)
+        self._les = (p, n)
+        self._call("lbm_les_set", _fptr(p), _fptr(n), ustar, h)
+
+    def les_training_data(self, factor: int, ustar: float, h: float):
+        """(X[nc][7], y[nc], ubar[3][nxc][nyc][nzc]) of the box-filtered state."""
+        nxc, nyc, nzc = (d // factor for d in self.shape)
+        nc = nxc * nyc * nzc
+        X = np.empty((nc, MLP_IN), dtype=np.float32)
+        y = np.empty(nc, dtype=np.float32)
+        ub = np.empty((3, nc), dtype=np.float64)
+        self._call("lbm_les_training_data", factor, ustar, h, _fptr(X), _fptr(y), _dptr(ub))
+        return X, y, ub.reshape(3, nzc, nyc, nxc).transpose(0, 3, 2, 1)
+
+    def les_nut(self) -> np.ndarray:
+        out = np.empty(self.shape, dtype=np.float64, order="F")
+        self._call("lbm_les_nut", _dptr(out))
+        return out
 
     def strain(self) -> tuple[np.ndarray, np.ndarray]:
         """S_ij S_ij per node by the two methods of sijstat01 (moments, populations)."""

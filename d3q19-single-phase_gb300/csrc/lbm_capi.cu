@@ -22,6 +22,9 @@ struct lbm_ctx {
     int parity = 0;            // 0: natural orientation, 1: after an even AA step
     int64_t nsteps = 0;
     double* d_stage = nullptr; // FP64 staging for layout conversion
+    float* d_les = nullptr;    // closure network parameters + normalisation
+    float* d_s9 = nullptr;     // per-node shear rate of the closure
+    int use_rows_saved = 0;    // the step kernel choice without the closure
     size_t stage_elems = 0;
     double* d_red = nullptr;   // reduction partials
     size_t red_elems = 0;
@@ -352,6 +355,7 @@ int lbm_create(const lbm_params* p, lbm_ctx** out) {
     cudaDeviceGetAttribute(&s.sm_count, cudaDevAttrMultiProcessorCount, p->device);
     s.use_rows = !(p->flags & LBM_FLAG_SIMPLE_STEP) && rows_supported(s);
     if (s.use_rows && prepare_step_rows() != cudaSuccess) s.use_rows = 0;
+    c->use_rows_saved = s.use_rows;
     e = cudaMalloc(&c->d_err, sizeof(int));
     if (e != cudaSuccess) { lbm_destroy(c); return cuda_fail(e, "cudaMalloc(error flag)"); }
     cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
@@ -387,6 +391,8 @@ int lbm_destroy(lbm_ctx* c) {
     cudaFree(c->P.counters);
     cudaFree(c->P.cell_count);
     cudaFree(c->P.geom);
+    cudaFree(c->d_les);
+    cudaFree(c->d_s9);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return LBM_OK;
@@ -594,6 +600,89 @@ int lbm_strain(lbm_ctx* c, double* m1, double* m2) {
         if (m2) CK(cudaMemcpyAsync(m2 + (size_t)z0 * pp, d2, n * 8, cudaMemcpyDeviceToHost, c->stream));
     }
     return sync(c);
+}
+
+int lbm_les_set(lbm_ctx* c, const float* params, const float* norm, double ustar, double h) {
+    if (check_ctx(c)) return LBM_ERR_INVALID_ARG;
+    if (int rc = set_device(c)) return rc;
+    if (!params) {
+        c->s.les_w = nullptr;
+        c->s.use_rows = c->use_rows_saved;
+        return LBM_OK;
+    }
+    if (!norm || !(ustar > 0.0) || !(h > 0.0)) return fail(LBM_ERR_INVALID_ARG, "closure needs norm, ustar > 0, h > 0");
+    if (c->p.precision == LBM_PREC_FP16) return fail(LBM_ERR_INVALID_ARG, "the LES closure runs with FP32 or FP64 storage");
+    if (c->P.npart > 0) return fail(LBM_ERR_STATE, "the LES closure is for particle-free channels");
+    if (!c->d_les) {
+        CK(cudaMalloc(&c->d_les, (LBM_MLP_PARAMS + LBM_MLP_NORM) * sizeof(float)));
+        CK(cudaMalloc(&c->d_s9, c->s.N * sizeof(float)));
+    }
+    CK(cudaMemcpyAsync(c->d_les, params, LBM_MLP_PARAMS * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_les + LBM_MLP_PARAMS, norm, LBM_MLP_NORM * sizeof(float), cudaMemcpyHostToDevice,
+                       c->stream));
+    {
+        // the first collision's features use the molecular rate
+        std::vector<float> s9(c->s.N, (float)c->p.s9);
+        CK(cudaMemcpyAsync(c->d_s9, s9.data(), c->s.N * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    c->s.les_w = c->d_les;
+    c->s.les_s9 = c->d_s9;
+    c->s.les_nu = (1.0 / c->p.s9 - 0.5) / 3.0;
+    c->s.les_ustar = (float)ustar;
+    c->s.les_h = (float)h;
+    c->s.use_rows = 0;
+    return sync(c);
+}
+
+int lbm_les_training_data(lbm_ctx* c, int32_t factor, double ustar, double h, float* X, float* y, double* ubar) {
+    if (check_ctx(c)) return LBM_ERR_INVALID_ARG;
+    if (factor < 1 || c->p.nx % factor || c->p.ny % factor || c->p.nz % factor || !(ustar > 0.0) || !(h > 0.0))
+        return fail(LBM_ERR_INVALID_ARG, "factor must divide nx, ny, nz; ustar and h positive");
+    if (c->P.npart > 0) return fail(LBM_ERR_STATE, "training data come from a particle-free channel");
+    if (int rc = set_device(c)) return rc;
+    const int nxc = c->p.nx / factor, nyc = c->p.ny / factor, nzc = c->p.nz / factor;
+    const size_t nc = (size_t)nxc * nyc * nzc;
+    double* d9 = nullptr;
+    float* dxy = nullptr;
+    CK(cudaMalloc(&d9, 9 * nc * sizeof(double)));
+    int rc = LBM_OK;
+    do {
+        if (cudaMalloc(&dxy, (LBM_MLP_IN + 1) * nc * sizeof(float)) != cudaSuccess) { rc = fail(LBM_ERR_CUDA, "cudaMalloc"); break; }
+        const double nu_f = (1.0 / c->p.s9 - 0.5) / 3.0;
+        cudaError_t e = launch_box_filter(c->s, c->parity, factor, nxc, nyc, nzc, d9, c->stream);
+        if (e == cudaSuccess)
+            e = launch_closure_targets(d9, nxc, nyc, nzc, (float)(nu_f / factor), (float)ustar, (float)(h / factor),
+                                       dxy, dxy + LBM_MLP_IN * nc, c->stream);
+        if (e == cudaSuccess && X) e = cudaMemcpyAsync(X, dxy, LBM_MLP_IN * nc * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess && y) e = cudaMemcpyAsync(y, dxy + LBM_MLP_IN * nc, nc * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess && ubar) e = cudaMemcpyAsync(ubar, d9, 3 * nc * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) { rc = fail(LBM_ERR_CUDA, std::string("closure training data: ") + cudaGetErrorString(e)); break; }
+    } while (false);
+    cudaFree(d9);
+    cudaFree(dxy);
+    if (rc) return rc;
+    return sync(c);
+}
+
+int lbm_les_nut(lbm_ctx* c, double* nut) {
+    if (check_ctx(c) || !nut) return fail(LBM_ERR_INVALID_ARG, "null argument");
+    if (!c->s.les_w) return fail(LBM_ERR_STATE, "the LES closure is off (lbm_les_set)");
+    if (int rc = set_device(c)) return rc;
+    std::vector<float> s9(c->s.N);
+    CK(cudaMemcpyAsync(s9.data(), c->d_s9, c->s.N * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    if (int rc = sync(c)) return rc;
+    const double nu = c->s.les_nu;
+    const Geometry& g = c->s.g;
+    for (int Z = 0; Z < g.NZ; ++Z)
+        for (int Y = 0; Y < g.NY; ++Y)
+            for (int X = 0; X < g.NX; ++X) {
+                const double s = s9[(size_t)X + (size_t)g.NX * ((size_t)Y + (size_t)g.NY * Z)];
+                // GPU (X, Y, Z) = reference (y, z, x)
+                nut[(size_t)Z + (size_t)c->p.nx * ((size_t)X + (size_t)c->p.ny * Y)] = ((1.0 / s - 0.5) / 3.0) / nu - 1.0;
+            }
+    return LBM_OK;
 }
 
 int lbm_profiles(lbm_ctx* c, double* out) {

@@ -3,6 +3,7 @@
 // macroscopic fields and FP64 reductions for the diagnostics.
 #include "lbm_internal.h"
 #include "lbm_strain.cuh"
+#include "lbm_mlp.cuh"
 
 namespace lbm {
 
@@ -279,6 +280,81 @@ __global__ void k_strain(DeviceState s, int parity, double* __restrict__ m1, dou
     }
 }
 
+// Training data of the closure, step 1: box filter of u and u_i u_j over
+// factor^3 fine nodes into coarse cell (ixc, iyc, izc); out[9][nc] (u, v, w,
+// uu, vv, ww, uv, vw, uw) in the coarse reference layout.
+template <typename T>
+__global__ void k_box_filter(DeviceState s, int parity, int factor, int nxc, int nyc, int nzc,
+                             double* __restrict__ out) {
+    const int ixc = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ixc >= nxc) return;
+    const int iyc = blockIdx.y, izc = blockIdx.z;
+    const double F[3] = {(double)s.cd.Fx, (double)s.cd.Fy, (double)s.cd.Fz};
+    double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int dz = 0; dz < factor; ++dz)
+        for (int dy = 0; dy < factor; ++dy)
+            for (int dx = 0; dx < factor; ++dx) {
+                const int ix = ixc * factor + dx, iy = iyc * factor + dy, iz = izc * factor + dz;
+                double f[Q];
+                gather_natural<T>(s, parity, iy, iz, ix, f);
+                double rho, u, v, w;
+                macro_of<double>(f, F, rho, u, v, w);
+                acc[0] += u; acc[1] += v; acc[2] += w;
+                acc[3] += u * u; acc[4] += v * v; acc[5] += w * w;
+                acc[6] += u * v; acc[7] += v * w; acc[8] += u * w;
+            }
+    const double inv = 1.0 / ((double)factor * factor * factor);
+    const size_t nc = (size_t)nxc * nyc * nzc;
+    const size_t o = (size_t)ixc + (size_t)nxc * ((size_t)iyc + (size_t)nyc * izc);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) out[k * nc + o] = acc[k] * inv;
+}
+
+// Training data, step 2: on the coarse grid the strain of the filtered
+// velocity (central differences; periodic in y and z, the no-slip image
+// u = -u(first cell) across the walls), the closure features and the target
+// nu_t* / nu_c = max(0, -tau^d : S / (2 S : S)) / nu_c with the subgrid stress
+// tau = filtered(u u) - filtered(u) filtered(u) (least-squares eddy viscosity).
+__global__ void k_closure_targets(const double* __restrict__ F9, int nxc, int nyc, int nzc, float nu_c,
+                                  float ustar, float h_c, float* __restrict__ X, float* __restrict__ y) {
+    const int ixc = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ixc >= nxc) return;
+    const int iyc = blockIdx.y, izc = blockIdx.z;
+    const size_t nc = (size_t)nxc * nyc * nzc;
+    auto at = [&](int k, int ix, int iy, int iz) -> double {
+        // velocity component k at a coarse cell, with the wall image in x
+        double sgn = 1.0;
+        if (ix < 0) { ix = 0; sgn = -1.0; }
+        if (ix >= nxc) { ix = nxc - 1; sgn = -1.0; }
+        iy = (iy + nyc) % nyc;
+        iz = (iz + nzc) % nzc;
+        return sgn * F9[k * nc + (size_t)ix + (size_t)nxc * ((size_t)iy + (size_t)nyc * iz)];
+    };
+    double G[3][3];                                   // G[a][b] = d u_a / d x_b
+    for (int a = 0; a < 3; ++a) {
+        G[a][0] = 0.5 * (at(a, ixc + 1, iyc, izc) - at(a, ixc - 1, iyc, izc));
+        G[a][1] = 0.5 * (at(a, ixc, iyc + 1, izc) - at(a, ixc, iyc - 1, izc));
+        G[a][2] = 0.5 * (at(a, ixc, iyc, izc + 1) - at(a, ixc, iyc, izc - 1));
+    }
+    const double S[6] = {G[0][0], G[1][1], G[2][2], 0.5 * (G[0][1] + G[1][0]), 0.5 * (G[1][2] + G[2][1]),
+                         0.5 * (G[0][2] + G[2][0])};
+    const size_t o = (size_t)ixc + (size_t)nxc * ((size_t)iyc + (size_t)nyc * izc);
+    const double u = F9[o], v = F9[nc + o], w = F9[2 * nc + o];
+    double tau[6] = {F9[3 * nc + o] - u * u, F9[4 * nc + o] - v * v, F9[5 * nc + o] - w * w,
+                     F9[6 * nc + o] - u * v, F9[7 * nc + o] - v * w, F9[8 * nc + o] - u * w};
+    const double t3 = (tau[0] + tau[1] + tau[2]) / 3.0;
+    tau[0] -= t3; tau[1] -= t3; tau[2] -= t3;
+    const double num = -(tau[0] * S[0] + tau[1] * S[1] + tau[2] * S[2] + 2.0 * (tau[3] * S[3] + tau[4] * S[4] + tau[5] * S[5]));
+    const double den = 2.0 * (S[0] * S[0] + S[1] * S[1] + S[2] * S[2] + 2.0 * (S[3] * S[3] + S[4] * S[4] + S[5] * S[5]));
+    const double nut = den > 0.0 ? fmax(num / den, 0.0) : 0.0;
+    float Sf[6], x[kMlpIn];
+    for (int k = 0; k < 6; ++k) Sf[k] = (float)S[k];
+    const float dwall = fminf((float)ixc + 0.5f, (float)nxc - (float)ixc - 0.5f);
+    closure_features(Sf, dwall, nu_c, ustar, h_c, x);
+    for (int k = 0; k < kMlpIn; ++k) X[o * kMlpIn + k] = x[k];
+    y[o] = (float)(nut / nu_c);
+}
+
 __global__ void k_ref_to_gpu_vec(Geometry g, size_t N, const double* __restrict__ ux,
                                  const double* __restrict__ uy, const double* __restrict__ uz,
                                  double* __restrict__ uf, int z0) {
@@ -454,6 +530,21 @@ cudaError_t launch_macro(const DeviceState& s, int parity, double* rho, double* 
 cudaError_t launch_strain(const DeviceState& s, int parity, double* m1, double* m2, int z0, int nzc,
                           cudaStream_t st) {
     LBM_DISPATCH(s.prec, (k_strain<T><<<ref_grid(s.g, nzc, kBx), kBx, 0, st>>>(s, parity, m1, m2, z0)))
+}
+
+cudaError_t launch_box_filter(const DeviceState& s, int parity, int factor, int nxc, int nyc, int nzc,
+                              double* out, cudaStream_t st) {
+    const int bx = nxc < 128 ? nxc : 128;
+    const dim3 grid((nxc + bx - 1) / bx, nyc, nzc);
+    LBM_DISPATCH(s.prec, (k_box_filter<T><<<grid, bx, 0, st>>>(s, parity, factor, nxc, nyc, nzc, out)))
+}
+
+cudaError_t launch_closure_targets(const double* F9, int nxc, int nyc, int nzc, float nu_c, float ustar,
+                                   float h_c, float* X, float* y, cudaStream_t st) {
+    const int bx = nxc < 128 ? nxc : 128;
+    const dim3 grid((nxc + bx - 1) / bx, nyc, nzc);
+    k_closure_targets<<<grid, bx, 0, st>>>(F9, nxc, nyc, nzc, nu_c, ustar, h_c, X, y);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_ref_to_gpu_vec(const DeviceState& s, const double* ux, const double* uy,

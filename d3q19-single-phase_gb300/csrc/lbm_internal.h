@@ -85,6 +85,13 @@ struct DeviceState {
     const int* owner;
     const double *ppos, *pvel, *pomg;
     double prho;
+    // learned LES closure (les_w == nullptr: off): network parameters and
+    // feature normalisation (1345 + 14 floats), per-node shear rate of the
+    // last collision, molecular viscosity and the wall units of the features
+    const float* les_w;
+    float* les_s9;
+    double les_nu;
+    float les_ustar, les_h;
 };
 
 // launchers (lbm_step.cu)
@@ -117,6 +124,10 @@ cudaError_t launch_macro(const DeviceState& s, int parity, double* rho,
 // velocity (nx*ny*nz*3 doubles, reference layout chunk) to GPU-layout frozen u
 cudaError_t launch_strain(const DeviceState& s, int parity, double* m1, double* m2, int z0, int nzc,
                           cudaStream_t st);
+cudaError_t launch_box_filter(const DeviceState& s, int parity, int factor, int nxc, int nyc, int nzc,
+                              double* out, cudaStream_t st);
+cudaError_t launch_closure_targets(const double* F9, int nxc, int nyc, int nzc, float nu_c, float ustar,
+                                   float h_c, float* X, float* y, cudaStream_t st);
 cudaError_t launch_ref_to_gpu_vec(const DeviceState& s, const double* ux,
                                   const double* uy, const double* uz,
                                   double* uf, int z0, int nzc, cudaStream_t st);

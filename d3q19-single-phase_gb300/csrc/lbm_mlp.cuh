@@ -59,3 +59,38 @@ __host__ __device__ inline float mlp_infer(const float* P, const float* norm, co
 }
 
 }  // namespace lbm
+
+namespace lbm {
+
+// The 7 inputs of the closure from the resolved strain rate
+// S = {xx, yy, zz, xy, yz, zx} (reference axes: x is the wall normal) and the
+// distance to the nearest wall; invariant under rotations about the wall
+// normal and reflections:
+//   x0 = log(1 + |S| nu / u*^2)        strain magnitude in wall units, |S| = sqrt(2 S:S)
+//   x1 = tr S / |S|                     dilatation ratio
+//   x2 = sqrt(6) det(D) / (D:D)^(3/2)   strain state of the deviator D
+//   x3 = D_xx / |D|                     normal strain along the wall normal
+//   x4 = sqrt(D_xy^2 + D_xz^2) / |D|    shear between the normal and the wall plane
+//   x5 = log(1 + d u* / nu)             wall distance in wall units
+//   x6 = d / h                          wall distance in outer units
+__host__ __device__ inline void closure_features(const float S[6], float dwall, float nu, float ustar, float h,
+                                                 float x[kMlpIn]) {
+    const float tr = S[0] + S[1] + S[2];
+    const float off = S[3] * S[3] + S[4] * S[4] + S[5] * S[5];
+    const float ss = S[0] * S[0] + S[1] * S[1] + S[2] * S[2] + 2.f * off;
+    const float smag = sqrtf(2.f * ss);
+    const float t3 = tr * (1.f / 3.f);
+    const float d0 = S[0] - t3, d1 = S[1] - t3, d2 = S[2] - t3;
+    const float i2 = d0 * d0 + d1 * d1 + d2 * d2 + 2.f * off;
+    const float det = d0 * (d1 * d2 - S[4] * S[4]) - S[3] * (S[3] * d2 - S[4] * S[5]) + S[5] * (S[3] * S[4] - d1 * S[5]);
+    const float rn = sqrtf(i2) + 1e-30f;
+    x[0] = log1pf(smag * nu / (ustar * ustar));
+    x[1] = tr / (smag + 1e-30f);
+    x[2] = 2.4494897f * det / (rn * rn * rn);
+    x[3] = d0 / rn;
+    x[4] = sqrtf(S[3] * S[3] + S[5] * S[5]) / rn;
+    x[5] = log1pf(dwall * ustar / nu);
+    x[6] = dwall / h;
+}
+
+}  // namespace lbm

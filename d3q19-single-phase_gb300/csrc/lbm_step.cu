@@ -21,6 +21,8 @@
 // node's own slot opp(i).  The periodic y/z exchange (collisionExchnge,
 // collision.f90:281-372) becomes index wrap-around.
 #include "lbm_internal.h"
+#include "lbm_mlp.cuh"
+#include "lbm_strain.cuh"
 
 namespace lbm {
 
@@ -116,6 +118,95 @@ k_step_odd(PopPtrs<T> P, CollideConsts<R> C, Geometry g)
     else                odd_node<T, R, 3, false, YF>(P, C, I, n, R(0), R(0), R(0), rho, jx, jy, jz);
 }
 
+// ---------------------------------------------------------------------------
+// Coarse-grid LES with the learned closure fused into the collision.  Per
+// node: the strain rate from the non-equilibrium moments (Yu et al. 2006,
+// with the shear rate of the node's previous collision, which produced that
+// non-equilibrium part), the closure's seven features, the network with its
+// weights in shared memory, and the shear moments relaxed at
+// s9 = s13 = 1 / (3 (nu + nu_t) + 1/2).  Storage with S = 1 (FP32/FP64).
+template <typename R, bool YF>
+__device__ __forceinline__ void les_collide(R f[Q], const CollideConsts<R>& C, const DeviceState& s,
+                                            const float* Ws, uint32_t n, int z) {
+    R rho = 0, jx = 0, jy = 0, jz = 0;
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        rho += f[i];
+        if (CXf(i)) jx += R(CXf(i)) * f[i];
+        if (CYf(i)) jy += R(CYf(i)) * f[i];
+        if (CZf(i)) jz += R(CZf(i)) * f[i];
+    }
+    jx += C.hFx; jy += C.hFy; jz += C.hFz;
+    R S6[6];
+    strain_from_moments<R>(f, rho, jx, jy, jz, C.ke * R(2394), (R)s.les_s9[n], S6);
+    float Sf[6], x[kMlpIn];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) Sf[k] = (float)S6[k];
+    const float dwall = fminf((float)z + 0.5f, (float)s.g.NZ - (float)z - 0.5f);
+    closure_features(Sf, dwall, (float)s.les_nu, s.les_ustar, s.les_h, x);
+    const float r = mlp_infer(Ws, Ws + kMlpParams, x);
+    const R s9 = R(1) / (R(3) * (R)s.les_nu * (R(1) + (R)r) + R(0.5));
+    s.les_s9[n] = (float)s9;
+    CollideConsts<R> cl = C;
+    cl.kp = s9 * R(1.0 / 36.0);
+    cl.kw = s9 * R(1.0 / 12.0);
+    cl.kxy = s9 * R(0.25);
+    R a, b, c, d;
+    collide<R, false, YF>(f, cl, R(0), R(0), R(0), a, b, c, d);
+}
+
+template <typename T, typename R, bool YF>
+__global__ void __launch_bounds__(kBlockX) k_les_even(PopPtrs<T> P, CollideConsts<R> C, DeviceState s) {
+    __shared__ float Ws[kMlpParams + kMlpNorm];
+    for (int e = threadIdx.x; e < kMlpParams + kMlpNorm; e += blockDim.x) Ws[e] = s.les_w[e];
+    __syncthreads();
+    const Geometry& g = s.g;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= g.NX) return;
+    const uint32_t n = x + g.NX * (blockIdx.y + g.NY * blockIdx.z);
+    R f[Q];
+#pragma unroll
+    for (int i = 0; i < Q; ++i) f[i] = ld_pop(P.p[i] + n);
+    les_collide<R, YF>(f, C, s, Ws, n, blockIdx.z);
+#pragma unroll
+    for (int i = 0; i < Q; ++i) st_pop(P.p[OPPf(i)] + n, f[i]);
+}
+
+template <typename T, typename R, int WALL, bool YF>
+__device__ __forceinline__ void les_odd_node(const PopPtrs<T>& P, const CollideConsts<R>& C, const DeviceState& s,
+                                             const float* Ws, const NodeIdx& I, uint32_t n, int z) {
+    R f[Q];
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        if (pull_bounces<WALL>(i)) f[i] = ld_pop(P.p[i] + n);
+        else f[i] = ld_pop(P.p[OPPf(i)] + I.at(-DXg(i), -DYg(i), -DZg(i)));
+    }
+    les_collide<R, YF>(f, C, s, Ws, n, z);
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        if (push_bounces<WALL>(i)) st_pop(P.p[OPPf(i)] + n, f[i]);
+        else st_pop(P.p[i] + I.at(DXg(i), DYg(i), DZg(i)), f[i]);
+    }
+}
+
+template <typename T, typename R, bool YF>
+__global__ void __launch_bounds__(kBlockX) k_les_odd(PopPtrs<T> P, CollideConsts<R> C, DeviceState s) {
+    __shared__ float Ws[kMlpParams + kMlpNorm];
+    for (int e = threadIdx.x; e < kMlpParams + kMlpNorm; e += blockDim.x) Ws[e] = s.les_w[e];
+    __syncthreads();
+    const Geometry& g = s.g;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= g.NX) return;
+    const int y = blockIdx.y, z = blockIdx.z;
+    const NodeIdx I = make_idx(g, x, y, z);
+    const uint32_t n = I.at(0, 0, 0);
+    const int wall = (z == 0 ? 1 : 0) | (z == g.NZ - 1 ? 2 : 0);
+    if (wall == 0)      les_odd_node<T, R, 0, YF>(P, C, s, Ws, I, n, z);
+    else if (wall == 1) les_odd_node<T, R, 1, YF>(P, C, s, Ws, I, n, z);
+    else if (wall == 2) les_odd_node<T, R, 2, YF>(P, C, s, Ws, I, n, z);
+    else                les_odd_node<T, R, 3, YF>(P, C, s, Ws, I, n, z);
+}
+
 // Pre-relaxation step (main.f90:69-90): velocity frozen at uf (GPU layout,
 // three planes of N doubles), rho = sum f.  rho holds the previous iteration's
 // density on entry and this iteration's on exit; maxabs receives
@@ -187,6 +278,18 @@ cudaError_t step_impl(const DeviceState& s, int parity, cudaStream_t st) {
     const CollideConsts<R>* C;
     if constexpr (sizeof(R) == 8) C = &s.cd; else C = &s.cf;
     const bool yf = C->Fx == R(0) && C->Fz == R(0);
+    if constexpr (PREC != LBM_PREC_FP16) {
+        if (s.les_w) {
+            if (yf) {
+                if (parity == 0) k_les_even<T, R, true><<<grid, bx, 0, st>>>(P, *C, s);
+                else             k_les_odd<T, R, true><<<grid, bx, 0, st>>>(P, *C, s);
+            } else {
+                if (parity == 0) k_les_even<T, R, false><<<grid, bx, 0, st>>>(P, *C, s);
+                else             k_les_odd<T, R, false><<<grid, bx, 0, st>>>(P, *C, s);
+            }
+            return cudaGetLastError();
+        }
+    }
     if (yf) {
         if (parity == 0) k_step_even<T, R, true><<<grid, bx, 0, st>>>(P, *C, s.g);
         else             k_step_odd<T, R, true><<<grid, bx, 0, st>>>(P, *C, s.g);

@@ -321,6 +321,28 @@ int lbm_mlp_gradient(lbm_mlp* m, int32_t flags, double* loss, float* grad);
 /* nu_t / nu for X[n][7] (FP32 forward pass, the one the LES collision runs). */
 int lbm_mlp_predict(lbm_mlp* m, const float* X, int64_t n, float* out);
 
+/* Coarse-grid LES: the closure fused into the collision.  Per node the strain
+ * rate from the non-equilibrium moments (Yu et al. 2006, with the shear rate
+ * of the node's previous collision), the 7 features (strain invariants with
+ * the wall normal, wall distance in wall units u* / nu and in units of h),
+ * the network (weights in shared memory) and s9 = s13 = 1 / (3 (nu + nu_t) +
+ * 1/2).  params == NULL turns it off.  FP32/FP64 storage, particle-free
+ * channels; steps use the one-node-per-thread kernels while it is on. */
+int lbm_les_set(lbm_ctx* ctx, const float* params, const float* norm, double ustar, double h);
+/* nu_t / nu of the last collision per node (host, nx*ny*nz doubles, reference
+ * layout). */
+int lbm_les_nut(lbm_ctx* ctx, double* nut);
+/* Training data of the closure from a fine (DNS) lattice of this context: box
+ * filter by `factor` (dividing nx, ny, nz) of u and u_i u_j; on the coarse
+ * grid the strain of the filtered velocity (central differences, no-slip
+ * image across the walls), the closure features in the coarse grid's units
+ * (nu_c = nu / factor, u* the same, h_c = h / factor: acoustic scaling) and the
+ * target nu_t* / nu_c = max(0, -tau^d : S / (2 S : S)) / nu_c, tau the subgrid
+ * stress.  Coarse cells in the reference layout: X[nc][7], y[nc] (FP32),
+ * ubar[3][nc] (FP64, filtered velocity); any may be NULL. */
+int lbm_les_training_data(lbm_ctx* ctx, int32_t factor, double ustar, double h, float* X, float* y,
+                          double* ubar);
+
 #ifdef __cplusplus
 }
 #endif

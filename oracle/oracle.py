@@ -413,3 +413,128 @@ def mlp_adam(p, g, m, v, t, lr, b1=0.9, b2=0.999, eps=1e-8):
     v = b2 * v + (1 - b2) * g * g
     p = p - lr * (m / (1 - b1**t)) / (np.sqrt(v / (1 - b2**t)) + eps)
     return p, m, v
+
+
+def strain_tensor(p: OrcParams, f: np.ndarray, s1: float, s9):
+    """S = {xx, yy, zz, xy, yz, zx} per node from the non-equilibrium moments
+    (the same formulas as strain_sij2's method 1, saveload.f90:2322-2376);
+    s9 may be a per-node array (the shear rate that produced the
+    non-equilibrium part)."""
+    rho, ux, uy, uz = macrovar(p, f)
+    ux2, uy2, uz2 = ux * ux, uy * uy, uz * uz
+    sum1 = f[1:7].sum(axis=0)
+    sum2 = f[7:19].sum(axis=0)
+    evlm1 = -30.0 * f[0] - 11.0 * sum1 + 8.0 * sum2
+    evlm6 = 2.0 * (f[1] + f[2]) - (f[3] + f[4] + f[5] + f[6]) + f[7:15].sum(axis=0) - 2.0 * f[15:19].sum(axis=0)
+    evlm8 = (f[3] + f[4] - f[5] - f[6]) + (f[7] + f[8] + f[9] + f[10] - f[11] - f[12] - f[13] - f[14])
+    n1 = s1 * (evlm1 - (-11.0 * rho + 19.0 * (ux2 + uy2 + uz2)))
+    n9 = s9 * (evlm6 - (2.0 * ux2 - uy2 - uz2))
+    n11 = s9 * (evlm8 - (uy2 - uz2))
+    S = np.empty((6,) + rho.shape)
+    S[0] = -(n1 + 19.0 * n9) / 38.0
+    S[1] = -(2.0 * n1 - 19.0 * (n9 - 3.0 * n11)) / 76.0
+    S[2] = -(2.0 * n1 - 19.0 * (n9 + 3.0 * n11)) / 76.0
+    S[3] = -1.5 * s9 * (f[7] - f[8] - f[9] + f[10] - ux * uy)
+    S[4] = -1.5 * s9 * (f[15] - f[16] - f[17] + f[18] - uy * uz)
+    S[5] = -1.5 * s9 * (f[11] - f[12] - f[13] + f[14] - ux * uz)
+    return S
+
+
+def closure_features(S, dwall, nu, ustar, h):
+    """The closure's 7 inputs (as lbm_mlp.cuh) in FP64; S (6, ...) and dwall
+    broadcastable; returns (..., 7)."""
+    tr = S[0] + S[1] + S[2]
+    off = S[3] ** 2 + S[4] ** 2 + S[5] ** 2
+    smag = np.sqrt(2.0 * (S[0] ** 2 + S[1] ** 2 + S[2] ** 2 + 2.0 * off))
+    d0, d1, d2 = S[0] - tr / 3, S[1] - tr / 3, S[2] - tr / 3
+    rn = np.sqrt(d0 * d0 + d1 * d1 + d2 * d2 + 2.0 * off) + 1e-30
+    det = d0 * (d1 * d2 - S[4] ** 2) - S[3] * (S[3] * d2 - S[4] * S[5]) + S[5] * (S[3] * S[4] - d1 * S[5])
+    dwall = np.broadcast_to(dwall, tr.shape)
+    return np.stack([np.log1p(smag * nu / ustar**2), tr / (smag + 1e-30), np.sqrt(6.0) * det / rn**3,
+                     d0 / rn, np.sqrt(S[3] ** 2 + S[5] ** 2) / rn, np.log1p(dwall * ustar / nu),
+                     dwall / h], axis=-1)
+
+
+OPP = np.array([int(np.flatnonzero((CX == -CX[i]) & (CY == -CY[i]) & (CZ == -CZ[i]))[0]) for i in range(Q)])
+
+
+def les_step(p: OrcParams, f: np.ndarray, s9prev: np.ndarray, params, norm, ustar: float, h: float):
+    """One coarse-LES step with the closure, FP64: per node the strain from the
+    non-equilibrium moments with s9prev, the features and the network give
+    s9 = s13 = 1/(3 nu (1 + nu_t/nu) + 1/2); collide_node with those rates;
+    push streaming with half-way bounce-back at the x walls and periodic y, z.
+    Returns (f, s9).  Small lattices only (a Python loop over nodes)."""
+    _, nx, ny, nz = f.shape
+    nu = (1.0 / p.s9 - 0.5) / 3.0
+    S = strain_tensor(p, f, p.s1, s9prev)
+    dwall = np.minimum(np.arange(nx) + 0.5, nx - np.arange(nx) - 0.5)[:, None, None]
+    X = closure_features(S, dwall, nu, ustar, h).reshape(-1, 7)
+    r, _ = mlp_forward(params, norm, X)
+    s9 = (1.0 / (3.0 * nu * (1.0 + r) + 0.5)).reshape(nx, ny, nz)
+    rho, ux, uy, uz = macrovar(p, f)
+    post = np.empty_like(f)
+    q = OrcParams.from_buffer_copy(p)
+    for ix in range(nx):
+        for iy in range(ny):
+            for iz in range(nz):
+                q.s9 = q.s13 = s9[ix, iy, iz]
+                post[:, ix, iy, iz] = collide_node(q, np.ascontiguousarray(f[:, ix, iy, iz]), rho[ix, iy, iz],
+                                                   ux[ix, iy, iz], uy[ix, iy, iz], uz[ix, iy, iz])
+    out = np.empty_like(f)
+    for i in range(Q):
+        moved = np.roll(np.roll(post[i], CY[i], axis=1), CZ[i], axis=2)
+        if CX[i] == 0:
+            out[i] = moved
+        elif CX[i] > 0:
+            out[i, 1:] = moved[:-1]
+        else:
+            out[i, :-1] = moved[1:]
+    # half-way bounce-back: a population leaving through a wall comes back
+    # into the opposite direction at the same node
+    for i in range(Q):
+        if CX[i] > 0:
+            out[OPP[i], -1] = post[i, -1]
+        elif CX[i] < 0:
+            out[OPP[i], 0] = post[i, 0]
+    return out, s9
+
+
+def closure_training_data(p: OrcParams, f: np.ndarray, factor: int, ustar: float, h: float):
+    """Box filter by `factor`, strain of the filtered velocity by central
+    differences (periodic y, z; no-slip image across the x walls), closure
+    features (coarse units: nu/factor, h/factor) and the target
+    max(0, -tau^d:S / (2 S:S)) / nu_c, FP64.  Returns (X[nc][7], y[nc],
+    ubar[3][nxc][nyc][nzc]) with coarse cells in Fortran order."""
+    _, ux, uy, uz = macrovar(p, f)
+    nx, ny, nz = ux.shape
+    nxc, nyc, nzc = nx // factor, ny // factor, nz // factor
+
+    def box(a):
+        return a.reshape(nxc, factor, nyc, factor, nzc, factor).mean(axis=(1, 3, 5))
+
+    u = [box(ux), box(uy), box(uz)]
+    uu = {(a, b): box([ux, uy, uz][a] * [ux, uy, uz][b]) for a in range(3) for b in range(a, 3)}
+
+    def grad(v):
+        g = np.empty((3,) + v.shape)
+        ext = np.concatenate([-v[:1], v, -v[-1:]], axis=0)           # no-slip image
+        g[0] = 0.5 * (ext[2:] - ext[:-2])
+        g[1] = 0.5 * (np.roll(v, -1, axis=1) - np.roll(v, 1, axis=1))
+        g[2] = 0.5 * (np.roll(v, -1, axis=2) - np.roll(v, 1, axis=2))
+        return g
+
+    G = [grad(v) for v in u]                                          # G[a][b] = d u_a / d x_b
+    S = np.stack([G[0][0], G[1][1], G[2][2], 0.5 * (G[0][1] + G[1][0]), 0.5 * (G[1][2] + G[2][1]),
+                  0.5 * (G[0][2] + G[2][0])])
+    tau = np.stack([uu[(0, 0)] - u[0] ** 2, uu[(1, 1)] - u[1] ** 2, uu[(2, 2)] - u[2] ** 2,
+                    uu[(0, 1)] - u[0] * u[1], uu[(1, 2)] - u[1] * u[2], uu[(0, 2)] - u[0] * u[2]])
+    t3 = (tau[0] + tau[1] + tau[2]) / 3.0
+    tau[:3] -= t3
+    num = -(tau[0] * S[0] + tau[1] * S[1] + tau[2] * S[2] + 2.0 * (tau[3] * S[3] + tau[4] * S[4] + tau[5] * S[5]))
+    den = 2.0 * (S[0] ** 2 + S[1] ** 2 + S[2] ** 2 + 2.0 * (S[3] ** 2 + S[4] ** 2 + S[5] ** 2))
+    nut = np.where(den > 0, np.maximum(num / np.where(den > 0, den, 1.0), 0.0), 0.0)
+    nu_c = (1.0 / p.s9 - 0.5) / 3.0 / factor
+    dwall = np.minimum(np.arange(nxc) + 0.5, nxc - np.arange(nxc) - 0.5)[:, None, None]
+    X = closure_features(S, dwall, nu_c, ustar, h / factor)
+    X = np.stack([X[..., k].ravel(order="F") for k in range(7)], axis=1)
+    return X, (nut / nu_c).ravel(order="F"), np.stack(u)

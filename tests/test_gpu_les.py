@@ -101,3 +101,76 @@ def test_mlp_training_fits_a_smooth_target(pkg, orc, fp32):
     # the GPU's weights reproduce the loss in the oracle
     lo, _ = orc.mlp_loss_grad(p.astype(np.float64), norm.astype(np.float64), X, y)
     assert abs(lo - l1) < 1e-3 * max(lo, 1e-12) + 1e-7
+
+
+def closure_net(orc, seed=0):
+    rng = np.random.default_rng(seed)
+    p = rng.normal(0, 0.2, orc.MLP_PARAMS).astype(np.float32)
+    p[-1] = 0.5                                       # b3: nu_t / nu around softplus(0.5)
+    norm = np.concatenate([rng.normal(0, 0.3, 7), rng.uniform(0.5, 2.0, 7)]).astype(np.float32)
+    return p, norm
+
+
+def les_case(pkg, orc, shape=(10, 12, 8), precision="fp64"):
+    nx, ny, nz = shape
+    run = pkg.RunParams(nx=nx, ny=ny, nz=nz, visc=0.01, force_y=1e-5, mrt_type=1,
+                        precision=pkg.PRECISIONS[precision])
+    p = orc.params_from(run)
+    f0 = orc.run(p, random_f(orc, shape, seed=6), 2)[0]   # with a non-equilibrium part
+    return run, p, f0
+
+
+def test_les_closure_steps_match_oracle(pkg, orc):
+    """Two steps (both AA parities) of the coarse LES with the closure fused
+    into the collision: populations and nu_t against the FP64 oracle (the GPU
+    evaluates features and network in FP32)."""
+    run, p, f0 = les_case(pkg, orc)
+    params, norm = closure_net(orc)
+    ustar, h = 0.005, 5.0
+    s9 = np.full(f0.shape[1:], p.s9)
+    fo = f0
+    for _ in range(2):
+        fo, s9 = orc.les_step(p, fo, s9, params.astype(np.float64), norm.astype(np.float64), ustar, h)
+    nu = (1.0 / p.s9 - 0.5) / 3.0
+    nut_o = (1.0 / s9 - 0.5) / 3.0 / nu - 1.0
+    with pkg.Lattice(run) as lat:
+        lat.upload_f(f0)
+        lat.les_set(params, norm, ustar, h)
+        lat.step(2)
+        g = lat.download_f()
+        nut = lat.les_nut()
+    assert nut_o.min() > 0.1                          # the closure acts
+    assert rel(nut, nut_o) < 1e-4
+    assert rel(g - f0, fo - f0) < 1e-5
+
+
+def test_les_closure_off_is_plain_mrt(pkg, orc):
+    """A network with nu_t ~ 0 reproduces the plain MRT step; les_set(None)
+    switches back."""
+    run, p, f0 = les_case(pkg, orc, shape=(9, 10, 7))
+    params, norm = closure_net(orc, seed=1)
+    params[orc.MLP_PARAMS - 33:orc.MLP_PARAMS - 1] = 0.0   # w3 = 0
+    params[-1] = -40.0                                     # b3: nu_t / nu = softplus(-40) ~ 4e-18
+    fo = orc.run(p, f0, 3)[0]
+    with pkg.Lattice(run) as lat:
+        lat.upload_f(f0)
+        lat.les_set(params, norm, 0.005, 5.0)
+        lat.step(2)
+        lat.les_set(None)
+        lat.step(1)
+        g = lat.download_f()
+    assert rel(g, fo) < 1e-12
+
+
+def test_closure_training_data_matches_oracle(pkg, orc):
+    shape = (16, 12, 8)
+    run, p, f0 = les_case(pkg, orc, shape=shape)
+    f3 = orc.run(p, f0, 3)[0]
+    Xo, yo, ubo = orc.closure_training_data(p, f3, 2, 0.005, 8.0)
+    with pkg.Lattice(run) as lat:
+        lat.upload_f(f0)
+        lat.step(3)
+        X, y, ub = lat.les_training_data(2, 0.005, 8.0)
+    assert rel(ub, ubo) < 1e-12
+    assert np.abs(X - Xo).max() < 1e-4 * max(1.0, np.abs(Xo).max())
+    assert np.abs(y - yo).max() < 1e-4 * max(np.abs(yo).max(), 1.0)

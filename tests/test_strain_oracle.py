@@ -36,3 +36,18 @@ def test_strain_zero_at_equilibrium(orc):
     # equilibrium populations carry no non-equilibrium part (up to the F/2 of
     # a zero force) -- both measures vanish to rounding
     assert np.abs(m1).max() < 1e-24 and np.abs(m2).max() < 1e-24
+
+
+def test_laminar_flow_has_no_subgrid_viscosity(orc):
+    """Box filtering a flow that varies only across the channel leaves a
+    subgrid stress with no shear component, so the target eddy viscosity of
+    the closure is zero."""
+    nx, ny, nz = 16, 8, 8
+    visc, g = 0.1, 1e-5
+    p = orc.params(stable_rates(visc), (0.0, g, 0.0))
+    zero = np.zeros((nx, ny, nz), order="F")
+    f = orc.run(p, orc.initpop(zero, zero, zero), 3000)[0]
+    X, y, ub = orc.closure_training_data(p, f, 4, 0.005, 8.0)
+    assert X.shape == (4 * 2 * 2, 7) and np.isfinite(X).all()
+    assert np.abs(y).max() < 1e-10
+    assert np.abs(ub[1]).max() > 0.01 * g / visc
