@@ -11,6 +11,16 @@ reference's drop-in interface for the hot path:
   (collision_MRT + collisionExchnge + macrovar, collision.f90:24-463),
   ``prerelax`` (main.f90:69-90), ``macrovar``, ``diag`` and ``profiles``
   (saveload.f90:1202-1676), ``save_flow``/``load_flow`` (saveload.f90:102-332);
+* ``Lattice.set_particles``/``particles``: moving solid spheres (interpolated
+  bounce-back, momentum exchange, refilling, Newton-Euler) run after every
+  step; the reference declares their data (var_inc.f90:120-150) without the
+  algorithm, which is this project's own;
+* ``Lattice.strain``: S_ij S_ij from the non-equilibrium populations, both
+  methods of sijstat01 (saveload.f90:2320-2432);
+* :class:`ClosureNet` and ``Lattice.les_set``/``les_training_data``: the
+  learned LES closure (no reference counterpart) -- a per-node eddy-viscosity
+  network trained on the GPU on box-filtered DNS and fused into the collision
+  of a coarse-grid LES; ``les_closure.py`` runs it end to end;
 * :data:`CHANNEL_CONFIGS` holds the benchmark channel workloads.
 
 Arrays use the reference layout: populations ``f(0:18, nx, ny, nz)`` and
@@ -52,6 +62,7 @@ EXPORTS = (
     "lbm_timing_enable", "lbm_timing_get", "lbm_strain",
     "lbm_mlp_create", "lbm_mlp_destroy", "lbm_mlp_get", "lbm_mlp_set", "lbm_mlp_set_data", "lbm_mlp_train",
     "lbm_mlp_gradient", "lbm_mlp_predict", "lbm_les_set", "lbm_les_nut", "lbm_les_training_data",
+    "lbm_les_features",
 )
 
 
@@ -146,6 +157,7 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
         "lbm_mlp_predict": (ctypes.c_int, [ctx, fp, ctypes.c_int64, fp]),
         "lbm_les_set": (ctypes.c_int, [ctx, fp, fp, ctypes.c_double, ctypes.c_double]),
         "lbm_les_nut": (ctypes.c_int, [ctx, dp]),
+        "lbm_les_features": (ctypes.c_int, [ctx, ctypes.c_double, ctypes.c_double, fp]),
         "lbm_les_training_data": (ctypes.c_int, [ctx, ctypes.c_int32, ctypes.c_double, ctypes.c_double, fp, fp, dp]),
         "lbm_diag": (ctypes.c_int, [ctx, ctypes.POINTER(LBMStats)]),
         "lbm_profiles": (ctypes.c_int, [ctx, dp]),
@@ -518,6 +530,12 @@ class Lattice:
         ub = np.empty((3, nc), dtype=np.float64)
         self._call("lbm_les_training_data", factor, ustar, h, _fptr(X), _fptr(y), _dptr(ub))
         return X, y, ub.reshape(3, nzc, nyc, nxc).transpose(0, 3, 2, 1)
+
+    def les_features(self, ustar: float, h: float) -> np.ndarray:
+        """The closure's features per node, X[n][7], nodes in Fortran order."""
+        X = np.empty((int(np.prod(self.shape)), MLP_IN), dtype=np.float32)
+        self._call("lbm_les_features", ustar, h, _fptr(X))
+        return X
 
     def les_nut(self) -> np.ndarray:
         out = np.empty(self.shape, dtype=np.float64, order="F")

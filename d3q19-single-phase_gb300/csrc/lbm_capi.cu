@@ -666,6 +666,19 @@ int lbm_les_training_data(lbm_ctx* c, int32_t factor, double ustar, double h, fl
     return sync(c);
 }
 
+int lbm_les_features(lbm_ctx* c, double ustar, double h, float* X) {
+    if (check_ctx(c) || !X || !(ustar > 0.0) || !(h > 0.0)) return fail(LBM_ERR_INVALID_ARG, "bad argument");
+    if (int rc = set_device(c)) return rc;
+    float* d = nullptr;
+    CK(cudaMalloc(&d, c->s.N * LBM_MLP_IN * sizeof(float)));
+    cudaError_t e = launch_les_features(c->s, c->parity, (float)ustar, (float)h, d, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(X, d, c->s.N * LBM_MLP_IN * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(LBM_ERR_CUDA, std::string("closure features: ") + cudaGetErrorString(e));
+    return sync(c);
+}
+
 int lbm_les_nut(lbm_ctx* c, double* nut) {
     if (check_ctx(c) || !nut) return fail(LBM_ERR_INVALID_ARG, "null argument");
     if (!c->s.les_w) return fail(LBM_ERR_STATE, "the LES closure is off (lbm_les_set)");

@@ -355,6 +355,32 @@ __global__ void k_closure_targets(const double* __restrict__ F9, int nxc, int ny
     y[o] = (float)(nut / nu_c);
 }
 
+// Features of the closure from the populations of this lattice: the strain
+// from the non-equilibrium moments (with the per-node shear rate of the last
+// closure collision, or the molecular s9), as the fused LES collision computes
+// them; X[n][7] with n in the reference layout (ix fastest).
+template <typename T>
+__global__ void k_les_features(DeviceState s, int parity, float ustar, float h, float* __restrict__ X, int z0) {
+    const RefNode r = ref_node(s.g, z0);
+    if (!r.ok) return;
+    double f[Q];
+    gather_natural<T>(s, parity, r.iy, r.iz, r.ix, f);
+    const double F[3] = {(double)s.cd.Fx, (double)s.cd.Fy, (double)s.cd.Fz};
+    double rho, ux, uy, uz;
+    macro_of<double>(f, F, rho, ux, uy, uz);
+    const uint32_t n = gpu_lin(s.g, r.ix, r.iy, r.iz);
+    const double s9 = s.les_w ? (double)s.les_s9[n] : (double)s.cd.kp * 36.0;
+    const double nu = (1.0 / ((double)s.cd.kp * 36.0) - 0.5) / 3.0;
+    double S6[6];
+    strain_from_moments(f, rho, ux, uy, uz, (double)s.cd.ke * 2394.0, s9, S6);
+    float Sf[6], x[kMlpIn];
+    for (int k = 0; k < 6; ++k) Sf[k] = (float)S6[k];
+    const float dwall = fminf((float)r.ix + 0.5f, (float)s.g.NZ - (float)r.ix - 0.5f);
+    closure_features(Sf, dwall, (float)nu, ustar, h, x);
+    const size_t o = (size_t)r.ix + (size_t)s.g.NZ * ((size_t)r.iy + (size_t)s.g.NX * (size_t)r.iz);
+    for (int k = 0; k < kMlpIn; ++k) X[o * kMlpIn + k] = x[k];
+}
+
 __global__ void k_ref_to_gpu_vec(Geometry g, size_t N, const double* __restrict__ ux,
                                  const double* __restrict__ uy, const double* __restrict__ uz,
                                  double* __restrict__ uf, int z0) {
@@ -545,6 +571,11 @@ cudaError_t launch_closure_targets(const double* F9, int nxc, int nyc, int nzc, 
     const dim3 grid((nxc + bx - 1) / bx, nyc, nzc);
     k_closure_targets<<<grid, bx, 0, st>>>(F9, nxc, nyc, nzc, nu_c, ustar, h_c, X, y);
     return cudaGetLastError();
+}
+
+cudaError_t launch_les_features(const DeviceState& s, int parity, float ustar, float h, float* X,
+                                cudaStream_t st) {
+    LBM_DISPATCH(s.prec, (k_les_features<T><<<ref_grid(s.g, s.g.NY, kBx), kBx, 0, st>>>(s, parity, ustar, h, X, 0)))
 }
 
 cudaError_t launch_ref_to_gpu_vec(const DeviceState& s, const double* ux, const double* uy,

@@ -128,6 +128,8 @@ cudaError_t launch_box_filter(const DeviceState& s, int parity, int factor, int 
                               double* out, cudaStream_t st);
 cudaError_t launch_closure_targets(const double* F9, int nxc, int nyc, int nzc, float nu_c, float ustar,
                                    float h_c, float* X, float* y, cudaStream_t st);
+cudaError_t launch_les_features(const DeviceState& s, int parity, float ustar, float h, float* X,
+                                cudaStream_t st);
 cudaError_t launch_ref_to_gpu_vec(const DeviceState& s, const double* ux,
                                   const double* uy, const double* uz,
                                   double* uf, int z0, int nzc, cudaStream_t st);

@@ -1,0 +1,264 @@
+"""Learned LES closure, end to end, on one GPU.
+
+Configuration c3 of the benchmark set: a particle-free DNS of the channel
+(512 x 256 x 256, Re_tau ~ 181, FP32) gives snapshots every 500 steps; each is
+box-filtered by 4 onto 128 x 64 x 64 (and, as a second case, by 8), and the
+library builds the closure's training pairs (features of the filtered strain,
+target eddy viscosity from the subgrid stress).  The network is trained with
+the library's own kernels (forward, backward, Adam; BF16 tensor-core
+products).  A coarse MRT LES with the network fused into the collision then
+starts from the last filtered snapshot, and plain MRT on the same coarse grid
+from the same state, while the DNS continues from that state over the same
+physical time; the mean streamwise profiles averaged over the second half of
+that window are compared (the DNS profile box-averaged to the coarse cells).
+
+Grids are named as in the benchmark (streamwise x spanwise x wall-normal);
+the library's reference axes are (wall-normal nx, streamwise ny, spanwise nz).
+The coarse grid uses acoustic scaling: the lattice velocity and u* stay, the
+spacing and the time step grow by the filter width, so nu_c = nu / 4 and
+h_c = h / 4.
+
+    python d3q19-single-phase_gb300/les_closure.py --out <dir> [--spinup N]
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+PKG_DIR = Path(__file__).resolve().parent
+if str(PKG_DIR.parent) not in sys.path:
+    sys.path.insert(0, str(PKG_DIR.parent))
+pkg = importlib.import_module(PKG_DIR.name)
+
+
+def trigger_velocity(nx, ny, nz, h, u0, amp, seed):
+    """Initial velocity that becomes turbulent: a parabolic mean profile with
+    centreline u0, streamwise vortices and streaks of spanwise wavelength nz/4
+    (~90 wall units at Re_tau 181) and seeded uniform noise of +-amp*u0.
+    Reference axes and layout (x wall-normal, Fortran order)."""
+    eta = (np.arange(nx) + 0.5) / h - 1.0
+    ys = np.arange(ny)
+    zs = np.arange(nz)
+    beta = 2 * np.pi * 4 / nz
+    alpha = 2 * np.pi * 2 / ny
+    E, Y, Z = np.meshgrid(eta, ys, zs, indexing="ij")
+    a = 0.15 * u0
+    ux = a * (1 - E**2) ** 2 * np.cos(beta * Z) * (1 + 0.3 * np.sin(alpha * Y))
+    uz = 4 * a * E * (1 - E**2) * np.sin(beta * Z) / (beta * h)
+    uy = u0 * (1 - E**2) + 0.3 * u0 * (1 - E**2) * np.cos(beta * Z) * np.cos(alpha * Y)
+    rng = np.random.default_rng(seed)
+    for u in (ux, uy, uz):
+        u += amp * u0 * rng.uniform(-1.0, 1.0, u.shape) * (1 - E**2)
+    return [np.asfortranarray(u) for u in (ux, uy, uz)]
+
+
+def mean_profile(lat, ustar):
+    """Plane-averaged streamwise velocity over the fluid nodes, lattice units."""
+    return pkg.statistics(lat.profiles(), ustar)["mean"][:, 1] * ustar
+
+
+def les_run(params, norm, ub, cfg, steps, sample_every, closure):
+    """Coarse LES from the filtered velocity ub (reference axes).  Returns
+    (time-averaged mean u_stream(x), ms per step, failure step or None,
+    mean nu_t/nu profile or None)."""
+    nxc, nyc, nzc = ub.shape[1:]
+    run = pkg.RunParams(nx=nxc, ny=nyc, nz=nzc, visc=cfg["visc"] / cfg["factor"],
+                        force_y=cfg["ustar"] ** 2 / (cfg["h"] / cfg["factor"]), mrt_type=pkg.MRT_STABLE,
+                        precision=pkg.PRECISIONS["fp32"])
+    prof = np.zeros(nxc)
+    nsamp = 0
+    fail = None
+    nut = None
+    with pkg.Lattice(run) as lat:
+        lat.initpop(*[np.asfortranarray(u) for u in ub])
+        if closure:
+            lat.les_set(params, norm, cfg["ustar"], cfg["h"] / cfg["factor"])
+        t0 = time.perf_counter()
+        done = 0
+        while done < steps:
+            k = min(sample_every, steps - done)
+            try:
+                lat.step(k)
+            except pkg.LBMError as e:
+                fail = done + k
+                break
+            done += k
+            d = lat.diag()
+            if d.nonfinite or not np.isfinite(d.vmax) or d.vmax > 0.3:
+                fail = done
+                break
+            if done > steps // 2:
+                prof += mean_profile(lat, cfg["ustar"])
+                nsamp += 1
+        ms = (time.perf_counter() - t0) * 1e3 / max(done, 1)
+        if closure and fail is None:
+            nut = lat.les_nut().mean(axis=(1, 2))
+    return (prof / max(nsamp, 1) if nsamp else None), ms, fail, nut
+
+
+def box_profile(prof, factor):
+    """A wall-normal profile averaged over consecutive groups of `factor`
+    nodes: the plane average of the box-filtered field."""
+    return prof.reshape(-1, factor).mean(axis=1)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", type=Path, required=True)
+    ap.add_argument("--grid", type=int, nargs=3, default=(512, 256, 256), help="DNS streamwise, spanwise, wall-normal")
+    ap.add_argument("--spinup", type=int, default=300000)
+    ap.add_argument("--snapshots", type=int, default=20)
+    ap.add_argument("--every", type=int, default=500)
+    ap.add_argument("--factors", type=int, nargs="+", default=(4, 8))
+    ap.add_argument("--train-steps", type=int, default=3000)
+    ap.add_argument("--window", type=int, default=80000, help="fine steps of the compared time window")
+    ap.add_argument("--seed", type=int, default=20240611)
+    ap.add_argument("--features", choices=("fd", "lattice"), default="fd",
+                    help="training features from finite differences of the filtered velocity (default: "
+                         "held-out explained variance 0.67 at filter 4) or from a coarse lattice seeded "
+                         "with the filtered snapshot, the inference path (0.23)")
+    ap.add_argument("--fixtures", type=Path, default=None, help="write the held-out test fixtures here")
+    args = ap.parse_args()
+    args.out.mkdir(parents=True, exist_ok=True)
+    stream, span, wall = args.grid
+    cfg0 = dict(visc=0.0024, ustar=0.0034, h=wall / 2.0)
+    rep = {"config": {"dns_grid_stream_span_wall": [stream, span, wall], **cfg0, "factors": list(args.factors),
+                      "window_fine_steps": args.window}}
+    log = lambda *a: print(*a, file=sys.stderr, flush=True)
+    sample_fine = 800                                   # profile sampling in the window, fine steps
+
+    # ---- DNS: spin-up, snapshots, and the compared window -------------------------
+    run = pkg.RunParams(nx=wall, ny=stream, nz=span, visc=cfg0["visc"], force_y=cfg0["ustar"] ** 2 / cfg0["h"],
+                        mrt_type=pkg.MRT_STABLE, precision=pkg.PRECISIONS["fp32"])
+    data = {f: ([], []) for f in args.factors}
+    ub0 = {}
+
+    def coarse_run(f):
+        return pkg.RunParams(nx=wall // f, ny=stream // f, nz=span // f, visc=cfg0["visc"] / f,
+                             force_y=cfg0["ustar"] ** 2 / (cfg0["h"] / f), mrt_type=pkg.MRT_STABLE,
+                             precision=pkg.PRECISIONS["fp32"])
+
+    def lattice_features(f, ub):
+        # the features the fused collision sees: a coarse lattice seeded with
+        # the filtered velocity, two plain steps to set up its
+        # non-equilibrium part, then the strain from its moments
+        with pkg.Lattice(coarse_run(f)) as cl:
+            cl.initpop(*[np.asfortranarray(u) for u in ub])
+            cl.step(2)
+            return cl.les_features(cfg0["ustar"], cfg0["h"] / f)
+
+    with pkg.Lattice(run) as lat:
+        lat.initpop(*trigger_velocity(wall, stream, span, cfg0["h"], 18.0 * cfg0["ustar"], 0.05, args.seed))
+        hist = []
+        t0 = time.perf_counter()
+        done = 0
+        while done < args.spinup:
+            k = min(20000, args.spinup - done)
+            lat.step(k)
+            done += k
+            st = pkg.statistics(lat.profiles(), cfg0["ustar"])
+            # Reynolds shear stress (units of u*^2) and centreline velocity (units of u*)
+            hist.append([done, float(np.abs(st["stress"][:, 1]).max()), float(st["mean"][:, 1].max())])
+            log(f"[dns] step {done}: |uv|/u*^2 max {hist[-1][1]:.3f}, centreline/u* {hist[-1][2]:.2f}")
+        dns_ms = (time.perf_counter() - t0) * 1e3 / max(done, 1)
+        rep["dns"] = {"spinup_steps": done, "ms_per_step": dns_ms, "history": hist}
+        for s in range(args.snapshots):
+            lat.step(args.every)
+            for f in args.factors:
+                X, y, ub = lat.les_training_data(f, cfg0["ustar"], cfg0["h"])
+                if args.features == "lattice":
+                    X = lattice_features(f, ub)
+                data[f][0].append(X)
+                data[f][1].append(y)
+                ub0[f] = ub
+        # the LES runs start from this state (the last snapshot); the DNS
+        # continues over the same physical time for the comparison
+        prof = np.zeros(wall)
+        nsamp = 0
+        done = 0
+        while done < args.window:
+            lat.step(sample_fine)
+            done += sample_fine
+            if done > args.window // 2:
+                prof += mean_profile(lat, cfg0["ustar"])
+                nsamp += 1
+        prof_dns = prof / nsamp
+        st = pkg.statistics(lat.profiles(), cfg0["ustar"])
+        rep["dns"]["final_stress_max_over_ustar2"] = float(np.abs(st["stress"][:, 1]).max())
+        rep["dns"]["final_centreline_over_ustar"] = float(st["mean"][:, 1].max())
+        rep["dns"]["window_profile"] = prof_dns.tolist()
+
+    rep["factors"] = {}
+    for f in args.factors:
+        cfg = dict(cfg0, factor=f)
+        # the last snapshot is held out of training
+        X = np.concatenate(data[f][0][:-1])
+        y = np.concatenate(data[f][1][:-1])
+        Xh, yh = data[f][0][-1], data[f][1][-1]
+        clip = float(np.quantile(y, 0.995))
+        y = np.minimum(y, clip)
+        yh = np.minimum(yh, clip)
+        out = {"data": {"samples": int(len(y)), "held_out": int(len(yh)), "target_mean": float(y.mean()),
+                        "target_clip": clip, "target_zero_fraction": float((y == 0).mean()),
+                        "features": args.features}}
+        # ---- training --------------------------------------------------------------
+        with pkg.ClosureNet(seed=args.seed + f) as net:
+            net.set_data(X, y)
+            t0 = time.perf_counter()
+            losses = net.train(args.train_steps, batch=65536, lr=1e-3)
+            train_s = time.perf_counter() - t0
+            loss_full, _ = net.gradient()
+            params, norm = net.get()
+            pred = net.predict(X[: 1 << 20])
+            ph = net.predict(Xh)
+        mse_h = float(np.mean((ph - yh) ** 2))
+        out["training"] = {"steps": args.train_steps, "batch": 65536, "lr": 1e-3, "seconds": train_s,
+                           "loss_first": float(losses[0]), "loss_last": float(losses[-1]),
+                           "loss_full_set": loss_full, "target_variance": float(y.var()),
+                           "explained_variance": float(1.0 - loss_full / max(float(y.var()), 1e-30)),
+                           "prediction_mean": float(pred.mean()),
+                           "held_out_mse": mse_h, "held_out_mse_no_model": float(np.mean(yh**2)),
+                           "held_out_mse_mean_predictor": float(np.mean((yh - y.mean()) ** 2))}
+        np.savez(args.out / f"closure_weights_f{f}.npz", params=params, norm=norm)
+        # ---- coarse LES with and without the closure, same window as the DNS --------
+        ref = box_profile(prof_dns, f)
+        res = {}
+        for name, closure in (("closure", True), ("plain_mrt", False)):
+            p_les, ms, fail, nut = les_run(params, norm, ub0[f], cfg, args.window // f, max(sample_fine // f, 1),
+                                           closure)
+            err = None if p_les is None else float(np.abs(p_les - ref).max() / np.abs(ref).max())
+            res[name] = {"mean_profile_rel_err": err, "ms_per_step": ms, "failed_at_step": fail,
+                         "profile": None if p_les is None else p_les.tolist(),
+                         "nut_over_nu_profile": None if nut is None else nut.tolist()}
+            log(f"[les x{f}] {name}: err {err}, {ms:.3f} ms/step, failed at {fail}")
+        out["les"] = res
+        out["les_steps"] = args.window // f
+        out["filtered_dns_profile"] = ref.tolist()
+        # GPU time for the same physical time: one coarse step = f fine steps
+        out["gpu_time_ratio_dns_over_les"] = (dns_ms * f) / res["closure"]["ms_per_step"]
+        rep["factors"][str(f)] = out
+        if args.fixtures is not None:
+            args.fixtures.mkdir(parents=True, exist_ok=True)
+            pick = np.random.default_rng(args.seed).choice(len(yh), min(4096, len(yh)), replace=False)
+            np.savez_compressed(
+                args.fixtures / f"closure_channel_{stream}x{span}x{wall}_filter{f}.npz",
+                params=params, norm=norm, X_held=Xh[pick], y_held=yh[pick].astype(np.float32),
+                target_mean=np.float32(y.mean()), dns_window_profile=ref,
+                les_closure_profile=np.array(res["closure"]["profile"] or []),
+                les_plain_profile=np.array(res["plain_mrt"]["profile"] or []),
+                ustar=cfg0["ustar"], h_coarse=cfg0["h"] / f, visc_coarse=cfg0["visc"] / f,
+                grid_coarse=np.array([wall // f, stream // f, span // f]))
+        print(json.dumps({"factor": f, **{k: out[k] for k in ("data", "training", "gpu_time_ratio_dns_over_les")},
+                          "les": {k: {kk: vv for kk, vv in v.items() if kk not in ("profile", "nut_over_nu_profile")}
+                                  for k, v in res.items()}}), flush=True)
+    (args.out / "report.json").write_text(json.dumps(rep, indent=1))
+
+
+if __name__ == "__main__":
+    main()

@@ -332,6 +332,11 @@ int lbm_les_set(lbm_ctx* ctx, const float* params, const float* norm, double ust
 /* nu_t / nu of the last collision per node (host, nx*ny*nz doubles, reference
  * layout). */
 int lbm_les_nut(lbm_ctx* ctx, double* nut);
+/* The closure's 7 features per node from this lattice's populations, as the
+ * fused collision computes them (strain from the non-equilibrium moments with
+ * the node's last closure rate, or the molecular s9 when the closure is off).
+ * X[n][7] FP32 host, nodes in the reference layout. */
+int lbm_les_features(lbm_ctx* ctx, double ustar, double h, float* X);
 /* Training data of the closure from a fine (DNS) lattice of this context: box
  * filter by `factor` (dividing nx, ny, nz) of u and u_i u_j; on the coarse
  * grid the strain of the filtered velocity (central differences, no-slip

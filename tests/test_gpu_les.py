@@ -174,3 +174,20 @@ def test_closure_training_data_matches_oracle(pkg, orc):
     assert rel(ub, ubo) < 1e-12
     assert np.abs(X - Xo).max() < 1e-4 * max(1.0, np.abs(Xo).max())
     assert np.abs(y - yo).max() < 1e-4 * max(np.abs(yo).max(), 1.0)
+
+
+def test_les_features_match_oracle(pkg, orc):
+    run, p, f0 = les_case(pkg, orc, shape=(10, 12, 8))
+    f3 = orc.run(p, f0, 3)[0]
+    r = run.rates()
+    nu = (1.0 / r["s9"] - 0.5) / 3.0
+    S = orc.strain_tensor(p, f3, r["s1"], r["s9"])
+    nx = f3.shape[1]
+    dwall = np.minimum(np.arange(nx) + 0.5, nx - np.arange(nx) - 0.5)[:, None, None]
+    Xo = orc.closure_features(S, dwall, nu, 0.005, 5.0)
+    Xo = np.stack([Xo[..., k].ravel(order="F") for k in range(7)], axis=1)
+    with pkg.Lattice(run) as lat:
+        lat.upload_f(f0)
+        lat.step(3)
+        X = lat.les_features(0.005, 5.0)
+    assert np.abs(X - Xo).max() < 1e-4 * max(1.0, np.abs(Xo).max())
