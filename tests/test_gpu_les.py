@@ -1,7 +1,11 @@
-"""GPU parity of the learned-closure path: strain from the non-equilibrium
-populations (both methods of sijstat01), through the C ABI, against the FP64
-oracle."""
+"""GPU checks of the learned-closure path through the C ABI: strain from the
+non-equilibrium populations (both methods of sijstat01), the closure network
+(gradients, prediction, training), the LES step with the closure fused into
+the collision and the training-data builder against the FP64 oracle; the
+committed trained networks on held-out data and in a coarse LES."""
 from __future__ import annotations
+
+from pathlib import Path
 
 import numpy as np
 import pytest
@@ -191,3 +195,50 @@ def test_les_features_match_oracle(pkg, orc):
         lat.step(3)
         X = lat.les_features(0.005, 5.0)
     assert np.abs(X - Xo).max() < 1e-4 * max(1.0, np.abs(Xo).max())
+
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+@pytest.mark.parametrize("factor", [4, 8])
+def test_trained_closure_beats_no_model_on_held_out_data(pkg, factor):
+    """The committed networks (tests/golden/closure_channel_*.npz, written by
+    les_closure.py from the 512x256x256 channel DNS, the last snapshot held out
+    of training) predict the held-out subgrid eddy viscosity better than no
+    model and better than the training mean, and never negative."""
+    d = np.load(GOLDEN / f"closure_channel_512x256x256_filter{factor}.npz")
+    with pkg.ClosureNet() as net:
+        net.set(d["params"], d["norm"])
+        pred = net.predict(d["X_held"])
+    y = d["y_held"].astype(np.float64)
+    mse = float(np.mean((pred - y) ** 2))
+    assert (pred >= 0).all()
+    assert mse < 0.6 * float(np.mean(y**2))
+    assert mse < 0.8 * float(np.mean((y - float(d["target_mean"])) ** 2))
+
+
+def test_trained_closure_runs_a_coarse_les(pkg):
+    """The committed filter-4 network fused into the 128x64x64 LES of the
+    channel: from the filtered DNS mean profile with seeded perturbations it
+    stays finite with 0 <= nu_t and keeps the mean profile close to the DNS
+    one."""
+    d = np.load(GOLDEN / "closure_channel_512x256x256_filter4.npz")
+    nx, ny, nz = (int(v) for v in d["grid_coarse"])
+    run = pkg.RunParams(nx=nx, ny=ny, nz=nz, visc=float(d["visc_coarse"]),
+                        force_y=float(d["ustar"]) ** 2 / float(d["h_coarse"]), mrt_type=pkg.MRT_STABLE,
+                        precision=pkg.PRECISIONS["fp32"])
+    prof = d["dns_window_profile"]
+    rng = np.random.default_rng(3)
+    ux = 0.05 * prof.max() * rng.uniform(-1, 1, (nx, ny, nz))
+    uy = np.broadcast_to(prof[:, None, None], (nx, ny, nz)) * (1 + 0.05 * rng.uniform(-1, 1, (nx, ny, nz)))
+    uz = 0.05 * prof.max() * rng.uniform(-1, 1, (nx, ny, nz))
+    with pkg.Lattice(run) as lat:
+        lat.initpop(*(np.asfortranarray(u) for u in (ux, uy, uz)))
+        lat.les_set(d["params"], d["norm"], float(d["ustar"]), float(d["h_coarse"]))
+        lat.step(2000)
+        st = lat.diag()
+        nut = lat.les_nut()
+        mean = pkg.statistics(lat.profiles(), float(d["ustar"]))["mean"][:, 1] * float(d["ustar"])
+    assert st.nonfinite == 0
+    assert nut.min() > -1e-4 and 0 < nut.mean() < 1.0          # nu_t from the FP32 rate: round-off only
+    assert np.abs(mean - prof).max() < 0.1 * prof.max()
