@@ -22,6 +22,8 @@ struct lbm_ctx {
     int parity = 0;            // 0: natural orientation, 1: after an even AA step
     int64_t nsteps = 0;
     double* d_stage = nullptr; // FP64 staging for layout conversion
+    double* d_mass = nullptr;  // fluid mass and node count (mean-density removal)
+    int mass_pending = 0;      // a mean-density removal waits for natural orientation
     float* d_les = nullptr;    // closure network parameters + normalisation
     float* d_s9 = nullptr;     // per-node shear rate of the closure
     int use_rows_saved = 0;    // the step kernel choice without the closure
@@ -393,6 +395,7 @@ int lbm_destroy(lbm_ctx* c) {
     cudaFree(c->P.geom);
     cudaFree(c->d_les);
     cudaFree(c->d_s9);
+    cudaFree(c->d_mass);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return LBM_OK;
@@ -488,6 +491,16 @@ int lbm_step_async(lbm_ctx* c, int32_t nsteps) {
         if (c->P.npart > 0) {
             CK(particles_after_step(c->s, c->P, c->parity, c->have_prev, c->stream));
             c->have_prev = 1;
+            // main.f90:163-167: with particles, every 100 steps the mean
+            // density is removed to correct the mass the interpolated
+            // bounce-back loses (avedensity); done at the first step from
+            // there on that leaves the array in natural orientation
+            if (c->nsteps % 100 == 0) c->mass_pending = 1;
+            if (c->mass_pending && c->parity == 0) {
+                CK(launch_remove_mean_density(c->s, c->d_mass, c->stream));
+                CK(launch_remove_mean_apply(c->s, c->d_mass, c->stream));
+                c->mass_pending = 0;
+            }
         }
         if (timed) {
             CK(cudaEventRecord(c->tev[3 * c->tn + 2], c->stream));
@@ -934,6 +947,7 @@ int lbm_particles_set(lbm_ctx* c, const lbm_particle_params* pp, const double* p
     if (!P.owner) CK(cudaMalloc(&P.owner, c->s.N * sizeof(int)));
     if (!P.counters) CK(cudaMalloc(&P.counters, 4 * sizeof(unsigned)));
     if (!c->d_count) CK(cudaMalloc(&c->d_count, sizeof(unsigned long long)));
+    if (!c->d_mass) CK(cudaMalloc(&c->d_mass, 2 * sizeof(double)));
     const int cap = std::max(4096, 64 * n);
     if (P.refill_cap < cap) {
         cudaFree(P.refill_node);

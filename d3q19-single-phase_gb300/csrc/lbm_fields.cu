@@ -1,6 +1,8 @@
 // Non-hot kernels: layout conversion between the reference's AoS FP64 array
 // f(0:18,nx,ny,nz) and the device SoA storage, equilibrium initialisation,
 // macroscopic fields and FP64 reductions for the diagnostics.
+#include <algorithm>
+
 #include "lbm_internal.h"
 #include "lbm_strain.cuh"
 #include "lbm_mlp.cuh"
@@ -502,6 +504,146 @@ __global__ void k_add_rest(DeviceState s, double delta) {
     }
 }
 
+// Fluid mass and fluid node count (acc[0], acc[1]) for the mean-density
+// removal of avedensity (collision.f90:487-513), with the array in natural
+// orientation (every population in its own node's slot).  A thread takes
+// 16 bytes of every plane (8 FP16, 4 FP32 or 2 FP64 nodes); sums per node in
+// the storage's arithmetic type (FP32 for FP32/FP16: GB300's FP64 rate is
+// 1/64 of FP32), FP64 per thread and per block, one atomic pair per block.
+// Nodes beyond the last whole group are summed one by one.
+template <typename T>
+struct Vec16 {
+    static constexpr int N = 16 / (int)sizeof(T);
+    __device__ __forceinline__ static void load(const T* p, float (&v)[16 / sizeof(T)]) {
+        const uint4 w = *reinterpret_cast<const uint4*>(p);
+        if constexpr (sizeof(T) == 2) {
+            const __half2* h = reinterpret_cast<const __half2*>(&w);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) { const float2 f = __half22float2(h[k]); v[2 * k] = f.x; v[2 * k + 1] = f.y; }
+        } else {
+            const float* f = reinterpret_cast<const float*>(&w);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) v[k] = f[k];
+        }
+    }
+    __device__ __forceinline__ static void store(T* p, const float (&v)[16 / sizeof(T)]) {
+        uint4 w;
+        if constexpr (sizeof(T) == 2) {
+            __half2* h = reinterpret_cast<__half2*>(&w);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) h[k] = __floats2half2_rn(v[2 * k], v[2 * k + 1]);
+        } else {
+            float* f = reinterpret_cast<float*>(&w);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) f[k] = v[k];
+        }
+        *reinterpret_cast<uint4*>(p) = w;
+    }
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_fluid_mass(DeviceState s, double* __restrict__ acc) {
+    using R = typename DiagR<T>::type;
+    double m = 0.0, cnt = 0.0;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t t0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if constexpr (sizeof(T) < 8) {
+        constexpr int V = Vec16<T>::N;
+        const size_t groups = s.N / V;
+        for (size_t gidx = t0; gidx < groups; gidx += stride) {
+            const size_t n0 = gidx * V;
+            float r[V];
+#pragma unroll
+            for (int v = 0; v < V; ++v) r[v] = 0.f;
+#pragma unroll
+            for (int i = 0; i < Q; ++i) {
+                float x[V];
+                Vec16<T>::load(pop_plane<T>(s, i) + n0, x);
+#pragma unroll
+                for (int v = 0; v < V; ++v) r[v] += x[v];
+            }
+            float part = 0.f, c = 0.f;
+#pragma unroll
+            for (int v = 0; v < V; ++v)
+                if (!s.owner || s.owner[n0 + v] < 0) { part += r[v]; c += 1.f; }
+            m += (double)part;
+            cnt += (double)c;
+        }
+        for (size_t n = groups * V + t0; n < s.N; n += stride) {
+            if (s.owner && s.owner[n] >= 0) continue;
+            R r = 0;
+#pragma unroll
+            for (int i = 0; i < Q; ++i) r += (R)ld_pop(pop_plane<T>(s, i) + n);
+            m += (double)r;
+            cnt += 1.0;
+        }
+    } else {
+        for (size_t n = t0; n < s.N; n += stride) {
+            if (s.owner && s.owner[n] >= 0) continue;
+            double r = 0.0;
+#pragma unroll
+            for (int i = 0; i < Q; ++i) r += ld_pop(pop_plane<T>(s, i) + n);
+            m += r;
+            cnt += 1.0;
+        }
+    }
+    m *= s.cd.invS;
+    for (int o = 16; o > 0; o >>= 1) {
+        m += __shfl_xor_sync(0xffffffffu, m, o);
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    }
+    __shared__ double sh[2][8];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) { sh[0][w] = m; sh[1][w] = cnt; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) { a += sh[0][k]; b += sh[1][k]; }
+        atomicAdd(acc, a);
+        atomicAdd(acc + 1, b);
+    }
+}
+
+// Remove the mean density acc[0] / acc[1] (w_i * mean from every population),
+// 16 bytes per plane and thread as above.
+template <typename T>
+__global__ void k_remove_mean(DeviceState s, const double* __restrict__ acc) {
+    using R = typename DiagR<T>::type;
+    const R dS = (R)((acc[1] > 0.0 ? -acc[0] / acc[1] : 0.0) * s.cd.S);   // scaled delta
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if constexpr (sizeof(T) < 8) {
+        constexpr int V = Vec16<T>::N;
+        const size_t groups = s.N / V;
+        if (t < groups) {
+#pragma unroll
+            for (int i = 0; i < Q; ++i) {
+                T* p = pop_plane<T>(s, i) + t * V;
+                float x[V];
+                Vec16<T>::load(p, x);
+                const float d = (float)weight(i) * (float)dS;
+#pragma unroll
+                for (int v = 0; v < V; ++v) x[v] += d;
+                Vec16<T>::store(p, x);
+            }
+        } else {
+            const size_t n = groups * V + (t - groups);
+            if (n >= s.N) return;
+#pragma unroll
+            for (int i = 0; i < Q; ++i) {
+                T* p = pop_plane<T>(s, i) + n;
+                st_pop(p, (float)((R)ld_pop(p) + (R)weight(i) * dS));
+            }
+        }
+    } else {
+        if (t >= s.N) return;
+#pragma unroll
+        for (int i = 0; i < Q; ++i) {
+            T* p = pop_plane<T>(s, i) + t;
+            *p = ld_pop(p) + weight(i) * (double)dS;
+        }
+    }
+}
+
 dim3 ref_grid(const Geometry& g, int nzc, int bx) {
     return dim3((g.NX + bx - 1) / bx, g.NZ, nzc);
 }
@@ -604,6 +746,22 @@ cudaError_t launch_add_rest(const DeviceState& s, int parity, double delta, cuda
     (void)parity;
     const unsigned nb = (unsigned)((s.N + 255) / 256);
     LBM_DISPATCH(s.prec, (k_add_rest<T><<<nb, 256, 0, st>>>(s, delta)))
+}
+
+cudaError_t launch_remove_mean_density(const DeviceState& s, double* acc, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(acc, 0, 2 * sizeof(double), st);
+    if (e != cudaSuccess) return e;
+    const unsigned grid = (unsigned)std::max(1, 8 * s.sm_count);
+    LBM_DISPATCH(s.prec, (k_fluid_mass<T><<<grid, 256, 0, st>>>(s, acc)))
+}
+
+cudaError_t launch_remove_mean_apply(const DeviceState& s, const double* acc, cudaStream_t st) {
+    // one thread per 16-byte group plus the remainder nodes (FP16/FP32), one
+    // per node (FP64)
+    const size_t V = s.prec == LBM_PREC_FP64 ? 1 : (s.prec == LBM_PREC_FP32 ? 4 : 8);
+    const size_t threads = V == 1 ? s.N : s.N / V + s.N % V;
+    const unsigned nb = (unsigned)((threads + 255) / 256);
+    LBM_DISPATCH(s.prec, (k_remove_mean<T><<<nb, 256, 0, st>>>(s, acc)))
 }
 
 }  // namespace lbm

@@ -201,3 +201,19 @@ def test_particles_low_precision_follow_fp64(pkg, orc, prec):
     assert res[prec][1].nonfinite == 0
     assert rel(a["vel"], b["vel"]) < (1e-4 if prec == "fp32" else 3e-2)
     assert rel(a["pos"], b["pos"]) < 1e-6
+
+
+def test_mean_density_removed_every_100_steps_with_spheres(pkg, orc):
+    """main.f90:163-167: with particles the mean fluid density is removed
+    every 100 steps (avedensity), so after step 100 it is zero again."""
+    shape = (24, 32, 22)
+    run, f0 = channel_with_spheres(orc, pkg, shape, POS)
+    with pkg.Lattice(run) as lat:
+        lat.upload_f(f0)
+        lat.set_particles(POS, radius=4.0, rho_ratio=2.0, vel=VEL)
+        lat.step(99)
+        d99 = lat.diag()
+        lat.step(1)
+        d100 = lat.diag()
+    assert abs(d99.rho_sum / d99.nfluid) > 1e-9
+    assert abs(d100.rho_sum / d100.nfluid) < 1e-13
