@@ -453,7 +453,7 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=1000)
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
-    ap.add_argument("--config", default="c4")
+    ap.add_argument("--config", default="spheres-1024x512x512")
     ap.add_argument("--precision", choices=tuple(BYTES), default=None)
     ap.add_argument("--accuracy-steps", type=int, default=100)
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU work for the CPU baseline")

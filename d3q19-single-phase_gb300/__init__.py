@@ -392,15 +392,15 @@ class ChannelConfig:
 
 CHANNEL_CONFIGS = {
     # plain turbulent channel, Re_tau ~ 93
-    "c0": ChannelConfig("c0-channel-128x64x64", 128, 64, 64, visc=0.0012, ustar=0.0035, h=32, steps=2000),
+    "channel-128x64x64": ChannelConfig("channel-128x64x64", 128, 64, 64, visc=0.0012, ustar=0.0035, h=32, steps=2000),
     # particle-laden channel, Re_tau ~ 181 (fluid part)
-    "c1": ChannelConfig("c1-particles-256x128x128", 256, 128, 128, visc=0.0012, ustar=0.0034, h=64,
+    "spheres-256x128x128": ChannelConfig("spheres-256x128x128", 256, 128, 128, visc=0.0012, ustar=0.0034, h=64,
                         steps=5000, spheres=256, radius=4.0, s16=1.2),
     # precision sweep, Re_tau ~ 181
-    "c2": ChannelConfig("c2-precision-512x256x256", 512, 256, 256, visc=0.0024, ustar=0.0034, h=128,
+    "spheres-512x256x256": ChannelConfig("spheres-512x256x256", 512, 256, 256, visc=0.0024, ustar=0.0034, h=128,
                         steps=20000, spheres=2048, radius=8.0, s16=1.2),
     # large channel, FP32 compute / FP16 storage, Re_tau ~ 363
-    "c4": ChannelConfig("c4-large-1024x512x512", 1024, 512, 512, visc=0.0024, ustar=0.0034, h=256,
+    "spheres-1024x512x512": ChannelConfig("spheres-1024x512x512", 1024, 512, 512, visc=0.0024, ustar=0.0034, h=256,
                         steps=2000, precision="fp16", spheres=16384, radius=8.0, s16=1.2),
 }
 

@@ -1,6 +1,6 @@
 // Learned LES closure, training side: the eddy-viscosity network
 // (lbm_mlp.cuh) trained on the GPU with hand-written forward, backward and
-// Adam kernels.  The reference has no counterpart (SURVEY row a16).
+// Adam kernels.  The reference has no counterpart.
 //
 // One CTA of 128 threads takes a tile of 128 samples and runs the forward
 // pass, the loss and the backward pass in shared memory; weight gradients go

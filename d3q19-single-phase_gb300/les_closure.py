@@ -1,6 +1,6 @@
 """Learned LES closure, end to end, on one GPU.
 
-Configuration c3 of the benchmark set: a particle-free DNS of the channel
+The closure workload: a particle-free DNS of the channel
 (512 x 256 x 256, Re_tau ~ 181, FP32) gives snapshots every 500 steps; each is
 box-filtered by 4 onto 128 x 64 x 64 (and, as a second case, by 8), and the
 library builds the closure's training pairs (features of the filtered strain,

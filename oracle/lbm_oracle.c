@@ -484,7 +484,7 @@ void orc_channel_velocity(int nx, int ny, int nz, double uc, double amp, uint64_
 /* =========================================================================
  * Moving spheres.  The reference declares links, fill lists and particle
  * state (var_inc.f90:120-150, para.f90:332-379, solid-node velocity in
- * macrovar collision.f90:420-458) but ships no algorithm (SURVEY F5); the
+ * macrovar collision.f90:420-458) but ships no algorithm; the
  * algorithm below is the project's own design, restated on the CPU as the
  * checker of the GPU kernels:
  *   - geometry: node (ix,iy,iz) (0-based) sits at (ix+1/2, iy+1/2, iz+1/2);

@@ -77,7 +77,7 @@ void orc_channel_velocity(int nx, int ny, int nz, double uc, double amp,
                           uint64_t seed, double* ux, double* uy, double* uz);
 
 /* ---- moving spheres (the reference declares the data but ships no
- * algorithm, SURVEY F5; this is the project's own design, restated here as
+ * algorithm; this is the project's own design, restated here as
  * the checker of the GPU kernels) ---------------------------------------- */
 typedef struct orc_particles {
     int npart;

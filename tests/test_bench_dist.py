@@ -51,7 +51,7 @@ def test_dist_setup_barrier_and_max_over_ranks():
 def test_reference_arm_under_torchrun_prints_one_line():
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(free_port()), str(REPO / "bench.py"),
-           "--impl", "reference", "--config", "c0", "--steps", "1", "--warmup", "3", "--cpu-budget", "1"]
+           "--impl", "reference", "--config", "channel-128x64x64", "--steps", "1", "--warmup", "3", "--cpu-budget", "1"]
     env = dict(os.environ, OMP_NUM_THREADS="2")
     p = subprocess.run(cmd, capture_output=True, text=True, timeout=300, cwd=REPO, env=env)
     assert p.returncode == 0, p.stderr[-2000:]

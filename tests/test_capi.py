@@ -84,10 +84,10 @@ def test_channel_velocity_host_copy_matches_oracle(pkg, orc):
 
 
 def test_channel_configs(pkg):
-    c0 = pkg.CHANNEL_CONFIGS["c0"]
-    assert (c0.wall, c0.stream, c0.span) == (64, 128, 64)
-    assert c0.force == pytest.approx(0.0035**2 / 32)
-    p = c0.params()
+    ch = pkg.CHANNEL_CONFIGS["channel-128x64x64"]
+    assert (ch.wall, ch.stream, ch.span) == (64, 128, 64)
+    assert ch.force == pytest.approx(0.0035**2 / 32)
+    p = ch.params()
     assert (p.nx, p.ny, p.nz) == (64, 128, 64)
-    c4 = pkg.CHANNEL_CONFIGS["c4"]
-    assert c4.nodes == 1024 * 512 * 512 and c4.precision == "fp16"
+    big = pkg.CHANNEL_CONFIGS["spheres-1024x512x512"]
+    assert big.nodes == 1024 * 512 * 512 and big.precision == "fp16"

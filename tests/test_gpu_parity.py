@@ -3,7 +3,7 @@ oracle and the committed golden fixtures.
 
 Tolerances
   FP64 storage + arithmetic: relative L-infinity <= 1e-10 in f, rho and u after
-    100 steps (the spec bar); the kernels reorder the same FP64
+    100 steps (the parity bar of the FP64 path); the kernels reorder the same FP64
     arithmetic, so the observed gap is ~1e-14.
   FP32 and FP16 storage (FP32 arithmetic): checked against FP64 through the
     mean profile and bounded population errors, see test_precision_*.
@@ -105,18 +105,18 @@ def test_golden_fixture(pkg):
 
 
 def test_config0_fp64_parity_100_steps(pkg, orc):
-    """Plain turbulent channel 128 x 64 x 64 (c0), seeded Poiseuille + 5 %
+    """Plain turbulent channel 128 x 64 x 64 (ch), seeded Poiseuille + 5 %
     noise, 100 steps: relative L-inf <= 1e-10 in f, rho and u."""
-    c0 = pkg.CHANNEL_CONFIGS["c0"]
-    run = c0.params("fp64")
+    ch = pkg.CHANNEL_CONFIGS["channel-128x64x64"]
+    run = ch.params("fp64")
     shape = (run.nx, run.ny, run.nz)
-    u = orc.channel_velocity(*shape, c0.uc, c0.amp, c0.seed)
+    u = orc.channel_velocity(*shape, ch.uc, ch.amp, ch.seed)
     f0 = orc.initpop(*u)
     p = orc.params_from(run)
     fo = orc.run_omp(p, np.array(f0, order="F", copy=True), 100, orc.max_threads())
     rho, ux, uy, uz = orc.macrovar(p, fo)
     with pkg.Lattice(run) as lat:
-        lat.init_channel(c0.uc, c0.amp, c0.seed)
+        lat.init_channel(ch.uc, ch.amp, ch.seed)
         assert np.array_equal(lat.download_f(), f0)
         lat.step(100)
         g = lat.download_f()
@@ -168,15 +168,15 @@ def test_poiseuille_startup_on_gpu(pkg, orc):
 
 
 def test_diag_and_mass_conservation(pkg, orc):
-    c0 = pkg.CHANNEL_CONFIGS["c0"]
-    run = c0.params("fp64")
+    ch = pkg.CHANNEL_CONFIGS["channel-128x64x64"]
+    run = ch.params("fp64")
     with pkg.Lattice(run) as lat:
-        lat.init_channel(c0.uc, c0.amp, c0.seed)
+        lat.init_channel(ch.uc, ch.amp, ch.seed)
         st0 = lat.diag()
         lat.step(200)
         st = lat.diag()
         rho, ux, uy, uz = lat.macrovar()
-    assert st.nfluid == c0.nodes and st.nonfinite == 0
+    assert st.nfluid == ch.nodes and st.nonfinite == 0
     assert abs(st.rho_sum - st0.rho_sum) < 1e-9
     assert st.rho_max == pytest.approx(rho.max(), rel=1e-12)
     assert st.rho_min == pytest.approx(rho.min(), rel=1e-12)
@@ -244,18 +244,18 @@ def test_checkpoint_files_in_reference_format(pkg, orc):
 
 
 def test_precision_variants_against_fp64(pkg):
-    """FP32 and FP16-storage runs of the c0 channel against FP64 after 300
+    """FP32 and FP16-storage runs of the ch channel against FP64 after 300
     steps: mean streamwise profile within 1 % and bounded population error."""
-    c0 = pkg.CHANNEL_CONFIGS["c0"]
+    ch = pkg.CHANNEL_CONFIGS["channel-128x64x64"]
     res = {}
     for prec in ("fp64", "fp32", "fp16"):
-        with pkg.Lattice(c0.params(prec)) as lat:
-            lat.init_channel(c0.uc, c0.amp, c0.seed)
+        with pkg.Lattice(ch.params(prec)) as lat:
+            lat.init_channel(ch.uc, ch.amp, ch.seed)
             lat.step(300)
             res[prec] = (lat.profiles(), lat.download_f(), lat.diag())
-    ref = pkg.statistics(res["fp64"][0], c0.ustar)
+    ref = pkg.statistics(res["fp64"][0], ch.ustar)
     for prec, tol_f in (("fp32", 1e-5), ("fp16", 2e-2)):
-        st = pkg.statistics(res[prec][0], c0.ustar)
+        st = pkg.statistics(res[prec][0], ch.ustar)
         err_mean = np.abs(st["mean"][:, 1] - ref["mean"][:, 1]).max() / np.abs(ref["mean"][:, 1]).max()
         assert err_mean < 1e-2, (prec, err_mean)
         assert rel_linf(res[prec][1], res["fp64"][1]) < tol_f, prec
@@ -305,20 +305,20 @@ def test_row_pipelined_kernels_match_simple_kernels(pkg, orc, prec, shape):
 def test_row_kernels_full_size_config4_properties(pkg):
     """1024 x 512 x 512 FP16 store (the large channel): no NaN, mass drift and
     mean profile against the one-node-per-thread kernels after 20 steps."""
-    c4 = pkg.CHANNEL_CONFIGS["c4"]
+    big = pkg.CHANNEL_CONFIGS["spheres-1024x512x512"]
     res = {}
     for flags in (0, pkg.FLAG_SIMPLE_STEP):
-        run = c4.params("fp16")
+        run = big.params("fp16")
         run.flags = flags
         with pkg.Lattice(run) as lat:
-            lat.init_channel(c4.uc, c4.amp, c4.seed)
+            lat.init_channel(big.uc, big.amp, big.seed)
             d0 = lat.diag()
             lat.step(20)
             d1 = lat.diag()
             res[flags] = (lat.profiles(), d1, d1.rho_sum - d0.rho_sum)
     a, b = res[0], res[pkg.FLAG_SIMPLE_STEP]
     assert a[1].nonfinite == 0 and b[1].nonfinite == 0
-    ma = pkg.statistics(a[0], c4.ustar)["mean"][:, 1]
-    mb = pkg.statistics(b[0], c4.ustar)["mean"][:, 1]
+    ma = pkg.statistics(a[0], big.ustar)["mean"][:, 1]
+    mb = pkg.statistics(b[0], big.ustar)["mean"][:, 1]
     assert np.abs(ma - mb).max() < 1e-4 * np.abs(mb).max()
-    assert abs(a[2]) < 1e-5 * c4.nodes and abs(b[2]) < 1e-5 * c4.nodes
+    assert abs(a[2]) < 1e-5 * big.nodes and abs(b[2]) < 1e-5 * big.nodes

@@ -2,7 +2,7 @@
 Newton-Euler, refilling) through the C ABI against the FP64 oracle.
 
 Tolerances: FP64 storage -- relative L-inf <= 1e-10 in the populations and in
-particle positions, velocities, forces and torques (the spec bar for
+particle positions, velocities, forces and torques (the parity bar for
 particle forces); FP32/FP16 storage -- stability and forces within a few
 percent of FP64.
 """

@@ -30,9 +30,9 @@ def check_close(out, ref):
 @pytest.mark.parametrize("prec", ["fp64", "fp16"])
 def test_noalloc_profiles_match_lbm_profiles(pkg, prec):
     lib = pkg.load_library()
-    c0 = pkg.CHANNEL_CONFIGS["c0"]
-    with pkg.Lattice(c0.params(prec)) as lat:
-        lat.init_channel(c0.uc, c0.amp, c0.seed)
+    ch = pkg.CHANNEL_CONFIGS["channel-128x64x64"]
+    with pkg.Lattice(ch.params(prec)) as lat:
+        lat.init_channel(ch.uc, ch.amp, ch.seed)
         for steps in (7, 1):                      # swapped, then natural AA state
             lat.step(steps)
             ref = lat.profiles()
