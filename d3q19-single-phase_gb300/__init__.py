@@ -56,9 +56,10 @@ EXPORTS = (
     "lbm_strerror", "lbm_last_error", "lbm_version", "lbm_params_init", "lbm_create", "lbm_destroy",
     "lbm_device_bytes", "lbm_upload_f", "lbm_download_f", "lbm_initpop", "lbm_init_channel",
     "lbm_channel_velocity", "lbm_step", "lbm_step_async", "lbm_synchronize", "lbm_stream",
-    "lbm_step_count", "lbm_prerelax", "lbm_macrovar", "lbm_diag", "lbm_profiles", "lbm_avedensity",
+    "lbm_step_count", "lbm_set_step_count", "lbm_prerelax", "lbm_macrovar", "lbm_diag", "lbm_profiles", "lbm_avedensity",
     "lbm_save_flow", "lbm_load_flow", "lbm_profiles_noalloc", "lbm_particle_params_init",
-    "lbm_particles_place", "lbm_particles_set", "lbm_particles_get", "lbm_particle_counts",
+    "lbm_particles_place", "lbm_particles_set", "lbm_particles_get", "lbm_particles_get_history",
+    "lbm_particles_set_history", "lbm_particle_counts",
     "lbm_timing_enable", "lbm_timing_get", "lbm_strain",
     "lbm_mlp_create", "lbm_mlp_destroy", "lbm_mlp_get", "lbm_mlp_set", "lbm_mlp_set_data", "lbm_mlp_train",
     "lbm_mlp_gradient", "lbm_mlp_predict", "lbm_les_set", "lbm_les_nut", "lbm_les_training_data",
@@ -143,6 +144,7 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
         "lbm_synchronize": (ctypes.c_int, [ctx]),
         "lbm_stream": (ctypes.c_int, [ctx, ctypes.POINTER(ctypes.c_void_p)]),
         "lbm_step_count": (ctypes.c_int, [ctx, ctypes.POINTER(ctypes.c_int64)]),
+        "lbm_set_step_count": (ctypes.c_int, [ctx, ctypes.c_int64]),
         "lbm_prerelax": (ctypes.c_int, [ctx, dp, dp, dp, ctypes.c_double, ctypes.c_int32,
                                         ctypes.POINTER(ctypes.c_int32), dp]),
         "lbm_macrovar": (ctypes.c_int, [ctx, dp, dp, dp, dp]),
@@ -175,6 +177,8 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
                                                dp]),
         "lbm_particles_set": (ctypes.c_int, [ctx, ctypes.POINTER(LBMParticleParams), dp, dp, dp]),
         "lbm_particles_get": (ctypes.c_int, [ctx, dp, dp, dp, dp, dp]),
+        "lbm_particles_get_history": (ctypes.c_int, [ctx, dp, dp]),
+        "lbm_particles_set_history": (ctypes.c_int, [ctx, dp, dp]),
         "lbm_particle_counts": (ctypes.c_int, [ctx, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
                                                ctypes.POINTER(ctypes.c_int64)]),
     }
@@ -494,6 +498,9 @@ class Lattice:
         self._call("lbm_step_count", ctypes.byref(n))
         return n.value
 
+    def set_step_count(self, n: int) -> None:
+        self._call("lbm_set_step_count", n)
+
     def device_bytes(self) -> int:
         n = ctypes.c_size_t()
         self._call("lbm_device_bytes", ctypes.byref(n))
@@ -577,6 +584,18 @@ class Lattice:
         o = None if omg is None else np.ascontiguousarray(omg, dtype=np.float64).reshape(-1, 3)
         self._npart = len(pos)
         self._call("lbm_particles_set", ctypes.byref(pp), _dptr(pos), _dptr(v), _dptr(o))
+
+    def particle_history(self) -> tuple[np.ndarray, np.ndarray]:
+        """Total force and torque of the previous step (Adams-Bashforth history)."""
+        n = getattr(self, "_npart", 0)
+        fp, tp = np.empty((n, 3)), np.empty((n, 3))
+        self._call("lbm_particles_get_history", _dptr(fp), _dptr(tp))
+        return fp, tp
+
+    def set_particle_history(self, fprev, tprev) -> None:
+        fp = np.ascontiguousarray(fprev, dtype=np.float64).reshape(-1, 3)
+        tp = np.ascontiguousarray(tprev, dtype=np.float64).reshape(-1, 3)
+        self._call("lbm_particles_set_history", _dptr(fp), _dptr(tp))
 
     def particles(self) -> dict:
         n = getattr(self, "_npart", 0)

@@ -23,7 +23,6 @@ struct lbm_ctx {
     int64_t nsteps = 0;
     double* d_stage = nullptr; // FP64 staging for layout conversion
     double* d_mass = nullptr;  // fluid mass and node count (mean-density removal)
-    int mass_pending = 0;      // a mean-density removal waits for natural orientation
     float* d_les = nullptr;    // closure network parameters + normalisation
     float* d_s9 = nullptr;     // per-node shear rate of the closure
     int use_rows_saved = 0;    // the step kernel choice without the closure
@@ -493,13 +492,10 @@ int lbm_step_async(lbm_ctx* c, int32_t nsteps) {
             c->have_prev = 1;
             // main.f90:163-167: with particles, every 100 steps the mean
             // density is removed to correct the mass the interpolated
-            // bounce-back loses (avedensity); done at the first step from
-            // there on that leaves the array in natural orientation
-            if (c->nsteps % 100 == 0) c->mass_pending = 1;
-            if (c->mass_pending && c->parity == 0) {
-                CK(launch_remove_mean_density(c->s, c->d_mass, c->stream));
+            // bounce-back loses (avedensity)
+            if (c->nsteps % 100 == 0) {
+                CK(launch_remove_mean_density(c->s, c->parity, c->d_mass, c->stream));
                 CK(launch_remove_mean_apply(c->s, c->d_mass, c->stream));
-                c->mass_pending = 0;
             }
         }
         if (timed) {
@@ -532,6 +528,12 @@ int lbm_stream(lbm_ctx* c, void** stream) {
 int lbm_step_count(const lbm_ctx* c, int64_t* n) {
     if (check_ctx(c) || !n) return fail(LBM_ERR_INVALID_ARG, "null argument");
     *n = c->nsteps;
+    return LBM_OK;
+}
+
+int lbm_set_step_count(lbm_ctx* c, int64_t n) {
+    if (check_ctx(c) || n < 0) return fail(LBM_ERR_INVALID_ARG, "bad step count");
+    c->nsteps = n;
     return LBM_OK;
 }
 
@@ -1014,6 +1016,30 @@ int lbm_particles_get(lbm_ctx* c, double* pos, double* vel, double* omg, double*
     for (int k = 0; k < 5; ++k)
         if (dst[k]) CK(cudaMemcpyAsync(dst[k], src[k], b, cudaMemcpyDeviceToHost, c->stream));
     return sync(c);
+}
+
+int lbm_particles_get_history(lbm_ctx* c, double* fprev, double* tprev) {
+    if (check_ctx(c)) return LBM_ERR_INVALID_ARG;
+    if (c->P.npart == 0) return fail(LBM_ERR_STATE, "no spheres set");
+    if (int rc = set_device(c)) return rc;
+    const size_t b = 3 * (size_t)c->P.npart * sizeof(double);
+    if (fprev) CK(cudaMemcpyAsync(fprev, c->P.fprev, b, cudaMemcpyDeviceToHost, c->stream));
+    if (tprev) CK(cudaMemcpyAsync(tprev, c->P.tprev, b, cudaMemcpyDeviceToHost, c->stream));
+    return sync(c);
+}
+
+int lbm_particles_set_history(lbm_ctx* c, const double* fprev, const double* tprev) {
+    if (check_ctx(c) || !fprev || !tprev) return fail(LBM_ERR_INVALID_ARG, "null argument");
+    if (c->P.npart == 0) return fail(LBM_ERR_STATE, "no spheres set");
+    const size_t m = 3 * (size_t)c->P.npart;
+    for (size_t k = 0; k < m; ++k)
+        if (!std::isfinite(fprev[k]) || !std::isfinite(tprev[k])) return fail(LBM_ERR_INVALID_ARG, "non-finite history");
+    if (int rc = set_device(c)) return rc;
+    CK(cudaMemcpyAsync(c->P.fprev, fprev, m * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->P.tprev, tprev, m * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    if (int rc = sync(c)) return rc;
+    c->have_prev = 1;
+    return LBM_OK;
 }
 
 int lbm_particle_counts(lbm_ctx* c, int64_t* nsolid, int64_t* nlinks, int64_t* nrefill) {

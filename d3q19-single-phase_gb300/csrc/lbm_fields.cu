@@ -604,8 +604,46 @@ __global__ void __launch_bounds__(256) k_fluid_mass(DeviceState s, double* __res
     }
 }
 
+// Same sum with the array after an odd number of AA steps: each fluid node's
+// populations are gathered from their parity-1 slots (every 100 steps only).
+template <typename T>
+__global__ void __launch_bounds__(256) k_fluid_mass_gather(DeviceState s, double* __restrict__ acc) {
+    using R = typename DiagR<T>::type;
+    const Geometry& g = s.g;
+    double m = 0.0, cnt = 0.0;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x; n < s.N; n += stride) {
+        if (s.owner && s.owner[n] >= 0) continue;
+        const int x = (int)(n % g.NX), y = (int)((n / g.NX) % g.NY), z = (int)(n / g.NXY);
+        R f[Q];
+        gather_natural_r<T, R>(s, 1, x, y, z, f);
+        R r = 0;
+#pragma unroll
+        for (int i = 0; i < Q; ++i) r += f[i];
+        m += (double)r;
+        cnt += 1.0;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        m += __shfl_xor_sync(0xffffffffu, m, o);
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    }
+    __shared__ double sh[2][8];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) { sh[0][w] = m; sh[1][w] = cnt; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) { a += sh[0][k]; b += sh[1][k]; }
+        atomicAdd(acc, a);
+        atomicAdd(acc + 1, b);
+    }
+}
+
 // Remove the mean density acc[0] / acc[1] (w_i * mean from every population),
-// 16 bytes per plane and thread as above.
+// 16 bytes per plane and thread as above.  Every storage slot holds one
+// population of one node in either parity, and slot opp(i) of the parity-1
+// layout holds direction i with w_opp(i) = w_i, so the same pass serves both
+// parities.
 template <typename T>
 __global__ void k_remove_mean(DeviceState s, const double* __restrict__ acc) {
     using R = typename DiagR<T>::type;
@@ -748,10 +786,13 @@ cudaError_t launch_add_rest(const DeviceState& s, int parity, double delta, cuda
     LBM_DISPATCH(s.prec, (k_add_rest<T><<<nb, 256, 0, st>>>(s, delta)))
 }
 
-cudaError_t launch_remove_mean_density(const DeviceState& s, double* acc, cudaStream_t st) {
+cudaError_t launch_remove_mean_density(const DeviceState& s, int parity, double* acc, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(acc, 0, 2 * sizeof(double), st);
     if (e != cudaSuccess) return e;
     const unsigned grid = (unsigned)std::max(1, 8 * s.sm_count);
+    if (parity) {
+        LBM_DISPATCH(s.prec, (k_fluid_mass_gather<T><<<grid, 256, 0, st>>>(s, acc)))
+    }
     LBM_DISPATCH(s.prec, (k_fluid_mass<T><<<grid, 256, 0, st>>>(s, acc)))
 }
 

@@ -130,9 +130,9 @@ cudaError_t launch_closure_targets(const double* F9, int nxc, int nyc, int nzc, 
                                    float h_c, float* X, float* y, cudaStream_t st);
 cudaError_t launch_les_features(const DeviceState& s, int parity, float ustar, float h, float* X,
                                 cudaStream_t st);
-// mean-density removal on the device (array in natural orientation): fluid
-// mass into acc[2], then applied
-cudaError_t launch_remove_mean_density(const DeviceState& s, double* acc, cudaStream_t st);
+// mean-density removal on the device, either parity: fluid mass into acc[2],
+// then applied
+cudaError_t launch_remove_mean_density(const DeviceState& s, int parity, double* acc, cudaStream_t st);
 cudaError_t launch_remove_mean_apply(const DeviceState& s, const double* acc, cudaStream_t st);
 cudaError_t launch_ref_to_gpu_vec(const DeviceState& s, const double* ux,
                                   const double* uy, const double* uz,

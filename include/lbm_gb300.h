@@ -177,6 +177,10 @@ int lbm_timing_get(lbm_ctx* ctx, double* fluid_even_ms, double* fluid_odd_ms,
 int lbm_stream(lbm_ctx* ctx, void** stream);
 /* Steps taken since the last upload / init. */
 int lbm_step_count(const lbm_ctx* ctx, int64_t* nsteps);
+/* Set the step counter, e.g. to istep0 after loadcntdflow, so that the
+ * every-100-steps work of the main loop (main.f90:163) keeps the absolute
+ * step numbering of the run being continued. */
+int lbm_set_step_count(lbm_ctx* ctx, int64_t nsteps);
 
 /* Density pre-relaxation of main.f90:69-90 with the velocity frozen at
  * (ux,uy,uz) (arrays (nx,ny,nz)): repeat {rho = sum f (rhoupdat);
@@ -284,6 +288,12 @@ int lbm_particles_set(lbm_ctx* ctx, const lbm_particle_params* pp,
  * torque are the hydrodynamic (momentum-exchange) parts of the last step. */
 int lbm_particles_get(lbm_ctx* ctx, double* pos, double* vel, double* omg,
                       double* force, double* torque);
+/* Adams-Bashforth history: total force and torque (hydrodynamic + repulsion
+ * + body force) of the previous step, forcepp/torqpp of savecntdpart01
+ * (saveload.f90:523-560).  set: continue a run with its second-order update
+ * (without it the first update after lbm_particles_set is first order). */
+int lbm_particles_get_history(lbm_ctx* ctx, double* fprev, double* tprev);
+int lbm_particles_set_history(lbm_ctx* ctx, const double* fprev, const double* tprev);
 /* Solid node count, boundary links and refilled nodes of the last step. */
 int lbm_particle_counts(lbm_ctx* ctx, int64_t* nsolid, int64_t* nlinks,
                         int64_t* nrefill);

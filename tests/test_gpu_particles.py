@@ -217,3 +217,22 @@ def test_mean_density_removed_every_100_steps_with_spheres(pkg, orc):
         d100 = lat.diag()
     assert abs(d99.rho_sum / d99.nfluid) > 1e-9
     assert abs(d100.rho_sum / d100.nfluid) < 1e-13
+
+
+def test_mean_density_removed_at_odd_parity(pkg, orc):
+    """A run continued from step 1 reaches step 100 after an odd number of
+    steps (array in the parity-1 layout); the removal still happens at step
+    100, as main.f90:163 counts absolute steps."""
+    shape = (24, 32, 22)
+    run, f0 = channel_with_spheres(orc, pkg, shape, POS)
+    with pkg.Lattice(run) as lat:
+        lat.upload_f(f0)
+        lat.set_particles(POS, radius=4.0, rho_ratio=2.0, vel=VEL)
+        lat.set_step_count(1)
+        lat.step(98)
+        d99 = lat.diag()
+        lat.step(1)
+        d100 = lat.diag()
+        assert lat.step_count() == 100
+    assert abs(d99.rho_sum / d99.nfluid) > 1e-9
+    assert abs(d100.rho_sum / d100.nfluid) < 1e-13
