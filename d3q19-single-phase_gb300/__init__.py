@@ -59,7 +59,7 @@ EXPORTS = (
     "lbm_step_count", "lbm_set_step_count", "lbm_prerelax", "lbm_macrovar", "lbm_diag", "lbm_profiles", "lbm_avedensity",
     "lbm_save_flow", "lbm_load_flow", "lbm_profiles_noalloc", "lbm_particle_params_init",
     "lbm_particles_place", "lbm_particles_set", "lbm_particles_get", "lbm_particles_get_history",
-    "lbm_particles_set_history", "lbm_particle_counts",
+    "lbm_particles_set_history", "lbm_save_part", "lbm_load_part", "lbm_particle_counts",
     "lbm_timing_enable", "lbm_timing_get", "lbm_strain",
     "lbm_mlp_create", "lbm_mlp_destroy", "lbm_mlp_get", "lbm_mlp_set", "lbm_mlp_set_data", "lbm_mlp_train",
     "lbm_mlp_gradient", "lbm_mlp_predict", "lbm_les_set", "lbm_les_nut", "lbm_les_training_data",
@@ -179,6 +179,8 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
         "lbm_particles_get": (ctypes.c_int, [ctx, dp, dp, dp, dp, dp]),
         "lbm_particles_get_history": (ctypes.c_int, [ctx, dp, dp]),
         "lbm_particles_set_history": (ctypes.c_int, [ctx, dp, dp]),
+        "lbm_save_part": (ctypes.c_int, [ctx, ctypes.c_char_p]),
+        "lbm_load_part": (ctypes.c_int, [ctx, ctypes.c_char_p, ctypes.POINTER(LBMParticleParams)]),
         "lbm_particle_counts": (ctypes.c_int, [ctx, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
                                                ctypes.POINTER(ctypes.c_int64)]),
     }
@@ -596,6 +598,30 @@ class Lattice:
         fp = np.ascontiguousarray(fprev, dtype=np.float64).reshape(-1, 3)
         tp = np.ascontiguousarray(tprev, dtype=np.float64).reshape(-1, 3)
         self._call("lbm_particles_set_history", _dptr(fp), _dptr(tp))
+
+    def save_part(self, path: str | Path) -> None:
+        """endrunpart2D checkpoint of the spheres (savecntdpart, saveload.f90:604-647)."""
+        self._call("lbm_save_part", str(path).encode())
+
+    def load_part(self, path: str | Path, radius: float, rho_ratio: float = 2.0, **overrides) -> None:
+        """Attach the spheres of an endrunpart2D checkpoint (loadcntdpart, saveload.f90:649-693)."""
+        n = self.part_count(path)
+        pp = LBMParticleParams()
+        _check(self.lib, self.lib.lbm_particle_params_init(ctypes.byref(pp), n, radius, rho_ratio),
+               "lbm_particle_params_init")
+        for k, v in overrides.items():
+            setattr(pp, k, v)
+        self._call("lbm_load_part", str(path).encode(), ctypes.byref(pp))
+        self._npart = n
+
+    @staticmethod
+    def part_count(path: str | Path) -> int:
+        """nps of an endrunpart2D file (first integer of its first record)."""
+        with open(path, "rb") as fh:
+            head = fh.read(8)
+        if len(head) < 8:
+            raise ValueError(f"{path}: not a particle checkpoint")
+        return int(np.frombuffer(head[4:8], dtype="<i4")[0])
 
     def particles(self) -> dict:
         n = getattr(self, "_npart", 0)

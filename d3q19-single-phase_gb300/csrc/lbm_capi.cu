@@ -1042,6 +1042,148 @@ int lbm_particles_set_history(lbm_ctx* c, const double* fprev, const double* tpr
     return LBM_OK;
 }
 
+// savecntdpart / loadcntdpart (saveload.f90:604-693) for one process.
+int lbm_save_part(lbm_ctx* c, const char* path) {
+    if (check_ctx(c) || !path) return fail(LBM_ERR_INVALID_ARG, "null argument");
+    if (c->P.npart == 0) return fail(LBM_ERR_STATE, "no spheres set");
+    if (int rc = set_device(c)) return rc;
+    const int np = c->P.npart;
+    const size_t msize = 10 * (size_t)np;                  // para.f90:369 with nproc = 1
+    const size_t m3 = 3 * (size_t)np;
+    std::vector<double> st(5 * m3);                         // pos, vel, omg, fprev, tprev
+    const double* src[5] = {c->P.pos, c->P.vel, c->P.omg, c->P.fprev, c->P.tprev};
+    for (int k = 0; k < 5; ++k)
+        CK(cudaMemcpyAsync(st.data() + k * m3, src[k], m3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if (int rc = sync(c)) return rc;
+    FILE* fp = std::fopen(path, "wb");
+    if (!fp) return fail(LBM_ERR_IO, std::string("cannot open ") + path);
+    bool ok = true;
+    auto record = [&](std::initializer_list<std::pair<const void*, int64_t>> parts) {
+        int64_t total = 0;
+        for (auto& q : parts) total += q.second;
+        RecordWriter w(fp, total);
+        for (auto& q : parts) w.put(q.first, q.second);
+        ok = ok && w.ok && w.done == w.total;
+    };
+    // {nps, ipglb(msize)}
+    std::vector<int32_t> ipglb(msize, 0);
+    for (int k = 0; k < np; ++k) ipglb[k] = k + 1;
+    const int32_t nps = np;
+    record({{&nps, 4}, {ipglb.data(), (int64_t)(4 * msize)}});
+    // {ibnodes(lx,ly,lz), isnodes(lx,ly,lz)}: converted plane chunks
+    if (ok) {
+        const size_t pp = plane_nodes(c->p);
+        const int kz = chunk_planes(c, 1);
+        RecordWriter w(fp, (int64_t)(8 * nodes(c->p)));
+        std::vector<int32_t> h(2 * (size_t)kz * pp);
+        for (int pass = 0; pass < 2 && w.ok; ++pass) {
+            for (int z0 = 0; z0 < c->p.nz && w.ok; z0 += kz) {
+                const int nzc = std::min(kz, c->p.nz - z0);
+                int32_t* ib = reinterpret_cast<int32_t*>(c->d_stage);
+                int32_t* is = ib + (size_t)nzc * pp;
+                cudaError_t e = launch_owner_to_ref(c->s, c->P.owner, ib, is, z0, nzc, c->stream);
+                if (e == cudaSuccess)
+                    e = cudaMemcpyAsync(h.data(), pass == 0 ? ib : is, (size_t)nzc * pp * 4, cudaMemcpyDeviceToHost,
+                                        c->stream);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+                if (e != cudaSuccess) { std::fclose(fp); return cuda_fail(e, "node flags download"); }
+                w.put(h.data(), (int64_t)nzc * pp * 4);
+            }
+        }
+        ok = w.ok && w.done == w.total;
+    }
+    // {yp, thetap}, {forcepp, torqpp}, {dwdt, domgdt}: local arrays of msize
+    // particles (here the first npart); thetap is not integrated (zero);
+    // dwdt, domgdt = total force / mass and torque / moment of inertia of the
+    // last step
+    std::vector<double> a(3 * msize, 0.0), b(3 * msize, 0.0);
+    auto fill = [&](std::vector<double>& v, const double* x, double scale) {
+        std::fill(v.begin(), v.end(), 0.0);
+        for (size_t k = 0; k < m3; ++k) v[k] = x[k] * scale;
+    };
+    const double R = c->P.R;
+    const double mass = c->P.rho_ratio * (4.0 / 3.0 * 3.14159265358979323846 * R * R * R);
+    const double inertia = 0.4 * mass * R * R;
+    const int64_t lb = (int64_t)(8 * 3 * msize);
+    fill(a, st.data(), 1.0);
+    std::fill(b.begin(), b.end(), 0.0);
+    if (ok) record({{a.data(), lb}, {b.data(), lb}});
+    fill(a, st.data() + 3 * m3, 1.0);
+    fill(b, st.data() + 4 * m3, 1.0);
+    if (ok) record({{a.data(), lb}, {b.data(), lb}});
+    fill(a, st.data() + 3 * m3, 1.0 / mass);
+    fill(b, st.data() + 4 * m3, 1.0 / inertia);
+    if (ok) record({{a.data(), lb}, {b.data(), lb}});
+    // {ypglb, wp, omgp} (process 0)
+    const int64_t gb = (int64_t)(8 * m3);
+    if (ok) record({{st.data(), gb}, {st.data() + m3, gb}, {st.data() + 2 * m3, gb}});
+    if (std::fclose(fp) != 0 || !ok) return fail(LBM_ERR_IO, "write failed");
+    return LBM_OK;
+}
+
+int lbm_load_part(lbm_ctx* c, const char* path, const lbm_particle_params* pp) {
+    if (check_ctx(c) || !path || !pp) return fail(LBM_ERR_INVALID_ARG, "null argument");
+    if (pp->npart <= 0) return fail(LBM_ERR_INVALID_ARG, "npart must be positive");
+    FILE* fp = std::fopen(path, "rb");
+    if (!fp) return fail(LBM_ERR_IO, std::string("cannot open ") + path);
+    const int np = pp->npart;
+    const size_t m3 = 3 * (size_t)np;
+    auto bad = [&](const std::string& why) { std::fclose(fp); return fail(LBM_ERR_IO, why); };
+    // {nps, ipglb(msize)}: msize from the record length
+    std::vector<int32_t> ipglb;
+    size_t msize = 0;
+    {
+        RecordReader r(fp);
+        int32_t nps = 0;
+        if (!r.ok || r.more || r.total < 4 || (r.total - 4) % 4 != 0 || !r.get(&nps, 4))
+            return bad("bad {nps, ipglb} record");
+        msize = (size_t)(r.total - 4) / 4;
+        if (nps != np || msize < (size_t)np) return bad("file holds " + std::to_string(nps) + " spheres, expected " +
+                                                        std::to_string(np));
+        ipglb.resize(msize);
+        if (!r.get(ipglb.data(), (int64_t)(4 * msize)) || !r.finish()) return bad("bad {nps, ipglb} record");
+        std::vector<char> seen(np, 0);
+        for (int k = 0; k < np; ++k) {
+            const int id = ipglb[k];
+            if (id < 1 || id > np || seen[id - 1]) return bad("ipglb is not a permutation of 1..npart");
+            seen[id - 1] = 1;
+        }
+    }
+    // {ibnodes, isnodes} and {yp, thetap}: rebuilt from the centres / unused
+    for (int k = 0; k < 2; ++k) {
+        RecordReader r(fp);
+        if (r.ok) r.finish();                                   // skip: finish() is false for a partial read
+        if (!r.ok) return bad("truncated particle checkpoint");
+    }
+    // {forcepp, torqpp} in local order -> global order
+    std::vector<double> fl(3 * msize), tl(3 * msize), fprev(m3), tprev(m3);
+    {
+        RecordReader r(fp);
+        if (!r.ok || !r.get(fl.data(), (int64_t)(8 * 3 * msize)) || !r.get(tl.data(), (int64_t)(8 * 3 * msize)) ||
+            !r.finish())
+            return bad("bad {forcepp, torqpp} record");
+        for (int k = 0; k < np; ++k)
+            for (int a = 0; a < 3; ++a) {
+                fprev[3 * (ipglb[k] - 1) + a] = fl[3 * k + a];
+                tprev[3 * (ipglb[k] - 1) + a] = tl[3 * k + a];
+            }
+    }
+    {
+        RecordReader r(fp);                                     // {dwdt, domgdt}
+        if (r.ok) r.finish();
+        if (!r.ok) return bad("truncated particle checkpoint");
+    }
+    std::vector<double> g(3 * m3);                              // ypglb, wp, omgp
+    {
+        RecordReader r(fp);
+        if (!r.ok || !r.get(g.data(), (int64_t)(8 * 3 * m3)) || !r.finish())
+            return bad("bad {ypglb, wp, omgp} record");
+    }
+    std::fclose(fp);
+    if (int rc = lbm_particles_set(c, pp, g.data(), g.data() + m3, g.data() + 2 * m3)) return rc;
+    return lbm_particles_set_history(c, fprev.data(), tprev.data());
+}
+
 int lbm_particle_counts(lbm_ctx* c, int64_t* nsolid, int64_t* nlinks, int64_t* nrefill) {
     if (check_ctx(c)) return LBM_ERR_INVALID_ARG;
     if (c->P.npart == 0) {

@@ -136,6 +136,22 @@ __global__ void k_aos_to_store(DeviceState s, const double* __restrict__ aos, in
     for (int i = 0; i < Q; ++i) put<T>(s, i, n, aos[src + i]);
 }
 
+// Node flags of the particle checkpoint for ref z planes [z0, z0 + nzc), in
+// reference layout: ibnodes = 1 solid / -1 fluid (saveload.f90:1359-1360),
+// isnodes = 1-based id of the owning sphere / -1 (collision.f90:422).
+__global__ void k_owner_to_ref(Geometry g, const int* __restrict__ owner, int32_t* __restrict__ ib,
+                               int32_t* __restrict__ is, int z0) {
+    RefNode r;
+    r.iy = blockIdx.x * blockDim.x + threadIdx.x;
+    r.ix = blockIdx.y;
+    r.iz = z0 + blockIdx.z;
+    if (r.iy >= g.NX) return;
+    const int own = owner[gpu_lin(g, r.ix, r.iy, r.iz)];
+    const size_t o = ref_lin(g, r.ix, r.iy, r.iz - z0);
+    ib[o] = own >= 0 ? 1 : -1;
+    is[o] = own >= 0 ? own + 1 : -1;
+}
+
 template <typename T>
 __global__ void k_store_to_aos(DeviceState s, int parity, double* __restrict__ aos, int z0) {
     const RefNode r = ref_node(s.g, z0);
@@ -726,6 +742,12 @@ cudaError_t launch_initpop(const DeviceState& s, const double* ux, const double*
 cudaError_t launch_init_channel(const DeviceState& s, double uc, double amp, uint64_t seed,
                                 cudaStream_t st) {
     LBM_DISPATCH(s.prec, (k_init_channel<T><<<ref_grid(s.g, s.g.NY, kBx), kBx, 0, st>>>(s, uc, amp, seed)))
+}
+
+cudaError_t launch_owner_to_ref(const DeviceState& s, const int* owner, int32_t* ib, int32_t* is, int z0, int nzc,
+                               cudaStream_t st) {
+    k_owner_to_ref<<<ref_grid(s.g, nzc, kBx), kBx, 0, st>>>(s.g, owner, ib, is, z0);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_macro(const DeviceState& s, int parity, double* rho, double* ux, double* uy,

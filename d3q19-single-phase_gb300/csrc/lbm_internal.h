@@ -117,6 +117,10 @@ cudaError_t launch_initpop(const DeviceState& s, const double* ux,
                            cudaStream_t st);
 cudaError_t launch_init_channel(const DeviceState& s, double uc, double amp,
                                 uint64_t seed, cudaStream_t st);
+// particle checkpoint node flags (ibnodes, isnodes) for ref z planes
+// [z0, z0+nzc), reference layout
+cudaError_t launch_owner_to_ref(const DeviceState& s, const int* owner, int32_t* ib, int32_t* is, int z0, int nzc,
+                               cudaStream_t st);
 // macrovar for ref z planes [z0, z0+nzc) into reference-layout FP64 arrays
 cudaError_t launch_macro(const DeviceState& s, int parity, double* rho,
                          double* ux, double* uy, double* uz, int z0, int nzc,

@@ -14,7 +14,8 @@
 //                                   nstat steps (saveload.f90:1348-1502), wall
 //                                   clock limit
 //   savecntdflow                 -> lbm_save_flow (kind 1)
-//   savecntdpart01               -> endrunpart.<istep>.000 (saveload.f90:523-560)
+//   savecntdpart / loadcntdpart  -> lbm_save_part / lbm_load_part
+//                                   (endrunpart2D.<istep>.000, saveload.f90:604-693)
 //
 // Usage: channel_gb300 [key=value ...], keys (defaults = configuration c0):
 //   nx ny nz          lattice, reference axes (wall-normal, streamwise, spanwise)
@@ -32,7 +33,7 @@
 //   npart rad rhopart spheres: count, radius, density ratio (0 spheres: ipart off)
 //   iseedp gap wgap   seeded placement: seed, surface gaps sphere-sphere and sphere-wall
 //   qfp64             1: boundary-link fractions in FP64 for FP32/FP16 storage
-//   restart_part      endrunpart file to continue the spheres from
+//   restart_part      endrunpart2D file to continue the spheres from
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -67,47 +68,6 @@ int check(int rc, const char* what) {
         std::exit(2);
     }
     return rc;
-}
-
-// Fortran sequential unformatted records: 4-byte length, payload, 4-byte length.
-bool write_record(FILE* fp, const void* data, size_t bytes) {
-    const int32_t n = (int32_t)bytes;
-    return std::fwrite(&n, 4, 1, fp) == 1 && (bytes == 0 || std::fwrite(data, 1, bytes, fp) == bytes) &&
-           std::fwrite(&n, 4, 1, fp) == 1;
-}
-bool read_record(FILE* fp, void* data, size_t bytes) {
-    int32_t a = 0, b = 0;
-    return std::fread(&a, 4, 1, fp) == 1 && (size_t)a == bytes &&
-           (bytes == 0 || std::fread(data, 1, bytes, fp) == bytes) && std::fread(&b, 4, 1, fp) == 1 && a == b;
-}
-
-// savecntdpart01 for one process (saveload.f90:523-560): {nps, ipglb},
-// {ypglb, wp, omgp}, {forcepp, torqpp} with forcepp/torqpp the total force and
-// torque of the last step (the Adams-Bashforth history); positions in
-// reference axes with node ix at ix - 1/2.  The node masks of the reference's record 2 (ibnodes0,
-// isnodes0) are rebuilt from the centres on load and are not written.
-bool save_part(const std::string& path, int npart, const std::vector<double>& st) {
-    FILE* fp = std::fopen(path.c_str(), "wb");
-    if (!fp) return false;
-    std::vector<int32_t> rec1(1 + (size_t)npart);
-    rec1[0] = npart;
-    for (int i = 0; i < npart; ++i) rec1[1 + i] = i + 1;
-    const size_t m = 3 * (size_t)npart;
-    bool ok = write_record(fp, rec1.data(), rec1.size() * 4) && write_record(fp, st.data(), 3 * m * 8) &&
-              write_record(fp, st.data() + 3 * m, 2 * m * 8);
-    return std::fclose(fp) == 0 && ok;
-}
-// st: 15 * npart doubles = pos, vel, omg, forcepp, torqpp (each 3 * npart)
-bool load_part(const std::string& path, int npart, std::vector<double>& st) {
-    FILE* fp = std::fopen(path.c_str(), "rb");
-    if (!fp) return false;
-    std::vector<int32_t> rec1(1 + (size_t)npart);
-    const size_t m = 3 * (size_t)npart;
-    st.assign(5 * m, 0.0);
-    bool ok = read_record(fp, rec1.data(), rec1.size() * 4) && rec1[0] == npart &&
-              read_record(fp, st.data(), 3 * m * 8) && read_record(fp, st.data() + 3 * m, 2 * m * 8);
-    std::fclose(fp);
-    return ok;
 }
 
 // statistc2 normalisation and its 15 columns (saveload.f90:1442-1496)
@@ -196,24 +156,15 @@ int main(int argc, char** argv) {
         lbm_particle_params pp;
         check(lbm_particle_params_init(&pp, npart, rad, rhopart), "particle parameters");
         if (argi("qfp64", 0)) pp.flags |= LBM_PFLAG_Q_FP64;
-        std::vector<double> st;
         if (g_args.count("restart_part")) {
-            if (!load_part(args("restart_part", ""), npart, st)) {
-                std::fprintf(stderr, "loadcntdpart: cannot read %s for %d spheres\n",
-                             args("restart_part", "").c_str(), npart);
-                lbm_destroy(ctx);
-                return 2;
-            }
+            check(lbm_load_part(ctx, args("restart_part", "").c_str(), &pp), "loadcntdpart");
         } else {
-            st.assign(15 * (size_t)npart, 0.0);
+            std::vector<double> pos(3 * (size_t)npart);
             check(lbm_particles_place(nx, ny, nz, npart, rad, argd("gap", 2.0), argd("wgap", 1.0),
-                                      (uint64_t)argi("iseedp", 12345), st.data()),
+                                      (uint64_t)argi("iseedp", 12345), pos.data()),
                   "initpartpos");
+            check(lbm_particles_set(ctx, &pp, pos.data(), nullptr, nullptr), "beads");
         }
-        const size_t m = 3 * (size_t)npart;
-        check(lbm_particles_set(ctx, &pp, st.data(), st.data() + m, st.data() + 2 * m), "beads");
-        if (g_args.count("restart_part"))
-            check(lbm_particles_set_history(ctx, st.data() + 3 * m, st.data() + 4 * m), "forcepp/torqpp");
         int64_t nsolid = 0, nlinks = 0, nrefill = 0;
         check(lbm_particle_counts(ctx, &nsolid, &nlinks, &nrefill), "particle counts");
         std::printf(" spheres: %d of radius %.3f, %lld solid nodes\n", npart, rad, (long long)nsolid);
@@ -265,17 +216,8 @@ int main(int argc, char** argv) {
         int32_t h3[3] = {(int32_t)(istep0 + done), 0, 0};
         check(lbm_save_flow(ctx, (out + name).c_str(), 1, h3), "savecntdflow");
         if (npart > 0) {
-            std::vector<double> st(15 * (size_t)npart);
-            const size_t m = 3 * (size_t)npart;
-            check(lbm_particles_get(ctx, st.data(), st.data() + m, st.data() + 2 * m, nullptr, nullptr),
-                  "particle state");
-            check(lbm_particles_get_history(ctx, st.data() + 3 * m, st.data() + 4 * m), "forcepp/torqpp");
-            std::snprintf(name, sizeof(name), "/endrunpart.%07ld.000", istep0 + done);
-            if (!save_part(out + name, npart, st)) {
-                std::fprintf(stderr, "savecntdpart: cannot write %s%s\n", out.c_str(), name);
-                lbm_destroy(ctx);
-                return 2;
-            }
+            std::snprintf(name, sizeof(name), "/endrunpart2D.%07ld.000", istep0 + done);
+            check(lbm_save_part(ctx, (out + name).c_str()), "savecntdpart");
         }
     }
     std::printf(" time_max = %.6f  steps = %ld  GLUPS = %.4f\n", time_max, done,

@@ -294,6 +294,22 @@ int lbm_particles_get(lbm_ctx* ctx, double* pos, double* vel, double* omg,
  * (without it the first update after lbm_particles_set is first order). */
 int lbm_particles_get_history(lbm_ctx* ctx, double* fprev, double* tprev);
 int lbm_particles_set_history(lbm_ctx* ctx, const double* fprev, const double* tprev);
+/* Particle checkpoint in the reference's endrunpart2D format for one
+ * process (savecntdpart / loadcntdpart, saveload.f90:604-693), Fortran
+ * unformatted sequential records, FP64 reals and 4-byte integers:
+ *   {nps, ipglb(msize)} {ibnodes(lx,ly,lz), isnodes(lx,ly,lz)}
+ *   {yp(3,msize), thetap(3,msize)} {forcepp(3,msize), torqpp(3,msize)}
+ *   {dwdt(3,msize), domgdt(3,msize)} {ypglb(3,npart), wp(3,npart), omgp(3,npart)}
+ * with msize = 10 npart (para.f90:369, one process), ibnodes 1 solid / -1
+ * fluid, isnodes the 1-based owning sphere / -1, forcepp/torqpp the
+ * Adams-Bashforth history (total force and torque of the last step),
+ * dwdt/domgdt that force / mass and torque / moment of inertia, thetap zero
+ * (orientation is not integrated).  lbm_load_part attaches the spheres (as
+ * lbm_particles_set with pp, whose npart must equal the file's nps) from
+ * ypglb/wp/omgp, restores the history, and rebuilds the node flags from the
+ * centres. */
+int lbm_save_part(lbm_ctx* ctx, const char* path);
+int lbm_load_part(lbm_ctx* ctx, const char* path, const lbm_particle_params* pp);
 /* Solid node count, boundary links and refilled nodes of the last step. */
 int lbm_particle_counts(lbm_ctx* ctx, int64_t* nsolid, int64_t* nlinks,
                         int64_t* nrefill);
