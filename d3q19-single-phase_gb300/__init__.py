@@ -47,6 +47,7 @@ PREC_FP64, PREC_FP32, PREC_FP16 = 0, 1, 2
 PRECISIONS = {"fp64": PREC_FP64, "fp32": PREC_FP32, "fp16": PREC_FP16}
 MRT_STABLE, MRT_LBGK, MRT_LOWDISS = 1, 2, 3
 PROFILE_COLS = 12
+DISSIPATION_COLS = 5
 FLAG_SIMPLE_STEP = 1
 PFLAG_Q_FP64 = 1
 PROFILE_NAMES = ("ux", "uy", "uz", "uxuz", "uxuy", "uyuz", "uxux", "uyuy", "uzuz", "rho", "rhorho", "count")
@@ -60,6 +61,7 @@ EXPORTS = (
     "lbm_save_flow", "lbm_load_flow", "lbm_profiles_noalloc", "lbm_particle_params_init",
     "lbm_particles_place", "lbm_particles_set", "lbm_particles_get", "lbm_particles_get_history",
     "lbm_particles_set_history", "lbm_save_part", "lbm_load_part", "lbm_particle_counts",
+    "lbm_dissipation",
     "lbm_timing_enable", "lbm_timing_get", "lbm_strain",
     "lbm_mlp_create", "lbm_mlp_destroy", "lbm_mlp_get", "lbm_mlp_set", "lbm_mlp_set_data", "lbm_mlp_train",
     "lbm_mlp_gradient", "lbm_mlp_predict", "lbm_les_set", "lbm_les_nut", "lbm_les_training_data",
@@ -180,6 +182,7 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
         "lbm_particles_get_history": (ctypes.c_int, [ctx, dp, dp]),
         "lbm_particles_set_history": (ctypes.c_int, [ctx, dp, dp]),
         "lbm_save_part": (ctypes.c_int, [ctx, ctypes.c_char_p]),
+        "lbm_dissipation": (ctypes.c_int, [ctx, dp]),
         "lbm_load_part": (ctypes.c_int, [ctx, ctypes.c_char_p, ctypes.POINTER(LBMParticleParams)]),
         "lbm_particle_counts": (ctypes.c_int, [ctx, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
                                                ctypes.POINTER(ctypes.c_int64)]),
@@ -598,6 +601,13 @@ class Lattice:
         fp = np.ascontiguousarray(fprev, dtype=np.float64).reshape(-1, 3)
         tp = np.ascontiguousarray(tprev, dtype=np.float64).reshape(-1, 3)
         self._call("lbm_particles_set_history", _dptr(fp), _dptr(tp))
+
+    def dissipation(self) -> np.ndarray:
+        """dissipation_calc plane sums (saveload.f90:4644-4882): (nx, 5) =
+        S_ij S_ij (moments), S_ij S_ij (f - f^eq), S_xy of both, fluid nodes."""
+        out = np.empty((self.nx, DISSIPATION_COLS), dtype=np.float64)
+        self._call("lbm_dissipation", _dptr(out))
+        return out
 
     def save_part(self, path: str | Path) -> None:
         """endrunpart2D checkpoint of the spheres (savecntdpart, saveload.f90:604-647)."""

@@ -732,6 +732,25 @@ int lbm_profiles(lbm_ctx* c, double* out) {
     return LBM_OK;
 }
 
+int lbm_dissipation(lbm_ctx* c, double* out) {
+    if (check_ctx(c) || !out) return fail(LBM_ERR_INVALID_ARG, "null argument");
+    if (int rc = set_device(c)) return rc;
+    const int nb = profile_blocks(c->s);
+    const size_t need = (size_t)c->s.g.NZ * nb * LBM_DISSIPATION_COLS;
+    if (int rc = ensure_red(c, need)) return rc;
+    CK(launch_dissipation(c->s, c->parity, c->d_red, nb, c->stream));
+    std::vector<double> h(need);
+    CK(cudaMemcpyAsync(h.data(), c->d_red, need * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (int rc = sync(c)) return rc;
+    for (int z = 0; z < c->s.g.NZ; ++z)
+        for (int k = 0; k < LBM_DISSIPATION_COLS; ++k) {
+            double acc = 0.0;
+            for (int b = 0; b < nb; ++b) acc += h[((size_t)z * nb + b) * LBM_DISSIPATION_COLS + k];
+            out[k + (size_t)LBM_DISSIPATION_COLS * z] = acc;
+        }
+    return LBM_OK;
+}
+
 int lbm_diag(lbm_ctx* c, lbm_stats* st) {
     if (check_ctx(c) || !st) return fail(LBM_ERR_INVALID_ARG, "null argument");
     std::vector<double> prof((size_t)LBM_PROFILE_COLS * c->p.nx);

@@ -261,6 +261,37 @@ __global__ void k_macro(DeviceState s, int parity, double* rho, double* ux, doub
 //    (3 / 2 tau) sum_i c_ia c_ib (f_i - f_i^eq) with the incompressible
 //    equilibrium of initial.f90:26-44.
 // Outputs S_ij S_ij of both; solid nodes give 0 (the reference masks them).
+// S_ij S_ij by both methods and the wall-normal/streamwise shear S_xy of both
+// at fluid GPU node (x, y, z), FP64 (dissipation_calc, saveload.f90:4683-4778).
+struct NodeStrain { double m1, m2, sxy1, sxy2; };
+template <typename T>
+__device__ NodeStrain node_strain(const DeviceState& s, int parity, int x, int y, int z) {
+    double f[Q];
+    gather_natural<T>(s, parity, x, y, z, f);
+    const double F[3] = {(double)s.cd.Fx, (double)s.cd.Fy, (double)s.cd.Fz};
+    double rho, ux, uy, uz;
+    macro_of<double>(f, F, rho, ux, uy, uz);
+    const double s1 = (double)s.cd.ke * 2394.0, s9 = (double)s.cd.kp * 36.0;
+    NodeStrain r;
+    double S6[6];
+    strain_from_moments(f, rho, ux, uy, uz, s1, s9, S6);
+    r.m1 = S6[0] * S6[0] + S6[1] * S6[1] + S6[2] * S6[2] + 2.0 * (S6[3] * S6[3] + S6[4] * S6[4] + S6[5] * S6[5]);
+    r.sxy1 = S6[3];
+    const double usq = 1.5 * (ux * ux + uy * uy + uz * uz);
+    double a[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int i = 1; i < Q; ++i) {
+        const double cu = CXf(i) * ux + CYf(i) * uy + CZf(i) * uz;
+        const double fn = f[i] - weight(i) * (rho + 3.0 * cu + 4.5 * cu * cu - usq);
+        a[0] += fn * (CXf(i) * CXf(i)); a[1] += fn * (CYf(i) * CYf(i)); a[2] += fn * (CZf(i) * CZf(i));
+        a[3] += fn * (CXf(i) * CYf(i)); a[4] += fn * (CYf(i) * CZf(i)); a[5] += fn * (CZf(i) * CXf(i));
+    }
+    const double k = 1.5 * s9;                           // 1.5 / tau
+    r.m2 = (a[0] * a[0] + a[1] * a[1] + a[2] * a[2] + 2.0 * (a[3] * a[3] + a[4] * a[4] + a[5] * a[5])) * k * k;
+    r.sxy2 = a[3] * k;
+    return r;
+}
+
 template <typename T>
 __global__ void k_strain(DeviceState s, int parity, double* __restrict__ m1, double* __restrict__ m2, int z0) {
     const RefNode r = ref_node(s.g, z0);
@@ -272,30 +303,9 @@ __global__ void k_strain(DeviceState s, int parity, double* __restrict__ m1, dou
         if (m2) m2[o] = 0.0;
         return;
     }
-    double f[Q];
-    gather_natural<T>(s, parity, r.iy, r.iz, r.ix, f);
-    const double F[3] = {(double)s.cd.Fx, (double)s.cd.Fy, (double)s.cd.Fz};
-    double rho, ux, uy, uz;
-    macro_of<double>(f, F, rho, ux, uy, uz);
-    const double s1 = (double)s.cd.ke * 2394.0, s9 = (double)s.cd.kp * 36.0;
-    if (m1) {
-        double S6[6];
-        strain_from_moments(f, rho, ux, uy, uz, s1, s9, S6);
-        m1[o] = S6[0] * S6[0] + S6[1] * S6[1] + S6[2] * S6[2] + 2.0 * (S6[3] * S6[3] + S6[4] * S6[4] + S6[5] * S6[5]);
-    }
-    if (m2) {
-        const double usq = 1.5 * (ux * ux + uy * uy + uz * uz);
-        double a[6] = {0, 0, 0, 0, 0, 0};
-#pragma unroll
-        for (int i = 1; i < Q; ++i) {
-            const double cu = CXf(i) * ux + CYf(i) * uy + CZf(i) * uz;
-            const double fn = f[i] - weight(i) * (rho + 3.0 * cu + 4.5 * cu * cu - usq);
-            a[0] += fn * (CXf(i) * CXf(i)); a[1] += fn * (CYf(i) * CYf(i)); a[2] += fn * (CZf(i) * CZf(i));
-            a[3] += fn * (CXf(i) * CYf(i)); a[4] += fn * (CYf(i) * CZf(i)); a[5] += fn * (CZf(i) * CXf(i));
-        }
-        const double k = 1.5 * s9;                       // 1.5 / tau
-        m2[o] = (a[0] * a[0] + a[1] * a[1] + a[2] * a[2] + 2.0 * (a[3] * a[3] + a[4] * a[4] + a[5] * a[5])) * k * k;
-    }
+    const NodeStrain v = node_strain<T>(s, parity, r.iy, r.iz, r.ix);
+    if (m1) m1[o] = v.m1;
+    if (m2) m2[o] = v.m2;
 }
 
 // Training data of the closure, step 1: box filter of u and u_i u_j over
@@ -413,6 +423,36 @@ constexpr int kRedThreads = 256;
 
 // Plane sums for statistc2: block (b, Z) covers part of plane Z (ref x = Z+1).
 // Per-node values in the diagnostics type R, sums in FP64.
+// Plane sums of dissipation_calc (saveload.f90:4780-4814) over the fluid
+// nodes of each wall-normal plane: {S_ij S_ij method 1, method 2, S_xy method
+// 1, method 2, fluid nodes}; partial[NZ][nblk][LBM_DISSIPATION_COLS].
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_dissipation(DeviceState s, int parity, double* __restrict__ partial) {
+    const Geometry& g = s.g;
+    const int z = blockIdx.y;
+    double acc[LBM_DISSIPATION_COLS] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    const uint32_t plane = g.NXY;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < plane; t += gridDim.x * blockDim.x) {
+        if (s.owner && s.owner[t + plane * (uint32_t)z] >= 0) continue;     // solid node
+        const NodeStrain v = node_strain<T>(s, parity, (int)(t % g.NX), (int)(t / g.NX), z);
+        acc[0] += v.m1; acc[1] += v.m2; acc[2] += v.sxy1; acc[3] += v.sxy2; acc[4] += 1.0;
+    }
+    __shared__ double sh[LBM_DISSIPATION_COLS][kRedThreads / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < LBM_DISSIPATION_COLS; ++k) {
+        double v = acc[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) sh[k][wid] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < LBM_DISSIPATION_COLS) {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x / 32); ++w) v += sh[threadIdx.x][w];
+        partial[((size_t)z * gridDim.x + blockIdx.x) * LBM_DISSIPATION_COLS + threadIdx.x] = v;
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kRedThreads)
 k_profiles(DeviceState s, int parity, double* __restrict__ partial) {
@@ -790,6 +830,10 @@ int profile_blocks(const DeviceState& s) {
     const uint32_t plane = s.g.NXY;
     int nb = (int)((plane + kRedThreads * 8 - 1) / (kRedThreads * 8));
     return nb < 1 ? 1 : (nb > 64 ? 64 : nb);
+}
+
+cudaError_t launch_dissipation(const DeviceState& s, int parity, double* partial, int nblk, cudaStream_t st) {
+    LBM_DISPATCH(s.prec, (k_dissipation<T><<<dim3(nblk, s.g.NZ), kRedThreads, 0, st>>>(s, parity, partial)))
 }
 
 cudaError_t launch_profiles(const DeviceState& s, int parity, double* partial, int nblk,

@@ -146,6 +146,9 @@ cudaError_t launch_ref_to_gpu_vec(const DeviceState& s, const double* ux,
 cudaError_t launch_profiles(const DeviceState& s, int parity, double* partial,
                             int nblk, cudaStream_t st);
 int profile_blocks(const DeviceState& s);
+// dissipation_calc plane sums (LBM_DISSIPATION_COLS per wall-normal plane),
+// same partial layout and block count as launch_profiles
+cudaError_t launch_dissipation(const DeviceState& s, int parity, double* partial, int nblk, cudaStream_t st);
 // per-block extrema for diag: partial[kExtremaBlocks][5] =
 // {rho_max, rho_min, vmax, reference linear index of vmax, nonfinite count}
 constexpr int kExtremaBlocks = 1024;

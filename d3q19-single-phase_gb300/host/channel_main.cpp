@@ -30,6 +30,8 @@
 //   restart           checkpoint to continue from (endrunflow format)
 //   save              1: write endrunflow2D16x8.<istep>.000 at the end
 //   time_limit        wall-clock bound in seconds (para.f90:50-55)
+//   ndiss             every ndiss steps append dissipation.dat (dissipation_calc,
+//                     saveload.f90:4644-4882); 0 = off, as the reference's main loop
 //   npart rad rhopart spheres: count, radius, density ratio (0 spheres: ipart off)
 //   iseedp gap wgap   seeded placement: seed, surface gaps sphere-sphere and sphere-wall
 //   qfp64             1: boundary-link fractions in FP64 for FP32/FP16 storage
@@ -94,6 +96,24 @@ void write_profiles(const std::string& path, const std::vector<double>& prof, in
         if (i > lxh) yplus = (nx - i + 0.5) / ystar;
         std::fprintf(fp, "  %15.6E%15.6E%15.6E%15.6E%15.6E%15.6E%15.6E%15.6E%15.6E%15.6E%15.6E%15.6E%15.6E%15.6E%15.6E\n",
                      i - 0.5, yplus, vx, vy, vz, sxx, syy, szz, sxz, sxy, syz, pr, prsq, volf, 1.0 - volf);
+    }
+    std::fclose(fp);
+}
+
+// dissipation_calc output (saveload.f90:4846-4872): plane means of S_ij S_ij
+// and S_xy by both methods
+void write_dissipation(const std::string& path, const std::vector<double>& d, int nx, long istep, double ystar) {
+    FILE* fp = std::fopen(path.c_str(), "a");
+    if (!fp) return;
+    std::fprintf(fp, " %ld\n", istep);
+    const int lxh = nx / 2;
+    for (int i = 1; i <= nx; ++i) {
+        const double* r = &d[(size_t)LBM_DISSIPATION_COLS * (i - 1)];
+        const double n = r[4];
+        double yplus = (i - 0.5) / ystar;
+        if (i > lxh) yplus = (nx - i + 0.5) / ystar;
+        std::fprintf(fp, "  %16.6E%16.6E%16.6E%16.6E%16.6E%16.6E\n", i - 0.5, yplus, r[0] / n, r[1] / n, r[2] / n,
+                     r[3] / n);
     }
     std::fclose(fp);
 }
@@ -172,7 +192,8 @@ int main(int argc, char** argv) {
     std::printf("Loading successful\n");
 
     const double ystar = visc / ustar;
-    std::vector<double> prof((size_t)LBM_PROFILE_COLS * nx);
+    std::vector<double> prof((size_t)LBM_PROFILE_COLS * nx), diss((size_t)LBM_DISSIPATION_COLS * nx);
+    const long ndiss = argi("ndiss", 0);
     const auto t0 = std::chrono::steady_clock::now();
     long istep = istep0;
     for (istep = istep0 + 1; istep <= istep0 + nsteps; ++istep) {
@@ -204,6 +225,10 @@ int main(int argc, char** argv) {
         if (istep % nstat == 0) {
             check(lbm_profiles(ctx, prof.data()), "statistc2");
             write_profiles(out + "/profiles2.dat", prof, nx, istep, ustar, ystar, (long)ny * nz);
+        }
+        if (ndiss > 0 && istep % ndiss == 0) {
+            check(lbm_dissipation(ctx, diss.data()), "dissipation_calc");
+            write_dissipation(out + "/dissipation.dat", diss, nx, istep, ystar);
         }
         const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         if (el > time_bond) break;

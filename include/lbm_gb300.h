@@ -114,6 +114,7 @@ typedef struct lbm_stats {
  * sum over the plane of: ux, uy, uz, ux*uz, ux*uy, uy*uz, ux^2, uy^2, uz^2,
  * rho, rho^2, fluid count (the sums of statistc2, saveload.f90:1392-1423). */
 #define LBM_PROFILE_COLS 12
+#define LBM_DISSIPATION_COLS 5
 
 typedef struct lbm_ctx lbm_ctx;
 
@@ -206,6 +207,16 @@ int lbm_diag(lbm_ctx* ctx, lbm_stats* st);
  * be NULL); solid nodes give 0. */
 int lbm_strain(lbm_ctx* ctx, double* sij2_m1, double* sij2_m2);
 
+/* Plane sums of dissipation_calc (saveload.f90:4644-4882) over the fluid
+ * nodes of each wall-normal plane: out[LBM_DISSIPATION_COLS*nx] with column c
+ * of plane ix at out[c + LBM_DISSIPATION_COLS*(ix-1)]: S_ij S_ij from the
+ * non-equilibrium moments (method 1), from f - f^eq (method 2), S_xy of both
+ * methods (x wall-normal, y streamwise), each with the reference's formula
+ * and sign: -1.5 neqm13 (= +du_y/dx / 2 in a shear flow u_y(x)) and
+ * (1.5/tau) sum f_neq c_x c_y (= -du_y/dx / 2), and the fluid node count.  Divided
+ * by the count they are the columns 3-6 of dissipation.dat; epsilon =
+ * 2 nu <S_ij S_ij>.  FP64 per node. */
+int lbm_dissipation(lbm_ctx* ctx, double* out);
 /* Plane sums for statistc/statistc2: out[LBM_PROFILE_COLS*nx], column-major
  * (column c of plane ix at out[c + LBM_PROFILE_COLS*(ix-1)]). FP64. */
 int lbm_profiles(lbm_ctx* ctx, double* out);

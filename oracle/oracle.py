@@ -351,6 +351,28 @@ def strain_sij2(p: OrcParams, f: np.ndarray, s1: float, s9: float):
     return m1, m2
 
 
+def dissipation_sums(p: OrcParams, f: np.ndarray, s1: float, s9: float, solid=None):
+    """dissipation_calc (saveload.f90:4644-4882): per wall-normal plane the
+    sums over fluid nodes of S_ij S_ij (moments, f - f^eq) and S_xy of both
+    methods, and the fluid count; (nx, 5).  S_xy: -1.5 neqm13 (:4730) and
+    (1.5 / tau) sum fneq c_x c_y (:4772).  solid: (nx, ny, nz) bool or None."""
+    m1, m2 = strain_sij2(p, f, s1, s9)
+    rho, ux, uy, uz = macrovar(p, f)
+    sxy1 = strain_tensor(p, f, s1, s9)[3]
+    usqr = 1.5 * (ux * ux + uy * uy + uz * uz)
+    a = np.zeros_like(rho)
+    for i in range(1, Q):
+        cu = CX[i] * ux + CY[i] * uy + CZ[i] * uz
+        a += (f[i] - W[i] * (rho + 3.0 * cu + 4.5 * cu * cu - usqr)) * CX[i] * CY[i]
+    sxy2 = a * (1.5 * s9)
+    fluid = np.ones_like(m1, dtype=bool) if solid is None else ~solid
+    out = np.empty((m1.shape[0], 5))
+    for k, v in enumerate((m1, m2, sxy1, sxy2)):
+        out[:, k] = np.where(fluid, v, 0.0).sum(axis=(1, 2))
+    out[:, 4] = fluid.sum(axis=(1, 2))
+    return out
+
+
 # ---- learned LES closure network (no reference counterpart) -----------------
 MLP_IN, MLP_H = 7, 32
 MLP_PARAMS = MLP_IN * MLP_H + MLP_H + MLP_H * MLP_H + MLP_H + MLP_H + 1

@@ -145,7 +145,7 @@ def test_part_checkpoint_round_trip(pkg, tmp_path):
 def test_driver_sphere_run_equals_binding(pkg, driver, tmp_path):
     steps = 30
     out = tmp_path / "drv"
-    log = run_driver(driver, out, steps=steps, ndiag=10, nstat=30, save=1, **COMMON)
+    log = run_driver(driver, out, steps=steps, ndiag=10, nstat=30, ndiss=15, save=1, **COMMON)
     assert "spheres: 3" in log
     nx, ny, nz = SHAPE
     force = COMMON["ustar"] ** 2 / COMMON["h"]
@@ -180,6 +180,11 @@ def test_driver_sphere_run_equals_binding(pkg, driver, tmp_path):
     prof = (out / "profiles2.dat").read_text().splitlines()
     assert prof[0].split() == ["30"] and len(prof) == 1 + nx
     assert all(len(ln.split()) == 15 for ln in prof[1:])
+    # dissipation.dat: two blocks (steps 15, 30) of nx rows of 6 columns
+    dis = (out / "dissipation.dat").read_text().splitlines()
+    assert len(dis) == 2 * (1 + nx) and dis[0].split() == ["15"] and dis[1 + nx].split() == ["30"]
+    rows = np.array([[float(v) for v in ln.split()] for ln in dis[2 + nx:]])
+    assert rows.shape == (nx, 6) and (rows[:, 2] > 0).all() and (rows[:, 3] > 0).all()
 
 
 def test_driver_restart_continues_sphere_run(driver, tmp_path):

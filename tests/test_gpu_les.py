@@ -53,6 +53,47 @@ def test_strain_masks_solid_nodes(pkg, orc):
     assert (m1[~solid] > 0).mean() > 0.99
 
 
+@pytest.mark.parametrize("shape", [(12, 16, 10), (7, 9, 5)])
+def test_dissipation_fp64_matches_oracle(pkg, orc, shape):
+    """dissipation_calc's plane sums (saveload.f90:4644-4882) at parity 1 and 0."""
+    nx, ny, nz = shape
+    run = pkg.RunParams(nx=nx, ny=ny, nz=nz, visc=0.01, force_y=1e-5, mrt_type=1,
+                        precision=pkg.PRECISIONS["fp64"])
+    f0 = random_f(orc, shape, seed=5)
+    p = orc.params_from(run)
+    r = run.rates()
+    with pkg.Lattice(run) as lat:
+        lat.upload_f(f0)
+        for n in (3, 1):
+            lat.step(n)
+            got = lat.dissipation()
+            want = orc.dissipation_sums(p, lat.download_f(), r["s1"], r["s9"])
+            assert (got[:, 4] == want[:, 4]).all()
+            for k in range(4):
+                assert rel(got[:, k], want[:, k]) < 1e-10, k
+
+
+def test_dissipation_with_spheres_sums_strain(pkg):
+    """With spheres the sums run over fluid nodes only and equal the plane
+    sums of lbm_strain's per-node values (FP32 storage)."""
+    shape = (24, 32, 22)
+    run = pkg.RunParams(nx=shape[0], ny=shape[1], nz=shape[2], visc=0.02, force_y=2e-6, mrt_type=1,
+                        precision=pkg.PRECISIONS["fp32"])
+    pos = np.array([[12.0, 16.0, 11.0], [6.5, 4.0, 5.0]])
+    with pkg.Lattice(run) as lat:
+        lat.init_channel(0.04, 0.05, 3)
+        lat.set_particles(pos, radius=4.0, rho_ratio=2.0)
+        lat.step(5)
+        d = lat.dissipation()
+        m1, m2 = lat.strain()
+        rho = lat.macrovar()[0]
+    fluid = rho != 2.0
+    assert (d[:, 4] == fluid.sum(axis=(1, 2))).all() and d[:, 4].min() < shape[1] * shape[2]
+    assert rel(d[:, 0], m1.sum(axis=(1, 2))) < 1e-12
+    assert rel(d[:, 1], m2.sum(axis=(1, 2))) < 1e-12
+    assert np.isfinite(d).all() and (d[:, 0] > 0).all()
+
+
 def net_and_data(orc, n=1000, seed=0):
     rng = np.random.default_rng(seed)
     p = rng.normal(0, 0.3, orc.MLP_PARAMS).astype(np.float32)

@@ -1,6 +1,7 @@
 """CPU checks of the oracle's strain rate (sijstat01's two methods): both give
 the analytic S_ij S_ij of a laminar Poiseuille flow, and agree with each
-other on a developed channel."""
+other on a developed channel; dissipation_calc's plane statistics give the
+analytic shear S_xy."""
 from __future__ import annotations
 
 import numpy as np
@@ -24,6 +25,20 @@ def test_poiseuille_strain_both_methods(orc):
         prof = m.mean(axis=(1, 2))
         assert np.abs(prof - exact).max() < 2e-2 * exact.max()
     assert np.abs(m1 - m2).max() < 2e-2 * exact.max()
+    # dissipation_calc's plane means: the same S_ij S_ij, and its two S_xy
+    # columns as the reference writes them: method 1 (-1.5 neqm13) gives
+    # +du/dx / 2, method 2 ((1.5 / tau) sum f_neq c_x c_y, with Chapman-Enskog
+    # sum f_neq c_x c_y = -(2 tau / 3) S_xy) gives -du/dx / 2
+    d = orc.dissipation_sums(p, f, rates["s1"], rates["s9"])
+    assert (d[:, 4] == ny * nz).all()
+    assert np.allclose(d[:, 0] / d[:, 4], m1.mean(axis=(1, 2)), rtol=1e-12, atol=0)
+    assert np.allclose(d[:, 1] / d[:, 4], m2.mean(axis=(1, 2)), rtol=1e-12, atol=0)
+    for k, sign in ((2, 1.0), (3, -1.0)):
+        assert np.abs(d[:, k] / d[:, 4] - sign * 0.5 * dudx).max() < 2e-2 * np.abs(0.5 * dudx).max()
+    solid = np.zeros((nx, ny, nz), dtype=bool)
+    solid[3, 1, 2] = True
+    ds = orc.dissipation_sums(p, f, rates["s1"], rates["s9"], solid)
+    assert ds[3, 4] == ny * nz - 1 and np.isclose(ds[3, 0], d[3, 0] - m1[3, 1, 2], rtol=1e-12)
 
 
 def test_strain_zero_at_equilibrium(orc):
