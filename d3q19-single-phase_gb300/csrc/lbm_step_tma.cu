@@ -9,16 +9,19 @@
 // copy per population.  Rows along X wrap onto themselves, which makes the
 // periodic x-shift of the odd step a modular index inside shared memory.
 //
-// Each persistent CTA owns one SM and a ring of NSTAGE stage buffers of 19
-// rows, each with an mbarrier that completes when its 19 bulk copies have
-// landed (expect_tx = 19 rows).  There is no CTA-wide barrier in the steady
-// state: every warp computes its share of an item (two adjacent nodes per
-// thread, results stored straight to HBM: aligned pairs as one 32/64-bit
-// store, x-shifted populations element-wise), then counts itself done on the
-// stage's counter; the last warp to finish a stage refills it with the item
-// NSTAGE ahead (lane i copies population i).  Warps therefore drift freely up
-// to NSTAGE-1 items apart, and NSTAGE-1 items are in flight per SM, so the
-// bytes in flight are set by shared memory, not by registers.
+// Each persistent CTA owns a ring of NSTAGE stage buffers of 19 rows, each
+// with an mbarrier that completes when its 19 bulk copies have landed
+// (expect_tx = 19 rows).  There is no CTA-wide barrier in the steady state:
+// every warp computes its share of an item (two adjacent nodes per thread)
+// and writes the results back into the stage in place -- in the AA pattern
+// each node's outputs land exactly on stage positions that the same node
+// read, so no other thread is disturbed -- then counts itself done on the
+// stage's counter.  The last warp to finish a stage copies its 19 result
+// rows back to HBM with bulk stores (lane i: the row slot i came from),
+// waits until they have read the stage, and refills it with the item NSTAGE
+// ahead.  Warps therefore drift freely up to NSTAGE-1 items apart, both
+// directions of HBM traffic are whole-row bulk copies, and the bytes in
+// flight are set by shared memory, not by registers.
 //
 // Every mbarrier wait is bounded; a wait that gives up sets the error flag
 // and the warp carries on with whatever the buffer holds, so the kernel always
@@ -62,6 +65,19 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
+// shared -> global bulk copy in this thread's bulk group
+__device__ __forceinline__ void bulk_store(void* dst, uint32_t src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(src), "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+// this thread's bulk stores have finished reading shared memory
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// this thread's bulk stores are complete
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+// generic-proxy shared-memory writes of this thread become visible to the
+// async proxy (the bulk copies)
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 // storage <-> arithmetic helpers for an aligned pair / a single element
 __device__ __forceinline__ void ld_pair(const __half* p, float& a, float& b) {
@@ -157,10 +173,17 @@ __device__ __forceinline__ void issue_item(const PopPtrs<T>& P, const Geometry& 
     }
 }
 
-// Two adjacent nodes (x, x+1), x even, of one item.
+// Two adjacent nodes (x, x+1), x even, of one item; the results go back into
+// the stage buffer.  Output population i belongs in the row that stage slot
+// opp(i) was loaded from (even step: plane opp(i) of this row; odd step:
+// plane i of row (Y,Z)+c_i, the source row of slot opp(i); at a wall the
+// bounced population stays in this row, which is again slot opp(i)), at the
+// position x + c_ix (x at a wall and in the even step), from which the same
+// node read slot opp(i).  Every thread therefore overwrites only stage
+// positions that it has read itself, and the finished stage holds the item's
+// results row for row, to be copied back to the addresses it was loaded from.
 template <typename T, bool ODD, int WALL, bool YF>
-__device__ __forceinline__ void pair_update(const PopPtrs<T>& P, const CollideConsts<float>& C,
-                                            const Geometry& g, const Item& I, const T* stage, int x) {
+__device__ __forceinline__ void pair_update(const CollideConsts<float>& C, const Geometry& g, T* stage, int x) {
     const int NX = g.NX;
     const int xm1 = (x == 0) ? NX - 1 : x - 1;
     const int xp2 = (x + 2 == NX) ? 0 : x + 2;
@@ -182,9 +205,8 @@ __device__ __forceinline__ void pair_update(const PopPtrs<T>& P, const CollideCo
     collide<float, false, YF>(fb, C, 0.f, 0.f, 0.f, rho, jx, jy, jz);
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
-        const bool local = !ODD || push_bb(WALL, i);
-        const int sh = local ? 0 : DXg(i);
-        T* d = local ? P.p[OPPf(i)] + I.row : P.p[i] + row_at(g, I.y + DYg(i), I.z + DZg(i));
+        const int sh = (ODD && !push_bb(WALL, i)) ? DXg(i) : 0;
+        T* d = stage + OPPf(i) * NX;
         if (sh == 0) {
             st_pair(d + x, fa[i], fb[i]);
         } else if (sh == 1) {
@@ -196,12 +218,27 @@ __device__ __forceinline__ void pair_update(const PopPtrs<T>& P, const CollideCo
 }
 
 // All pairs of an item handled by this thread; the wall case is fixed for
-// the whole loop so that row offsets can be hoisted out of it.
+// the whole loop.
 template <typename T, bool ODD, int WALL, bool YF>
-__device__ __forceinline__ void item_pairs(const PopPtrs<T>& P, const CollideConsts<float>& C, const Geometry& g,
-                                           const Item& I, const T* stage, int tid, int nthreads) {
+__device__ __forceinline__ void item_pairs(const CollideConsts<float>& C, const Geometry& g, T* stage, int tid,
+                                           int nthreads) {
     const int npairs = g.NX >> 1;
-    for (int p = tid; p < npairs; p += nthreads) pair_update<T, ODD, WALL, YF>(P, C, g, I, stage, 2 * p);
+    for (int p = tid; p < npairs; p += nthreads) pair_update<T, ODD, WALL, YF>(C, g, stage, 2 * p);
+}
+
+// Issued by the last warp to finish an item: lane i copies result row i back
+// to the row that slot i was loaded from, then waits until the copy has read
+// the stage (the stage is refilled next).
+template <typename T, bool ODD>
+__device__ __forceinline__ void store_item(const PopPtrs<T>& P, const Geometry& g, uint32_t it, uint32_t stage_smem,
+                                           uint32_t row_bytes, int lane) {
+    if (lane < Q) {
+        const Item I = item_of(g, it);
+        bulk_store(const_cast<T*>(src_row<T, ODD>(P, g, I, wall_of(g, I.z), lane)),
+                   stage_smem + (uint32_t)lane * row_bytes, row_bytes);
+        bulk_wait_read();
+    }
+    __syncwarp();
 }
 
 constexpr int kMaxStages = 5;
@@ -215,7 +252,7 @@ k_step_rows(PopPtrs<T> P, CollideConsts<float> C, Geometry g, int nstage, int* e
     const uint32_t stage_bytes = (uint32_t)Q * row_bytes;
     const uint32_t bars = smem_addr(smem);                 // nstage mbarriers (8 B each)
     const uint32_t data = bars + 128;                       // stage buffers, 16-B aligned
-    const T* const stage_ptr0 = reinterpret_cast<const T*>(smem + 128);
+    T* const stage_ptr0 = reinterpret_cast<T*>(smem + 128);
     const uint32_t total = (uint32_t)g.NY * (uint32_t)g.NZ;
     const uint32_t G = gridDim.x;
     const int tid = threadIdx.x;
@@ -244,12 +281,14 @@ k_step_rows(PopPtrs<T> P, CollideConsts<float> C, Geometry g, int nstage, int* e
         if (!mbar_wait(bars + 8 * s, (k / (uint32_t)nstage) & 1u)) failed = true;
         const Item I = item_of(g, it);
         const int wall = wall_of(g, I.z);
-        const T* stage = stage_ptr0 + (size_t)s * Q * g.NX;
-        if (wall == 0)      item_pairs<T, ODD, 0, YF>(P, C, g, I, stage, tid, NT);
-        else if (wall == 1) item_pairs<T, ODD, 1, YF>(P, C, g, I, stage, tid, NT);
-        else if (wall == 2) item_pairs<T, ODD, 2, YF>(P, C, g, I, stage, tid, NT);
-        else                item_pairs<T, ODD, 3, YF>(P, C, g, I, stage, tid, NT);
-        // this warp has finished reading stage s; the last warp refills it
+        T* stage = stage_ptr0 + (size_t)s * Q * g.NX;
+        if (wall == 0)      item_pairs<T, ODD, 0, YF>(C, g, stage, tid, NT);
+        else if (wall == 1) item_pairs<T, ODD, 1, YF>(C, g, stage, tid, NT);
+        else if (wall == 2) item_pairs<T, ODD, 2, YF>(C, g, stage, tid, NT);
+        else                item_pairs<T, ODD, 3, YF>(C, g, stage, tid, NT);
+        // this warp has finished with stage s; the last warp copies the
+        // results back and refills it
+        fence_proxy_async();
         __syncwarp();
         unsigned last = 0;
         if (lane == 0) {
@@ -260,10 +299,13 @@ k_step_rows(PopPtrs<T> P, CollideConsts<float> C, Geometry g, int nstage, int* e
         last = __shfl_sync(0xffffffffu, last, 0);
         if (last) {
             __threadfence_block();
+            fence_proxy_async();
+            store_item<T, ODD>(P, g, it, data + s * stage_bytes, row_bytes, lane);
             const uint32_t nit = blockIdx.x + (k + (uint32_t)nstage) * G;
             if (nit < total) issue_item<T, ODD>(P, g, nit, data + s * stage_bytes, bars + 8 * s, row_bytes, lane);
         }
     }
+    bulk_wait_all();
     if (failed) atomicExch(err, 1);
 }
 
