@@ -291,11 +291,13 @@ def run_gpu(args, world, rank, local):
     sampler.start()
     time.sleep(0.3)
     parity0 = lat.step_count() % 2
+    launches0 = lat.step_launches()
     lat.timing_enable(args.steps)
     for k in range(args.steps):
         evs[k].record(stream)
         lat.step_async(1)
     evs[-1].record(stream)
+    launches = lat.step_launches() - launches0
     lat.synchronize()
     torch.cuda.synchronize()
     barrier(world)
@@ -359,7 +361,7 @@ def run_gpu(args, world, rank, local):
                        "ustar": cfg.ustar, "h": cfg.h, "mrt": "MRTtype 1 (para.f90)" + (f", s16={cfg.s16} (sphere-laden)" if cfg.s16 else ""),
                        "l2": f"populations {N * 19 * BYTES[prec] / 1e9:.1f} GB >> 129 MB L2, no flush needed",
                        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
-            "roofline": roof, "clocks": clocks, "gpu_launches": args.steps,
+            "roofline": roof, "clocks": clocks, "gpu_launches": launches,
             "e2e": e2e, "cpu_baseline": cpu, "accuracy": accuracy,
         }
         print(json.dumps(line), flush=True)

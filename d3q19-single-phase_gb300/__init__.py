@@ -62,7 +62,7 @@ EXPORTS = (
     "lbm_particles_place", "lbm_particles_set", "lbm_particles_get", "lbm_particles_get_history",
     "lbm_particles_set_history", "lbm_save_part", "lbm_load_part", "lbm_particle_counts",
     "lbm_dissipation",
-    "lbm_timing_enable", "lbm_timing_get", "lbm_strain",
+    "lbm_timing_enable", "lbm_timing_get", "lbm_step_launches", "lbm_strain",
     "lbm_mlp_create", "lbm_mlp_destroy", "lbm_mlp_get", "lbm_mlp_set", "lbm_mlp_set_data", "lbm_mlp_train",
     "lbm_mlp_gradient", "lbm_mlp_predict", "lbm_les_set", "lbm_les_nut", "lbm_les_training_data",
     "lbm_les_features",
@@ -146,6 +146,7 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
         "lbm_synchronize": (ctypes.c_int, [ctx]),
         "lbm_stream": (ctypes.c_int, [ctx, ctypes.POINTER(ctypes.c_void_p)]),
         "lbm_step_count": (ctypes.c_int, [ctx, ctypes.POINTER(ctypes.c_int64)]),
+        "lbm_step_launches": (ctypes.c_int, [ctx, ctypes.POINTER(ctypes.c_int64)]),
         "lbm_set_step_count": (ctypes.c_int, [ctx, ctypes.c_int64]),
         "lbm_prerelax": (ctypes.c_int, [ctx, dp, dp, dp, ctypes.c_double, ctypes.c_int32,
                                         ctypes.POINTER(ctypes.c_int32), dp]),
@@ -501,6 +502,12 @@ class Lattice:
     def step_count(self) -> int:
         n = ctypes.c_int64()
         self._call("lbm_step_count", ctypes.byref(n))
+        return n.value
+
+    def step_launches(self) -> int:
+        """Kernels launched by the steps of this context so far."""
+        n = ctypes.c_int64()
+        self._call("lbm_step_launches", ctypes.byref(n))
         return n.value
 
     def set_step_count(self, n: int) -> None:

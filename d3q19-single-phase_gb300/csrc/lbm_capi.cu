@@ -21,6 +21,7 @@ struct lbm_ctx {
     cudaStream_t stream = nullptr;
     int parity = 0;            // 0: natural orientation, 1: after an even AA step
     int64_t nsteps = 0;
+    int64_t nlaunch = 0;          // kernels launched by lbm_step / lbm_step_async
     double* d_stage = nullptr; // FP64 staging for layout conversion
     double* d_mass = nullptr;  // fluid mass and node count (mean-density removal)
     float* d_les = nullptr;    // closure network parameters + normalisation
@@ -483,12 +484,14 @@ int lbm_step_async(lbm_ctx* c, int32_t nsteps) {
         if (timed) CK(cudaEventRecord(c->tev[3 * c->tn], c->stream));
         if (c->s.use_rows) CK(launch_step_rows(c->s, c->parity, c->d_err, c->stream));
         else CK(launch_step(c->s, c->parity, c->stream));
+        ++c->nlaunch;
         if (timed) CK(cudaEventRecord(c->tev[3 * c->tn + 1], c->stream));
         const int was = c->parity;
         c->parity ^= 1;
         ++c->nsteps;
         if (c->P.npart > 0) {
             CK(particles_after_step(c->s, c->P, c->parity, c->have_prev, c->stream));
+            c->nlaunch += particles_kernels_per_step(c->P);
             c->have_prev = 1;
             // main.f90:163-167: with particles, every 100 steps the mean
             // density is removed to correct the mass the interpolated
@@ -496,6 +499,7 @@ int lbm_step_async(lbm_ctx* c, int32_t nsteps) {
             if (c->nsteps % 100 == 0) {
                 CK(launch_remove_mean_density(c->s, c->parity, c->d_mass, c->stream));
                 CK(launch_remove_mean_apply(c->s, c->d_mass, c->stream));
+                c->nlaunch += 2;
             }
         }
         if (timed) {
@@ -1234,6 +1238,12 @@ int lbm_timing_enable(lbm_ctx* c, int32_t capacity) {
     c->tpar.assign(capacity, 0);
     c->tcap = capacity;
     c->tn = 0;
+    return LBM_OK;
+}
+
+int lbm_step_launches(const lbm_ctx* c, int64_t* n) {
+    if (!c || !n) return fail(LBM_ERR_INVALID_ARG, "null argument");
+    *n = c->nlaunch;
     return LBM_OK;
 }
 

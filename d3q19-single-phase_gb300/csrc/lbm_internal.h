@@ -175,6 +175,8 @@ size_t particles_smem_bytes(double R);
 cudaError_t particles_claim(const DeviceState& s, const DeviceParticles& P, cudaStream_t st);
 cudaError_t particles_after_step(const DeviceState& s, const DeviceParticles& P, int parity, int have_prev,
                                  cudaStream_t st);
+// kernels that one particles_after_step launches
+int particles_kernels_per_step(const DeviceParticles& P);
 cudaError_t particles_count_solid(const DeviceState& s, const DeviceParticles& P, unsigned long long* d_out,
                                   cudaStream_t st);
 

@@ -1200,6 +1200,13 @@ cudaError_t particles_after_step(const DeviceState& s, const DeviceParticles& P,
     return cudaGetLastError();
 }
 
+// k_ibb, repulsion (k_bin + k_repulsion_cells, or k_repulsion), k_newton,
+// two k_shell, k_reclaim, k_refill, k_refill_done
+int particles_kernels_per_step(const DeviceParticles& P) {
+    if (P.npart == 0) return 0;
+    return P.ncell > 0 ? 9 : 8;
+}
+
 cudaError_t particles_count_solid(const DeviceState& s, const DeviceParticles& P, unsigned long long* d_out,
                                   cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(d_out, 0, sizeof(unsigned long long), st);

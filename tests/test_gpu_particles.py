@@ -236,3 +236,21 @@ def test_mean_density_removed_at_odd_parity(pkg, orc):
         assert lat.step_count() == 100
     assert abs(d99.rho_sum / d99.nfluid) > 1e-9
     assert abs(d100.rho_sum / d100.nfluid) < 1e-13
+
+
+def test_step_launch_count(pkg, orc):
+    """lbm_step_launches counts the kernels the steps launch: one per fluid
+    step, the sphere pass after each step, and the two kernels of the
+    mean-density removal at every step number that is a multiple of 100."""
+    shape = (24, 32, 22)
+    run, f0 = channel_with_spheres(orc, pkg, shape, POS)
+    with pkg.Lattice(run) as lat:
+        lat.upload_f(f0)
+        n0 = lat.step_launches()
+        lat.step(3)
+        assert lat.step_launches() - n0 == 3          # fluid only
+        lat.set_particles(POS, radius=4.0, rho_ratio=2.0, vel=VEL)
+        n1, s1 = lat.step_launches(), lat.step_count()
+        lat.step(110)
+        per = (lat.step_launches() - n1 - 2 * sum(1 for k in range(s1 + 1, s1 + 111) if k % 100 == 0)) / 110
+        assert per in (9.0, 10.0)                      # 1 fluid + 8 or 9 sphere kernels
