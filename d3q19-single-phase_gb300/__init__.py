@@ -598,7 +598,7 @@ class Lattice:
         self._call("lbm_particles_set", ctypes.byref(pp), _dptr(pos), _dptr(v), _dptr(o))
 
     def particle_history(self) -> tuple[np.ndarray, np.ndarray]:
-        """Total force and torque of the previous step (Adams-Bashforth history)."""
+        """Total force and torque of the previous step (the force history)."""
         n = getattr(self, "_npart", 0)
         fp, tp = np.empty((n, 3)), np.empty((n, 3))
         self._call("lbm_particles_get_history", _dptr(fp), _dptr(tp))

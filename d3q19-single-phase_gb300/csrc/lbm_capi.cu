@@ -36,7 +36,7 @@ struct lbm_ctx {
     int* d_err = nullptr;      // set by a kernel whose bounded wait gave up
     DeviceParticles P{};       // spheres (npart == 0: none)
     lbm_particle_params pp{};
-    int have_prev = 0;         // Adams-Bashforth history available
+    int have_prev = 0;         // previous-step force and torque available
     unsigned long long* d_count = nullptr;
     // per-step timing (lbm_timing_enable): 3 events per recorded step
     std::vector<cudaEvent_t> tev;

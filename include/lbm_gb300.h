@@ -267,7 +267,8 @@ int lbm_load_flow(lbm_ctx* ctx, const char* path, int32_t kind,
  * every lbm_step also does: interpolated bounce-back (quadratic Bouzidi,
  * moving wall) and Galilean-invariant momentum exchange on every boundary
  * link, soft-sphere repulsion (sphere-sphere and sphere-wall), the FP64
- * Newton-Euler update (second-order Adams-Bashforth), the geometry update and
+ * Newton-Euler update (driven by the average of this step's and the previous
+ * step's force and torque), the geometry update and
  * the refilling of uncovered nodes.  Positions are in reference axes with node
  * (ix,iy,iz) (1-based) at (ix-1/2, iy-1/2, iz-1/2), as in macrovar. */
 typedef struct lbm_particle_params {
@@ -304,10 +305,11 @@ int lbm_particles_set(lbm_ctx* ctx, const lbm_particle_params* pp,
  * torque are the hydrodynamic (momentum-exchange) parts of the last step. */
 int lbm_particles_get(lbm_ctx* ctx, double* pos, double* vel, double* omg,
                       double* force, double* torque);
-/* Adams-Bashforth history: total force and torque (hydrodynamic + repulsion
- * + body force) of the previous step, forcepp/torqpp of savecntdpart01
- * (saveload.f90:523-560).  set: continue a run with its second-order update
- * (without it the first update after lbm_particles_set is first order). */
+/* Force history: total force and torque (hydrodynamic + repulsion + body
+ * force) of the previous step, forcepp/torqpp of savecntdpart01
+ * (saveload.f90:523-560), which the Newton-Euler update averages with the
+ * current step's.  set: continue a run exactly (without it the first update
+ * after lbm_particles_set uses the current force alone). */
 int lbm_particles_get_history(lbm_ctx* ctx, double* fprev, double* tprev);
 int lbm_particles_set_history(lbm_ctx* ctx, const double* fprev, const double* tprev);
 /* Particle checkpoint in the reference's endrunpart2D format for one
@@ -318,7 +320,7 @@ int lbm_particles_set_history(lbm_ctx* ctx, const double* fprev, const double* t
  *   {dwdt(3,msize), domgdt(3,msize)} {ypglb(3,npart), wp(3,npart), omgp(3,npart)}
  * with msize = 10 npart (para.f90:369, one process), ibnodes 1 solid / -1
  * fluid, isnodes the 1-based owning sphere / -1, forcepp/torqpp the
- * Adams-Bashforth history (total force and torque of the last step),
+ * force history (total force and torque of the last step),
  * dwdt/domgdt that force / mass and torque / moment of inertia, thetap zero
  * (orientation is not integrated).  lbm_load_part attaches the spheres (as
  * lbm_particles_set with pp, whose npart must equal the file's nps) from

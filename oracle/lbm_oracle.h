@@ -85,7 +85,7 @@ typedef struct orc_particles {
     double stf0, stf1, stf0_w, stf1_w, zeta;
     double *pos, *vel, *omg;          /* 3*npart each, reference axes        */
     double *force, *torque;           /* hydrodynamic, last step (3*npart)   */
-    double *force_prev, *torque_prev; /* total of the previous step (AB2)    */
+    double *force_prev, *torque_prev; /* total of the previous step         */
     int have_prev;
 } orc_particles;
 

@@ -189,7 +189,7 @@ def test_driver_sphere_run_equals_binding(pkg, driver, tmp_path):
 
 def test_driver_restart_continues_sphere_run(driver, tmp_path):
     """Stop at odd step 51 and continue to 130: the restart keeps the absolute
-    step (mean density removed at step 100) and the Adams-Bashforth history."""
+    step (mean density removed at step 100) and the force history."""
     full, first, second = tmp_path / "full", tmp_path / "a", tmp_path / "b"
     run_driver(driver, full, steps=130, ndiag=1000, nstat=1000, save=1, **COMMON)
     run_driver(driver, first, steps=51, ndiag=1000, nstat=1000, save=1, **COMMON)

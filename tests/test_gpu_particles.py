@@ -254,3 +254,31 @@ def test_step_launch_count(pkg, orc):
         lat.step(110)
         per = (lat.step_launches() - n1 - 2 * sum(1 for k in range(s1 + 1, s1 + 111) if k % 100 == 0)) / 110
         assert per in (9.0, 10.0)                      # 1 fluid + 8 or 9 sphere kernels
+
+
+def test_config1_fp64_matches_oracle(pkg, orc):
+    """The particle-laden channel at full size (256 x 128 x 128, 256 spheres of
+    radius 4, density ratio 2, seeded placement and initial state), FP64:
+    populations and sphere state within 1e-10 of the oracle after 10 steps,
+    link and refill counts equal."""
+    cfg = pkg.CHANNEL_CONFIGS["spheres-256x128x128"]
+    run = cfg.params("fp64")
+    pos = pkg.place_spheres(cfg.wall, cfg.stream, cfg.span, cfg.spheres, cfg.radius, gap=2.0, wall_gap=1.0,
+                            seed=cfg.seed)
+    u = orc.channel_velocity(run.nx, run.ny, run.nz, cfg.uc, cfg.amp, cfg.seed)
+    f0 = orc.initpop(*u)
+    sp = orc.Spheres(pos, radius=cfg.radius, rho_ratio=2.0)
+    fo, owner, links, refills = orc.particle_run(orc.params_from(run), sp, f0, 10)
+    with pkg.Lattice(run) as lat:
+        lat.init_channel(cfg.uc, cfg.amp, cfg.seed)
+        assert np.array_equal(lat.download_f(), f0)
+        lat.set_particles(pos, cfg.radius, 2.0)
+        lat.step(10)
+        g = lat.download_f()
+        st = lat.particles()
+        nsolid, nlinks, nref = lat.particle_counts()
+    assert nlinks == links[-1] and nref == refills[-1]
+    assert nsolid == int((owner >= 0).sum())
+    assert rel(g, fo) < 1e-10
+    for k in ("pos", "vel", "omg", "force", "torque"):
+        assert rel(st[k], getattr(sp, k)) < 1e-10, k
