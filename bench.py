@@ -19,11 +19,14 @@ Printed JSON line (rank 0):
              arrays -- all inside the timed region
   roofline   38 populations x 2 B per node per step over the measured HBM copy
              bandwidth; traffic from the committed ncu capture
-  cpu_baseline  the FP64 oracle (C, OpenMP on all host cores) on a slab sample
-             of the same channel
+  cpu_baseline  the FP64 oracle (C, OpenMP on all host cores) on a bounded
+             sample of the same channel (with spheres: a 64^3 box at the
+             channel's sphere volume fraction)
+  gpu_launches  kernels the library launched in the timed steps, counted by
+             the library itself (lbm_step_launches)
   accuracy   FP16-store / FP32 run against FP64 over a 100-step window from
              the same initial state: mean streamwise profile, Reynolds shear
-             stress and mass drift
+             stress, mass drift and the spheres' forces and velocities
 --impl reference  times the CPU implementation (the oracle port; the Fortran
              reference cannot be built on these machines) on the same workload.
 """
