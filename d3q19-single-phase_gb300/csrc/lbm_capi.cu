@@ -37,6 +37,7 @@ struct lbm_ctx {
     DeviceParticles P{};       // spheres (npart == 0: none)
     lbm_particle_params pp{};
     int have_prev = 0;         // previous-step force and torque available
+    int order_age = 0;         // steps since the spheres' spatial order was sorted
     unsigned long long* d_count = nullptr;
     // per-step timing (lbm_timing_enable): 3 events per recorded step
     std::vector<cudaEvent_t> tev;
@@ -393,6 +394,7 @@ int lbm_destroy(lbm_ctx* c) {
     cudaFree(c->P.counters);
     cudaFree(c->P.cell_count);
     cudaFree(c->P.geom);
+    cudaFree(c->P.order);
     cudaFree(c->d_les);
     cudaFree(c->d_s9);
     cudaFree(c->d_mass);
@@ -490,6 +492,11 @@ int lbm_step_async(lbm_ctx* c, int32_t nsteps) {
         c->parity ^= 1;
         ++c->nsteps;
         if (c->P.npart > 0) {
+            if (++c->order_age >= kReorderEvery) {       // keep the spatial order current
+                CK(particles_reorder(c->P, c->stream));
+                c->nlaunch += kReorderKernels;
+                c->order_age = 0;
+            }
             CK(particles_after_step(c->s, c->P, c->parity, c->have_prev, c->stream));
             c->nlaunch += particles_kernels_per_step(c->P);
             c->have_prev = 1;
@@ -969,6 +976,7 @@ int lbm_particles_set(lbm_ctx* c, const lbm_particle_params* pp, const double* p
     DeviceParticles& P = c->P;
     if (P.pos) { cudaFree(P.pos); P.pos = nullptr; }
     if (P.geom) { cudaFree(P.geom); P.geom = nullptr; }
+    if (P.order) { cudaFree(P.order); P.order = nullptr; }
     if (!P.owner) CK(cudaMalloc(&P.owner, c->s.N * sizeof(int)));
     if (!P.counters) CK(cudaMalloc(&P.counters, 4 * sizeof(unsigned)));
     if (!c->d_count) CK(cudaMalloc(&c->d_count, sizeof(unsigned long long)));
@@ -1022,7 +1030,27 @@ int lbm_particles_set(lbm_ctx* c, const lbm_particle_params* pp, const double* p
     P.stf0 = pp->stf0; P.stf1 = pp->stf1; P.stf0_w = pp->stf0_w; P.stf1_w = pp->stf1_w; P.zeta = pp->zeta;
     c->pp = *pp;
     c->have_prev = 0;
+    if (n > 0) {
+        // the bounce-back kernel's spatial order: Morton cells 2R wide, at
+        // most 2^7 per axis (coarser cells on larger domains)
+        double cs = 2.0 * pp->radius;
+        int bits = 0;
+        for (;;) {
+            const int mx = (int)std::ceil(std::max({(double)c->p.nx, (double)c->p.ny, (double)c->p.nz}) / cs);
+            bits = 0;
+            while ((1 << bits) < mx) ++bits;
+            if (bits <= 7) break;
+            cs *= 2.0;
+        }
+        P.order_cs = cs;
+        P.order_nbins = 1 << (3 * bits);
+        CK(cudaMalloc(&P.order, (2 * (size_t)n + (size_t)P.order_nbins) * sizeof(int)));
+        P.order_key = P.order + n;
+        P.order_hist = P.order_key + n;
+    }
     CK(particles_claim(c->s, P, c->stream));
+    CK(particles_reorder(P, c->stream));
+    c->order_age = 0;
     c->s.owner = P.owner;
     c->s.ppos = P.pos; c->s.pvel = P.vel; c->s.pomg = P.omg;
     c->s.prho = pp->rho_ratio;

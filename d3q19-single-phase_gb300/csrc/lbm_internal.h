@@ -66,6 +66,15 @@ struct DeviceParticles {
     int ncell, cell_nx, cell_ny, cell_nz;   // cells along reference x, y, z
     int* cell_count;                        // [ncell]
     int* cell_list;                         // [ncell][kCellCap] sphere ids
+    // order in which the bounce-back kernel's CTAs take the spheres (sorted by
+    // the Morton code of cells order_cs wide, so that neighbouring spheres,
+    // which share cache lines of the population rows, run at the same time);
+    // nullptr: index order.  order_key [npart], order_hist [order_nbins].
+    int* order;
+    int* order_key;
+    int* order_hist;
+    double order_cs;
+    int order_nbins;
 };
 constexpr int kCellCap = 32;              // spheres per repulsion cell
 
@@ -177,6 +186,11 @@ cudaError_t particles_after_step(const DeviceState& s, const DeviceParticles& P,
                                  cudaStream_t st);
 // kernels that one particles_after_step launches
 int particles_kernels_per_step(const DeviceParticles& P);
+// re-sort the spheres into the bounce-back kernel's spatial order from their
+// current positions (3 kernels); a no-op without an order buffer
+cudaError_t particles_reorder(const DeviceParticles& P, cudaStream_t st);
+constexpr int kReorderKernels = 3;
+constexpr int kReorderEvery = 100;            // steps between re-sorts
 cudaError_t particles_count_solid(const DeviceState& s, const DeviceParticles& P, unsigned long long* d_out,
                                   cudaStream_t st);
 

@@ -177,7 +177,9 @@ int lbm_timing_get(lbm_ctx* ctx, double* fluid_even_ms, double* fluid_odd_ms,
 /* Kernels launched by lbm_step / lbm_step_async on this context since it was
  * created: one step kernel per step, plus the sphere pass (8 or 9 kernels)
  * and, every 100 steps with spheres, the two kernels of the mean-density
- * removal.  No counterpart in the reference (instrumentation of the step). */
+ * removal and the three that re-sort the spheres into the bounce-back
+ * kernel's spatial order.  No counterpart in the reference (instrumentation
+ * of the step). */
 int lbm_step_launches(const lbm_ctx* ctx, int64_t* nlaunch);
 /* The context's cudaStream_t, for event timing by the caller. */
 int lbm_stream(lbm_ctx* ctx, void** stream);

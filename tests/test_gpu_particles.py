@@ -240,8 +240,9 @@ def test_mean_density_removed_at_odd_parity(pkg, orc):
 
 def test_step_launch_count(pkg, orc):
     """lbm_step_launches counts the kernels the steps launch: one per fluid
-    step, the sphere pass after each step, and the two kernels of the
-    mean-density removal at every step number that is a multiple of 100."""
+    step, the sphere pass after each step, the two kernels of the
+    mean-density removal at every step number that is a multiple of 100, and
+    the three of the spheres' spatial re-sort every 100 steps."""
     shape = (24, 32, 22)
     run, f0 = channel_with_spheres(orc, pkg, shape, POS)
     with pkg.Lattice(run) as lat:
@@ -252,7 +253,9 @@ def test_step_launch_count(pkg, orc):
         lat.set_particles(POS, radius=4.0, rho_ratio=2.0, vel=VEL)
         n1, s1 = lat.step_launches(), lat.step_count()
         lat.step(110)
-        per = (lat.step_launches() - n1 - 2 * sum(1 for k in range(s1 + 1, s1 + 111) if k % 100 == 0)) / 110
+        removals = sum(1 for k in range(s1 + 1, s1 + 111) if k % 100 == 0)
+        resorts = 110 // 100                           # the spatial order, every 100 steps after set
+        per = (lat.step_launches() - n1 - 2 * removals - 3 * resorts) / 110
         assert per in (9.0, 10.0)                      # 1 fluid + 8 or 9 sphere kernels
 
 
@@ -279,6 +282,34 @@ def test_config1_fp64_matches_oracle(pkg, orc):
         nsolid, nlinks, nref = lat.particle_counts()
     assert nlinks == links[-1] and nref == refills[-1]
     assert nsolid == int((owner >= 0).sum())
+    assert rel(g, fo) < 1e-10
+    for k in ("pos", "vel", "omg", "force", "torque"):
+        assert rel(st[k], getattr(sp, k)) < 1e-10, k
+
+
+def test_particles_fp64_match_oracle_across_resort(pkg, orc):
+    """106 steps: the bounce-back kernel's spatial order of the spheres is
+    re-sorted from their positions at step 100 (the order in which CTAs take
+    the spheres, which changes no result) and the mean fluid density is
+    removed after step 100 (applied to the oracle's state here as the
+    library applies it: w_i times the mean over fluid nodes off every
+    population).  Populations and sphere state stay within 1e-10."""
+    shape = (24, 32, 22)
+    run, f0 = channel_with_spheres(orc, pkg, shape, POS)
+    p = orc.params_from(run)
+    sp = orc.Spheres(POS, radius=4.0, rho_ratio=2.0, vel=VEL)
+    fo, owner, _, _ = orc.particle_run(p, sp, f0, 100)
+    fluid = owner < 0
+    mean = fo[:, fluid].sum() / fluid.sum()
+    fo = fo - (orc.W * mean)[:, None, None, None]
+    fo, owner, links, _ = orc.particle_run(p, sp, fo, 6, owner=owner)
+    with pkg.Lattice(run) as lat:
+        lat.upload_f(f0)
+        lat.set_particles(POS, radius=4.0, rho_ratio=2.0, vel=VEL)
+        lat.step(106)
+        g = lat.download_f()
+        st = lat.particles()
+        assert lat.particle_counts()[1] == links[-1]
     assert rel(g, fo) < 1e-10
     for k in ("pos", "vel", "omg", "force", "torque"):
         assert rel(st[k], getattr(sp, k)) < 1e-10, k
