@@ -36,6 +36,7 @@
 //   iseedp gap wgap   seeded placement: seed, surface gaps sphere-sphere and sphere-wall
 //   qfp64             1: boundary-link fractions in FP64 for FP32/FP16 storage
 //   restart_part      endrunpart2D file to continue the spheres from
+#include <cerrno>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -45,11 +46,26 @@
 #include <string>
 #include <vector>
 
+#include <sys/stat.h>
+
 #include "lbm_gb300.h"
 
 namespace {
 
 std::map<std::string, std::string> g_args;
+
+// makedir (para.f90:311-317): the output directory and its parents exist
+// before the run writes into them
+bool make_dirs(const std::string& path) {
+    std::string cur;
+    for (size_t i = 0; i <= path.size(); ++i) {
+        if ((i == path.size() || path[i] == '/') && !cur.empty() && cur != "." && cur != "/") {
+            if (mkdir(cur.c_str(), 0755) != 0 && errno != EEXIST) return false;
+        }
+        if (i < path.size()) cur += path[i];
+    }
+    return true;
+}
 
 double argd(const char* k, double d) {
     auto it = g_args.find(k);
@@ -137,6 +153,10 @@ int main(int argc, char** argv) {
     const int prec = precs == "fp16" ? LBM_PREC_FP16 : (precs == "fp32" ? LBM_PREC_FP32 : LBM_PREC_FP64);
     const long nsteps = argi("steps", 100), ndiag = argi("ndiag", 250), nstat = argi("nstat", 1000);
     const std::string out = args("out", ".");
+    if (!make_dirs(out)) {
+        std::fprintf(stderr, "cannot create the output directory %s\n", out.c_str());
+        return 1;
+    }
     const double time_bond = argd("time_limit", (720.0 - 10.0) * 60.0);
 
     lbm_params p;

@@ -6,6 +6,7 @@ from __future__ import annotations
 
 import ctypes
 import re
+import subprocess
 from pathlib import Path
 
 import numpy as np
@@ -91,3 +92,15 @@ def test_channel_configs(pkg):
     assert (p.nx, p.ny, p.nz) == (64, 128, 64)
     big = pkg.CHANNEL_CONFIGS["spheres-1024x512x512"]
     assert big.nodes == 1024 * 512 * 512 and big.precision == "fp16"
+
+
+def test_driver_creates_its_output_directory(tmp_path):
+    """channel_gb300 creates its output directory and parents first, as the
+    reference's para makes its output directories (makedir, para.f90:311-317);
+    the run itself needs a GPU, so only the directory is checked here."""
+    drv = Path(__file__).resolve().parents[1] / "d3q19-single-phase_gb300" / "channel_gb300"
+    if not drv.exists():
+        pytest.skip("driver not built")
+    out = tmp_path / "runs" / "c0"
+    subprocess.run([str(drv), f"out={out}", "nx=4", "ny=8", "nz=4", "steps=0"], capture_output=True, timeout=120)
+    assert out.is_dir()
