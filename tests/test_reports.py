@@ -45,3 +45,35 @@ def test_precision_sweep_report(grid, shape, spheres, steps, fp16_drag):
     ref = np.array(r["profiles"]["fp64"]["mean"])
     lp = np.array(r["profiles"]["fp16"]["mean"])
     assert np.isclose(np.abs(lp - ref).max() / np.abs(ref).max(), r["errors"]["fp16"]["mean_profile_rel_err"])
+
+
+def _sweep_module():
+    import importlib.util
+    path = Path(__file__).resolve().parents[1] / "d3q19-single-phase_gb300" / "precision_sweep.py"
+    spec = importlib.util.spec_from_file_location("precision_sweep", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def _fake_run(scale, steps=(500, 1000, 1500, 2000), drag=None):
+    z = np.linspace(0.0, 1.0, 16)
+    return dict(samples=[dict(step=s, mean=scale * 18 * z * (2 - z), stress=scale * np.sin(3 * z),
+                              drag=(np.full(4, 1e-3) if drag is None else drag) * scale,
+                              rho_sum=1e-3 * s, nfluid=1000) for s in steps],
+                d0_rho_sum=0.0, d0_nfluid=1000, fail=None, s_per_step=1e-3, steps_done=steps[-1])
+
+
+def test_sweep_errors_and_drift():
+    """precision_sweep.py: errors are taken on the averages over the samples
+    after the window start, relative to the FP64 maximum, and the drifts
+    from the initial fluid mass."""
+    ps = _sweep_module()
+    ref, lp = _fake_run(1.0), _fake_run(1.02)
+    e = ps.compare(lp, ref, 1000)
+    assert e["window_samples"] == 2 and e["last_sample_step"] == 2000
+    for k in ("mean_profile_rel_err", "reynolds_stress_rel_err", "drag_mean_rel_err", "last_mean_profile_rel_err"):
+        assert e[k] == pytest.approx(0.02, rel=1e-9)
+    d = ps.drift(ref)
+    assert d["mass_drift"] == pytest.approx(2.0) and d["mean_density_drift"] == pytest.approx(2e-3)
+    assert ps.window(ref, 5000) == {}                     # no sample after the window start
