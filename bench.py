@@ -12,13 +12,17 @@ nu = 0.0024, u* = 0.0034, h = 256, seeded Poiseuille + 5 % noise initial
 state.  --no-particles leaves the spheres out.
 
 Printed JSON line (rank 0):
-  value      GLUPS over all ranks, device-resident state, CUDA-event timed
+  value      GLUPS over all ranks: fluid-node updates per second / 1e9 (the
+             nodes inside spheres are not counted, as the reference skips
+             them in its collision, collision.f90:54), device-resident state,
+             CUDA-event timed; `all_nodes_glups` counts every lattice node
   e2e        GLUPS through the C ABI with host buffers: initpop from pinned
              host velocity arrays, the steps (one synchronous lbm_step call
              each, lbm_diag every 250 steps), macrovar back to pinned host
              arrays -- all inside the timed region
-  roofline   38 populations x 2 B per node per step over the measured HBM copy
-             bandwidth; traffic from the committed ncu capture
+  roofline   38 populations x 2 B per fluid node per step over the measured
+             HBM copy bandwidth, for the step kernel and for the whole step;
+             traffic from the committed ncu capture
   cpu_baseline  the FP64 oracle (C, OpenMP on all host cores) on a bounded
              sample of the same channel (with spheres: a 64^3 box at the
              channel's sphere volume fraction)
@@ -28,7 +32,8 @@ Printed JSON line (rank 0):
              the same initial state: mean streamwise profile, Reynolds shear
              stress, mass drift and the spheres' forces and velocities
 --impl reference  times the CPU implementation (the oracle port; the Fortran
-             reference cannot be built on these machines) on the same workload.
+             reference cannot be built on these machines) on the same workload,
+             with the same metric; that arm loads only the oracle library.
 """
 from __future__ import annotations
 
@@ -48,8 +53,13 @@ import numpy as np
 REPO = Path(__file__).resolve().parent
 sys.path.insert(0, str(REPO))
 PKG = "d3q19-single-phase_gb300"
+METRIC = "GLUPS (fluid-node lattice updates per second / 1e9)"
 BYTES = {"fp64": 8, "fp32": 4, "fp16": 2}
 L2_BYTES = 129 * 2**20
+# FP64 instructions per node of the FP64 step kernels (DADD + DFMA + DMUL),
+# counted by ncu on one odd-step launch
+FP64_INST_PER_NODE = 215
+FP64_PROFILE = "profiles/step_fp64_k_step_odd_256x128x128.md"
 
 
 def log(*a):
@@ -62,6 +72,10 @@ def measured_peaks() -> dict:
         d = json.loads(p.read_text())
         return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
     return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def peak_gbs_glups(hbm_gbs: float, bytes_per_node: int) -> float:
+    return hbm_gbs * 1e9 / bytes_per_node / 1e9
 
 
 def committed_traffic(workload: str) -> dict | None:
@@ -189,19 +203,20 @@ def sphere_positions(pkg, cfg):
 
 
 # --------------------------------------------------------------------------
-def cpu_sample(orc, pkg, cfg, budget_s: float, threads: int, spheres: bool):
+def cpu_sample(orc, cfg, budget_s: float, threads: int, spheres: bool):
     """Time the oracle on a bounded sample of the workload.
 
     Particle-free: a 2-plane spanwise slab of the channel, OpenMP push.
-    With spheres: a 64^3 box at the channel's sphere volume fraction (fluid
-    push on OpenMP threads, sphere steps serial).  Returns (glups, nodes,
-    steps, seconds, description)."""
+    With spheres: a 64^3 box at the channel's sphere volume fraction, placed
+    by the oracle's own seeded placement (fluid push on OpenMP threads,
+    sphere steps serial).  Only fluid nodes count as updates.  Returns
+    (glups, fluid nodes, steps, seconds, description)."""
     run = cfg.params("fp64")
     p = orc.params_from(run)
     if spheres and cfg.spheres:
         shape = (64, 64, 64)
         n = max(1, round(cfg.spheres * 64**3 / cfg.nodes))
-        pos = pkg.place_spheres(*shape, n, cfg.radius, gap=2.0, wall_gap=1.0, seed=cfg.seed)
+        pos = orc.place_spheres(*shape, n, cfg.radius, gap=2.0, wall_gap=1.0, seed=cfg.seed)
         u = orc.channel_velocity(*shape, cfg.uc, cfg.amp, cfg.seed)
         f = orc.initpop(*u)
         sp = orc.Spheres(pos, radius=cfg.radius, rho_ratio=2.0)
@@ -210,12 +225,13 @@ def cpu_sample(orc, pkg, cfg, budget_s: float, threads: int, spheres: bool):
         f, owner, _, _ = orc.particle_run(p, sp, f, 1, owner=owner)
         t1 = time.perf_counter() - t0
         steps = max(1, int(budget_s / max(t1, 1e-6)))
+        fluid0 = int((owner == -1).sum())
         t0 = time.perf_counter()
-        orc.particle_run(p, sp, f, steps, owner=owner)
+        _, owner, _, _ = orc.particle_run(p, sp, f, steps, owner=owner)
         dt = time.perf_counter() - t0
-        nodes = 64**3
-        desc = (f"FP64 oracle port, 64x64x64 box with {n} spheres r={cfg.radius:g} (the channel's volume fraction), "
-                f"{steps} steps in {dt:.1f} s")
+        nodes = 0.5 * (fluid0 + int((owner == -1).sum()))
+        desc = (f"FP64 oracle port, 64x64x64 box with {n} spheres r={cfg.radius:g} (the channel's volume fraction; "
+                f"{nodes:.0f} fluid nodes), {steps} steps in {dt:.1f} s")
         return nodes * steps / dt / 1e9, nodes, steps, dt, desc
     shape = (cfg.wall, cfg.stream, 2)
     u = orc.channel_velocity(*shape, cfg.uc, cfg.amp, cfg.seed)
@@ -245,20 +261,20 @@ def run_reference(args, world, rank):
         return
     sys.path.insert(0, str(REPO / "oracle"))
     import oracle as orc
-    pkg = importlib.import_module(PKG)
+    pkg = importlib.import_module(PKG)      # configuration table only; the library is not loaded
     cfg = pkg.CHANNEL_CONFIGS[args.config]
     prec = args.precision or cfg.precision
     threads = os.cpu_count() or 1
     spheres = bool(cfg.spheres) and not args.no_particles
     per_step = args.cpu_budget / max(1, args.steps + args.warmup)
-    g, nodes, steps, dt, desc = cpu_sample(orc, pkg, cfg, per_step * (args.steps + args.warmup), threads, spheres)
+    g, nodes, steps, dt, desc = cpu_sample(orc, cfg, per_step * (args.steps + args.warmup), threads, spheres)
     sample = f"each step = one time step of: {desc}; {threads} host threads"
     line = {
-        "impl": "reference", "metric": "GLUPS (lattice updates per second / 1e9)", "value": round(g, 6),
+        "impl": "reference", "metric": METRIC, "value": round(g, 6),
         "unit": "GLUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(dt / max(steps, 1) * 1e3, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload_name(cfg, prec, spheres), "sample_nodes": nodes, "sample_steps": steps},
+        "config": {"workload": workload_name(cfg, prec, spheres), "sample_fluid_nodes": nodes, "sample_steps": steps},
         "cpu_baseline": {"value": round(g, 6), "unit": "GLUPS", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": round(g, 6), "unit": "GLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -281,11 +297,13 @@ def run_gpu(args, world, rank, local):
     lat = pkg.Lattice(run)
     lat.init_channel(cfg.uc, cfg.amp, cfg.seed)
     pos = None
+    pflags = pkg.PFLAG_Q_FP64 if args.qfp64 else 0
     if spheres:
         pos = sphere_positions(pkg, cfg)
-        lat.set_particles(pos, cfg.radius, 2.0)
+        lat.set_particles(pos, cfg.radius, 2.0, flags=pflags)
     log(f"[bench] rank {rank}: {wname}, {N} nodes, {lat.device_bytes() / 1e9:.2f} GB on device")
     lat.step(args.warmup)
+    fluid0 = lat.diag().nfluid
     stream = torch.cuda.ExternalStream(lat.stream())
     evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     sampler = ClockSampler(local)
@@ -293,7 +311,6 @@ def run_gpu(args, world, rank, local):
     torch.cuda.synchronize()
     sampler.start()
     time.sleep(0.3)
-    parity0 = lat.step_count() % 2
     launches0 = lat.step_launches()
     lat.timing_enable(args.steps)
     for k in range(args.steps):
@@ -305,63 +322,90 @@ def run_gpu(args, world, rank, local):
     torch.cuda.synchronize()
     barrier(world)
     clocks = sampler.stop()
-    per = np.array([evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)])   # ms
     total_ms = float(evs[0].elapsed_time(evs[-1]))
     total_ms = allmax(world, total_ms)
-    value = world * N * args.steps / (total_ms / 1e3) / 1e9
     st = lat.diag()
     if st.nonfinite:
         raise RuntimeError("non-finite populations after the timed steps")
+    # fluid nodes: the mean of the counts before and after the timed steps
+    # (sphere surfaces cover and uncover a few nodes per step)
+    NF = 0.5 * (fluid0 + st.nfluid)
+    value = world * NF * args.steps / (total_ms / 1e3) / 1e9
+    value_all = world * N * args.steps / (total_ms / 1e3) / 1e9
 
     # roofline of the fluid step kernel (even/odd AA launches alternate), timed
-    # by events the library records around each launch inside the timed loop
+    # by events the library records around each launch inside the timed loop;
+    # algorithmic bytes = 38 populations per fluid node
     tm = lat.timing()
     peaks = measured_peaks()
     ev_ms = tm["even_ms"] / max(tm["even"], 1)
     od_ms = tm["odd_ms"] / max(tm["odd"], 1)
     fluid_ms = (tm["even_ms"] + tm["odd_ms"]) / max(tm["even"] + tm["odd"], 1)
-    alg = bpn * N
+    alg = bpn * NF
     achieved = alg / (fluid_ms / 1e3) / 1e9
+    step_ach = alg / (total_ms / args.steps / 1e3) / 1e9
     traffic = committed_traffic(wname)
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "frac": round(achieved / peaks["hbm_gbs"], 4),
             "traffic": (round((traffic["even_bytes"] + traffic["odd_bytes"]) / 2) if traffic else None),
             "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json hbm_gbs)",
-            "algorithmic_bytes_per_launch": alg,
+            "kernel": ("k_step_rows" if prec != "fp64" and not args.simple else "k_step_even/odd")
+                      + " (even/odd AA launches alternate)",
+            "algorithmic_bytes_per_launch": round(alg),
+            "algorithmic_basis": f"38 populations x {BYTES[prec]} B per fluid node ({NF:.0f} fluid nodes)",
+            "whole_step": {"achieved": round(step_ach, 1), "frac": round(step_ach / peaks["hbm_gbs"], 4),
+                           "ms": round(total_ms / args.steps, 4)},
+            "all_nodes": {"nodes": N, "algorithmic_bytes_per_launch": bpn * N,
+                          "achieved": round(bpn * N / (fluid_ms / 1e3) / 1e9, 1),
+                          "frac": round(bpn * N / (fluid_ms / 1e3) / 1e9 / peaks["hbm_gbs"], 4)},
             "kernels": {"even_local": {"ms": round(ev_ms, 4), "achieved": round(alg / (ev_ms / 1e3) / 1e9, 1)},
                         "odd_neighbour": {"ms": round(od_ms, 4), "achieved": round(alg / (od_ms / 1e3) / 1e9, 1)},
                         "spheres_per_step_ms": round(tm["particle_ms"] / max(tm["even"] + tm["odd"], 1), 4)}}
     if spheres:
         ns, nl, nr = lat.particle_counts()
         roof["spheres"] = {"solid_nodes": ns, "links_last_step": nl, "refills_last_step": nr}
+    if prec == "fp64":
+        # the FP64 step is bound by the FP64 pipe (2 instructions per SM per
+        # cycle on GB300), not by bytes: the min(byte, FP64) roofline
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        mhz = clocks.get("sm_mhz") or 2070.0
+        peak_inst = 2.0 * sms * mhz * 1e6
+        per_node = FP64_INST_PER_NODE
+        ach_inst = per_node * N / (fluid_ms / 1e3)
+        roof["fp64_pipe"] = {"instructions_per_node": per_node, "source": FP64_PROFILE,
+                             "peak_ginst_s": round(peak_inst / 1e9, 1), "achieved_ginst_s": round(ach_inst / 1e9, 1),
+                             "frac": round(ach_inst / peak_inst, 4),
+                             "glups_roof_fp64": round(peak_inst / per_node / 1e9, 3),
+                             "glups_roof_bytes": round(peak_gbs_glups(peaks["hbm_gbs"], bpn), 3),
+                             "binding": "fp64 pipe"}
 
     lat.close()
     accuracy = None
     if rank == 0 and args.accuracy_steps > 0 and prec != "fp64":
-        accuracy = accuracy_window(pkg, cfg, prec, args.accuracy_steps, local, pos)
+        accuracy = accuracy_window(pkg, cfg, prec, args.accuracy_steps, local, pos, pflags)
 
     e2e = None
     if not args.no_e2e:
-        e2e = e2e_run(pkg, torch, cfg, prec, args.steps, local, world, pos)
+        e2e = e2e_run(pkg, torch, cfg, prec, args.steps, local, world, pos, pflags)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
         sys.path.insert(0, str(REPO / "oracle"))
         import oracle as orc
         threads = os.cpu_count() or 1
-        g, nodes, steps, dt, desc = cpu_sample(orc, pkg, cfg, args.cpu_budget, threads, spheres)
+        g, nodes, steps, dt, desc = cpu_sample(orc, cfg, args.cpu_budget, threads, spheres)
         cpu = {"value": round(g, 6), "unit": "GLUPS", "cores": threads, "kind": "port", "sample": desc}
 
     if rank == 0:
         line = {
-            "metric": "GLUPS (lattice updates per second / 1e9); FP16-store/FP32 vs FP64 error in `accuracy`",
-            "value": round(value, 4), "unit": "GLUPS", "n_gpus": world, "steps": args.steps,
+            "metric": METRIC, "value": round(value, 4), "unit": "GLUPS", "all_nodes_glups": round(value_all, 4), "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32" if prec != "fp64" else "f64",
             "data": "synthetic (seeded Poiseuille + uniform noise initial state)",
-            "config": {"workload": wname, "storage": prec, "nodes": N,
+            "config": {"workload": wname, "storage": prec, "nodes": N, "fluid_nodes": round(NF),
                        "grid_stream_span_wall": [cfg.stream, cfg.span, cfg.wall], "visc": cfg.visc,
                        "ustar": cfg.ustar, "h": cfg.h, "mrt": "MRTtype 1 (para.f90)" + (f", s16={cfg.s16} (sphere-laden)" if cfg.s16 else ""),
+                       "link_fractions": "fp64" if (args.qfp64 or prec == "fp64") else "fp32",
                        "l2": f"populations {N * 19 * BYTES[prec] / 1e9:.1f} GB >> 129 MB L2, no flush needed",
                        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
             "roofline": roof, "clocks": clocks, "gpu_launches": launches,
@@ -370,7 +414,7 @@ def run_gpu(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
-def accuracy_window(pkg, cfg, prec, steps, device, pos):
+def accuracy_window(pkg, cfg, prec, steps, device, pos, pflags=0):
     """FP64 vs the low-precision run over `steps` steps from the same initial
     state (the FP64 spot check of the large configuration)."""
     out = {}
@@ -379,7 +423,7 @@ def accuracy_window(pkg, cfg, prec, steps, device, pos):
         with pkg.Lattice(cfg.params(p, device=device)) as lat:
             lat.init_channel(cfg.uc, cfg.amp, cfg.seed)
             if pos is not None:
-                lat.set_particles(pos, cfg.radius, 2.0)
+                lat.set_particles(pos, cfg.radius, 2.0, flags=pflags)
             d0 = lat.diag()
             lat.step(steps)
             d1 = lat.diag()
@@ -409,7 +453,7 @@ def accuracy_window(pkg, cfg, prec, steps, device, pos):
     return out
 
 
-def e2e_run(pkg, torch, cfg, prec, steps, device, world, pos=None):
+def e2e_run(pkg, torch, cfg, prec, steps, device, world, pos=None, pflags=0):
     """GLUPS through the public C ABI with pinned host buffers in and out."""
     N = cfg.nodes
     shape = (cfg.wall, cfg.stream, cfg.span)
@@ -428,7 +472,7 @@ def e2e_run(pkg, torch, cfg, prec, steps, device, world, pos=None):
     t0 = time.perf_counter()
     lat.initpop(arrs[0], arrs[1], arrs[2])
     if pos is not None:
-        lat.set_particles(pos, cfg.radius, 2.0)
+        lat.set_particles(pos, cfg.radius, 2.0, flags=pflags)
     ndiags = 0
     for k in range(1, steps + 1):
         lat.step(1)
@@ -466,6 +510,8 @@ def main():
                     help="override the lattice (streamwise spanwise wall-normal), e.g. for a small ncu capture")
     ap.add_argument("--simple", action="store_true", help="one-node-per-thread step kernels (A/B reference)")
     ap.add_argument("--no-particles", action="store_true", help="leave the configuration's spheres out")
+    ap.add_argument("--qfp64", action="store_true",
+                    help="boundary-link fractions q in FP64 for FP32/FP16 storage (default FP32)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

@@ -56,7 +56,7 @@ PROFILE_NAMES = ("ux", "uy", "uz", "uxuz", "uxuy", "uyuz", "uxux", "uyuy", "uzuz
 EXPORTS = (
     "lbm_strerror", "lbm_last_error", "lbm_version", "lbm_params_init", "lbm_create", "lbm_destroy",
     "lbm_device_bytes", "lbm_upload_f", "lbm_download_f", "lbm_initpop", "lbm_init_channel",
-    "lbm_channel_velocity", "lbm_step", "lbm_step_async", "lbm_synchronize", "lbm_stream",
+    "lbm_channel_velocity", "lbm_init_loglaw", "lbm_loglaw_velocity", "lbm_step", "lbm_step_async", "lbm_synchronize", "lbm_stream",
     "lbm_step_count", "lbm_set_step_count", "lbm_prerelax", "lbm_macrovar", "lbm_diag", "lbm_profiles", "lbm_avedensity",
     "lbm_save_flow", "lbm_load_flow", "lbm_profiles_noalloc", "lbm_particle_params_init",
     "lbm_particles_place", "lbm_particles_set", "lbm_particles_get", "lbm_particles_get_history",
@@ -139,6 +139,9 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
         "lbm_download_f": (ctypes.c_int, [ctx, dp]),
         "lbm_initpop": (ctypes.c_int, [ctx, dp, dp, dp]),
         "lbm_init_channel": (ctypes.c_int, [ctx, ctypes.c_double, ctypes.c_double, ctypes.c_uint64]),
+        "lbm_init_loglaw": (ctypes.c_int, [ctx, ctypes.c_double, ctypes.c_double, ctypes.c_double]),
+        "lbm_loglaw_velocity": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                               ctypes.c_double, ctypes.c_double, dp, dp, dp]),
         "lbm_channel_velocity": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
                                                 ctypes.c_double, ctypes.c_uint64, dp, dp, dp]),
         "lbm_step": (ctypes.c_int, [ctx, ctypes.c_int32]),
@@ -421,8 +424,8 @@ CHANNEL_CONFIGS = {
 class Lattice:
     """Device-resident D3Q19 channel state (one GPU, one stream)."""
 
-    def __init__(self, params: RunParams | LBMParams):
-        self.lib = load_library()
+    def __init__(self, params: RunParams | LBMParams, lib: ctypes.CDLL | None = None):
+        self.lib = lib if lib is not None else load_library()
         self.cparams = params.to_c() if isinstance(params, RunParams) else params
         self.nx, self.ny, self.nz = self.cparams.nx, self.cparams.ny, self.cparams.nz
         self._ctx = ctypes.c_void_p()
@@ -484,6 +487,12 @@ class Lattice:
 
     def init_channel(self, uc: float, amp: float, seed: int) -> None:
         self._call("lbm_init_channel", ctypes.c_double(uc), ctypes.c_double(amp), ctypes.c_uint64(seed))
+
+    def init_loglaw(self, ustar: float, ystar: float, a9: float = 0.0) -> None:
+        """initvel's turbulent start (law-of-the-wall profile, initial.f90:101-147)
+        + initpop on the device; ystar = visc/ustar, a9 the perturbation
+        amplitude A9 (0 as the reference ships it)."""
+        self._call("lbm_init_loglaw", ctypes.c_double(ustar), ctypes.c_double(ystar), ctypes.c_double(a9))
 
     def step(self, n: int = 1) -> None:
         self._call("lbm_step", n)
@@ -677,6 +686,14 @@ def channel_velocity(nx: int, ny: int, nz: int, uc: float, amp: float, seed: int
     out = [np.empty((nx, ny, nz), dtype=np.float64, order="F") for _ in range(3)]
     _check(lib, lib.lbm_channel_velocity(nx, ny, nz, uc, amp, ctypes.c_uint64(seed), *map(_dptr, out)),
            "lbm_channel_velocity")
+    return tuple(out)
+
+
+def loglaw_velocity(nx: int, ny: int, nz: int, ustar: float, ystar: float, a9: float = 0.0):
+    """Host copy of the log-law initial velocity (ux, uy, uz), reference layout."""
+    lib = load_library()
+    out = [np.empty((nx, ny, nz), dtype=np.float64, order="F") for _ in range(3)]
+    _check(lib, lib.lbm_loglaw_velocity(nx, ny, nz, ustar, ystar, a9, *map(_dptr, out)), "lbm_loglaw_velocity")
     return tuple(out)
 
 

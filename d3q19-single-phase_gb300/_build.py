@@ -18,6 +18,11 @@ REPO = PKG_DIR.parent
 CSRC = PKG_DIR / "csrc"
 OBJ_DIR = PKG_DIR / "_build"
 LIB_PATH = PKG_DIR / "liblbm_gb300.so"
+# bounds-checked variant (-DLBM_BOUNDS_CHECK): every checked index that falls
+# outside its array is reported by the call that ran the kernel; for tests on
+# small lattices, not for timing
+DEBUG_OBJ_DIR = PKG_DIR / "_build_debug"
+DEBUG_LIB_PATH = PKG_DIR / "liblbm_gb300_debug.so"
 HOST_DIR = PKG_DIR / "host"
 DRIVER_PATH = PKG_DIR / "channel_gb300"
 
@@ -55,28 +60,33 @@ def _run(cmd: list[str]) -> None:
         raise RuntimeError(f"command failed ({proc.returncode}): {' '.join(cmd)}\n{proc.stdout}\n{proc.stderr}")
 
 
-def build_library(force: bool = False, verbose: bool = False) -> Path:
-    """Compile and link liblbm_gb300.so if any source changed; return its path."""
-    OBJ_DIR.mkdir(exist_ok=True)
+def build_library(force: bool = False, verbose: bool = False, debug: bool = False) -> Path:
+    """Compile and link liblbm_gb300.so (debug: the bounds-checked
+    liblbm_gb300_debug.so) if any source changed; return its path."""
+    obj_dir = DEBUG_OBJ_DIR if debug else OBJ_DIR
+    lib_path = DEBUG_LIB_PATH if debug else LIB_PATH
+    defines = ["-DLBM_BOUNDS_CHECK"] if debug else []
+    obj_dir.mkdir(exist_ok=True)
     exe = nvcc()
     deps = _deps()
     jobs = []
     objs = []
     for src in SOURCES:
         s = CSRC / src
-        o = OBJ_DIR / (src + ".o")
+        o = obj_dir / (src + ".o")
         objs.append(o)
         if force or _stale(o, [s, *deps]):
             extra = ["-Xptxas", "-v"] if verbose and src.endswith(".cu") else []
-            jobs.append([exe, *NVCC_FLAGS, *extra, "-I", str(REPO / "include"), "-c", str(s), "-o", str(o)])
+            jobs.append([exe, *NVCC_FLAGS, *defines, *extra, "-I", str(REPO / "include"), "-c", str(s),
+                         "-o", str(o)])
     if jobs:
         with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 1)) as ex:
             list(ex.map(_run, jobs))
-    if force or jobs or _stale(LIB_PATH, objs):
-        tmp = LIB_PATH.with_suffix(".so.tmp")
+    if force or jobs or _stale(lib_path, objs):
+        tmp = lib_path.with_suffix(".so.tmp")
         _run([exe, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"])
-        os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+        os.replace(tmp, lib_path)
+    return lib_path
 
 
 def build_driver(force: bool = False) -> Path:

@@ -138,10 +138,13 @@ int ensure_red(lbm_ctx* c, size_t elems) {
 int sync(lbm_ctx* c) {
     CK(cudaStreamSynchronize(c->stream));
     if (c->d_err) {
-        int flag = 0;
-        CK(cudaMemcpy(&flag, c->d_err, sizeof(int), cudaMemcpyDeviceToHost));
-        if (flag) {
-            cudaMemset(c->d_err, 0, sizeof(int));
+        int flag[2] = {0, 0};
+        CK(cudaMemcpy(flag, c->d_err, sizeof(flag), cudaMemcpyDeviceToHost));
+        if (flag[0] || flag[1]) {
+            cudaMemset(c->d_err, 0, sizeof(flag));
+            if (flag[1])
+                return fail(LBM_ERR_STATE, "bounds check failed at site " + std::to_string(flag[1]) +
+                                               "; the access was skipped and the results are invalid");
             return fail(LBM_ERR_CUDA, "a step kernel's bulk-copy wait timed out; populations are invalid");
         }
     }
@@ -359,9 +362,12 @@ int lbm_create(const lbm_params* p, lbm_ctx** out) {
     s.use_rows = !(p->flags & LBM_FLAG_SIMPLE_STEP) && rows_supported(s);
     if (s.use_rows && prepare_step_rows() != cudaSuccess) s.use_rows = 0;
     c->use_rows_saved = s.use_rows;
-    e = cudaMalloc(&c->d_err, sizeof(int));
+    // error flags: [0] a bounded wait gave up, [1] the first failing
+    // bounds-check site (bounds-checked build only)
+    e = cudaMalloc(&c->d_err, 2 * sizeof(int));
     if (e != cudaSuccess) { lbm_destroy(c); return cuda_fail(e, "cudaMalloc(error flag)"); }
-    cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
+    cudaMemsetAsync(c->d_err, 0, 2 * sizeof(int), c->stream);
+    c->s.bounds = reinterpret_cast<unsigned*>(c->d_err + 1);
     // staging: up to 256 MB, at least one reference z plane of AoS populations
     const size_t want = std::max<size_t>(plane_nodes(*p) * Q, (size_t)32 << 20);
     const size_t stage = std::min<size_t>(want, std::max<size_t>(plane_nodes(*p) * Q, s.N * Q));
@@ -475,6 +481,34 @@ int lbm_channel_velocity(int32_t nx, int32_t ny, int32_t nz, double uc, double a
                          double* ux, double* uy, double* uz) {
     if (nx < 1 || ny < 1 || nz < 1 || !ux || !uy || !uz) return fail(LBM_ERR_INVALID_ARG, "bad argument");
     channel_velocity_host(nx, ny, nz, uc, amp, seed, ux, uy, uz);
+    return LBM_OK;
+}
+
+int lbm_init_loglaw(lbm_ctx* c, double ustar, double ystar, double a9) {
+    if (check_ctx(c)) return LBM_ERR_INVALID_ARG;
+    if (!(ustar > 0.0) || !(ystar > 0.0) || !std::isfinite(ustar) || !std::isfinite(ystar) || !std::isfinite(a9))
+        return fail(LBM_ERR_INVALID_ARG, "ustar and ystar must be positive and finite, a9 finite");
+    if (int rc = set_device(c)) return rc;
+    const int nx = c->p.nx, ny = c->p.ny, nz = c->p.nz;
+    const size_t nt = loglaw_table_doubles(nx, ny, nz);
+    std::vector<double> tab(nt);
+    loglaw_tables_host(nx, ny, nz, ustar, ystar, a9, tab.data());
+    if (int rc = ensure_stage(c, nt)) return rc;
+    CK(cudaMemcpyAsync(c->d_stage, tab.data(), nt * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CK(launch_init_loglaw(c->s, c->d_stage, nx / 2, c->stream));
+    c->parity = 0;
+    c->nsteps = 0;
+    return sync(c);
+}
+
+int lbm_loglaw_velocity(int32_t nx, int32_t ny, int32_t nz, double ustar, double ystar, double a9, double* ux,
+                        double* uy, double* uz) {
+    if (nx < 1 || ny < 1 || nz < 1 || !ux || !uy || !uz) return fail(LBM_ERR_INVALID_ARG, "bad argument");
+    if (!(ustar > 0.0) || !(ystar > 0.0) || !std::isfinite(ustar) || !std::isfinite(ystar) || !std::isfinite(a9))
+        return fail(LBM_ERR_INVALID_ARG, "ustar and ystar must be positive and finite, a9 finite");
+    std::vector<double> tab(loglaw_table_doubles(nx, ny, nz));
+    loglaw_tables_host(nx, ny, nz, ustar, ystar, a9, tab.data());
+    loglaw_velocity_host(nx, ny, nz, tab.data(), ux, uy, uz);
     return LBM_OK;
 }
 
@@ -974,6 +1008,12 @@ int lbm_particles_set(lbm_ctx* c, const lbm_particle_params* pp, const double* p
     if (int rc = set_device(c)) return rc;
     const int n = pp->npart;
     DeviceParticles& P = c->P;
+    // Detach the old spheres before their arrays are freed: a failure below
+    // then leaves a particle-free context, never one whose step or field
+    // kernels read freed or null sphere arrays.
+    P.npart = 0;
+    c->s.owner = nullptr;
+    c->s.ppos = c->s.pvel = c->s.pomg = nullptr;
     if (P.pos) { cudaFree(P.pos); P.pos = nullptr; }
     if (P.geom) { cudaFree(P.geom); P.geom = nullptr; }
     if (P.order) { cudaFree(P.order); P.order = nullptr; }

@@ -2,6 +2,7 @@
 // f(0:18,nx,ny,nz) and the device SoA storage, equilibrium initialisation,
 // macroscopic fields and FP64 reductions for the diagnostics.
 #include <algorithm>
+#include <cmath>
 
 #include "lbm_internal.h"
 #include "lbm_strain.cuh"
@@ -200,6 +201,40 @@ __global__ void k_init_channel(DeviceState s, double uc, double amp, uint64_t se
     channel_velocity_node(s.g.NZ, s.g.NX, r.ix, r.iy, r.iz, uc, amp, seed, u, v, w);
     double f[Q];
     equilibrium_rn(u, v, w, f);
+    const uint32_t n = gpu_lin(s.g, r.ix, r.iy, r.iz);
+#pragma unroll
+    for (int i = 0; i < Q; ++i) put<T>(s, i, n, f[i]);
+}
+
+// Log-law initial velocity (initvel's turbulent branch, initial.f90:101-147)
+// from tables the host computes with its libm (loglaw_tables_host): per
+// wall plane m of the lower half the mean profile P[m] and the perturbation
+// factors Ay[m], Ax[m]; per streamwise/spanwise column sin and cos of the
+// perturbation's phase.  The device only multiplies and adds them in the
+// reference's order, so it builds the same bits as the host restatement.
+// Planes i = m + 1 and nx - m (1-based) share row m; with odd nx the middle
+// plane keeps zero velocity, as initvel leaves it.
+template <typename T>
+__global__ void k_init_loglaw(DeviceState s, const double* __restrict__ tab, int nxh) {
+    const RefNode r = ref_node(s.g, 0);
+    if (!r.ok) return;
+    const int nx = s.g.NZ;
+    int m = -1;
+    if (r.ix < nxh) m = r.ix;
+    else if (nx - 1 - r.ix < nxh) m = nx - 1 - r.ix;
+    double u = 0.0, v = 0.0;
+    if (m >= 0) {
+        const double* P = tab;
+        const double* Ay = tab + nxh;
+        const double* Ax = tab + 2 * (size_t)nxh;
+        const double* Sn = tab + 3 * (size_t)nxh;
+        const double* Cs = Sn + (size_t)s.g.NX * s.g.NY;
+        const size_t col = (size_t)r.iy + (size_t)s.g.NX * r.iz;
+        v = __dadd_rn(P[m], __dmul_rn(Ay[m], Sn[col]));
+        u = __dadd_rn(0.0, __dmul_rn(Ax[m], Cs[col]));
+    }
+    double f[Q];
+    equilibrium_rn(u, v, 0.0, f);
     const uint32_t n = gpu_lin(s.g, r.ix, r.iy, r.iz);
 #pragma unroll
     for (int i = 0; i < Q; ++i) put<T>(s, i, n, f[i]);
@@ -755,6 +790,74 @@ void channel_velocity_host(int nx, int ny, int nz, double uc, double amp, uint64
             }
 }
 
+size_t loglaw_table_doubles(int nx, int ny, int nz) {
+    return 3 * (size_t)(nx / 2) + 2 * (size_t)ny * (size_t)nz;
+}
+
+// Tables of initvel's turbulent branch (initial.f90:81-147) with its
+// constants A9 (perturbation amplitude, 0 as shipped), alpha = beta9 = 1,
+// cc = 60 and pi2 = 2*(4*atan(1)) (var_inc.f90:71-72).  Layout: P, Ay, Ax
+// (nx/2 each), then sin and cos of alpha*y9 + beta9*z9 per column
+// (iy + ny*iz).  Each expression keeps the reference's evaluation order.
+void loglaw_tables_host(int nx, int ny, int nz, double ustar, double ystar, double a9, double* tab) {
+    const int nxh = nx / 2;
+    const double pi2 = 2.0 * (4.0 * std::atan(1.0));
+    const double alpha = 1.0, beta9 = 1.0, cc = 60.0;
+    const double ccc1 = -((double)ny / pi2 / alpha / ystar * a9 * ustar / cc / cc);
+    double* P = tab;
+    double* Ay = tab + nxh;
+    double* Ax = tab + 2 * (size_t)nxh;
+    double* Sn = tab + 3 * (size_t)nxh;
+    double* Cs = Sn + (size_t)ny * nz;
+    for (int m = 0; m < nxh; ++m) {
+        const double yplus = ((double)(m + 1) - 0.5) / ystar;
+        if (yplus < 10.8) {
+            P[m] = yplus * ustar;
+        } else {
+            double u9 = std::log(yplus) / 0.41 + 5.0;
+            P[m] = u9 * ustar;
+        }
+        const double ccc9 = std::exp(-yplus / cc);
+        Ay[m] = ccc1 * yplus * ccc9;
+        Ax[m] = a9 * ustar * (1.0 - ccc9 - yplus / cc * ccc9);
+    }
+    for (int k = 0; k < nz; ++k) {
+        const double z9 = pi2 * ((double)(k + 1) - 0.5) / (double)nz;
+        for (int j = 0; j < ny; ++j) {
+            const double y9 = pi2 * ((double)(j + 1) - 0.5) / (double)ny;
+            const double arg = alpha * y9 + beta9 * z9;
+            Sn[(size_t)j + (size_t)ny * k] = std::sin(arg);
+            Cs[(size_t)j + (size_t)ny * k] = std::cos(arg);
+        }
+    }
+}
+
+void loglaw_velocity_host(int nx, int ny, int nz, const double* tab, double* ux, double* uy, double* uz) {
+    const int nxh = nx / 2;
+    const double* P = tab;
+    const double* Ay = tab + nxh;
+    const double* Ax = tab + 2 * (size_t)nxh;
+    const double* Sn = tab + 3 * (size_t)nxh;
+    const double* Cs = Sn + (size_t)ny * nz;
+    for (int iz = 0; iz < nz; ++iz)
+        for (int iy = 0; iy < ny; ++iy)
+            for (int ix = 0; ix < nx; ++ix) {
+                const size_t o = (size_t)ix + (size_t)nx * ((size_t)iy + (size_t)ny * iz);
+                int m = -1;
+                if (ix < nxh) m = ix;
+                else if (nx - 1 - ix < nxh) m = nx - 1 - ix;
+                double u = 0.0, v = 0.0;
+                if (m >= 0) {
+                    const size_t col = (size_t)iy + (size_t)ny * iz;
+                    v = P[m] + Ay[m] * Sn[col];
+                    u = 0.0 + Ax[m] * Cs[col];
+                }
+                ux[o] = u;
+                uy[o] = v;
+                uz[o] = 0.0;
+            }
+}
+
 #define LBM_DISPATCH(PREC_EXPR, CALL)                                   \
     switch (PREC_EXPR) {                                                \
         case LBM_PREC_FP64: { using T = double; CALL; } break;          \
@@ -782,6 +885,10 @@ cudaError_t launch_initpop(const DeviceState& s, const double* ux, const double*
 cudaError_t launch_init_channel(const DeviceState& s, double uc, double amp, uint64_t seed,
                                 cudaStream_t st) {
     LBM_DISPATCH(s.prec, (k_init_channel<T><<<ref_grid(s.g, s.g.NY, kBx), kBx, 0, st>>>(s, uc, amp, seed)))
+}
+
+cudaError_t launch_init_loglaw(const DeviceState& s, const double* tab, int nxh, cudaStream_t st) {
+    LBM_DISPATCH(s.prec, (k_init_loglaw<T><<<ref_grid(s.g, s.g.NY, kBx), kBx, 0, st>>>(s, tab, nxh)))
 }
 
 cudaError_t launch_owner_to_ref(const DeviceState& s, const int* owner, int32_t* ib, int32_t* is, int z0, int nzc,

@@ -25,6 +25,21 @@ __device__ __forceinline__ void st_pop(double* p, double v) { *p = v; }
 __device__ __forceinline__ void st_pop(float* p, float v)   { *p = v; }
 __device__ __forceinline__ void st_pop(__half* p, float v)  { *p = __float2half_rn(v); }
 
+// Bounds-checked build (-DLBM_BOUNDS_CHECK; the debug library of the build
+// recipe): the index checks of the kernels record the site number of the
+// first failing check in a device flag and skip the access, and the host
+// reports it as an error after the call.  Nothing traps.  In the normal
+// build every check is the constant true and compiles away.
+#ifdef LBM_BOUNDS_CHECK
+__device__ __forceinline__ bool bounds_ok(unsigned* flag, bool ok, unsigned site) {
+    if (!ok && flag) atomicCAS(flag, 0u, site);
+    return ok;
+}
+#define LBM_IN_BOUNDS(FLAG, COND, SITE) ::lbm::bounds_ok((FLAG), (COND), (SITE))
+#else
+#define LBM_IN_BOUNDS(FLAG, COND, SITE) true
+#endif
+
 // One base pointer per population plane, passed by value so that every
 // address is a single IMAD.WIDE from the constant bank.
 template <typename T>
@@ -87,6 +102,7 @@ struct DeviceState {
     void* f;             // 19 * pstride elements of the storage type
     CollideConsts<double> cd;
     CollideConsts<float> cf;
+    unsigned* bounds;    // first failing bounds-check site (bounds-checked build)
     int sm_count;        // SMs of the device (persistent grids)
     int use_rows;        // 1: row-pipelined bulk-copy kernels for the step
     // spheres (owner == nullptr without spheres): fluid masks and the rigid
@@ -196,5 +212,12 @@ cudaError_t particles_count_solid(const DeviceState& s, const DeviceParticles& P
 
 void channel_velocity_host(int nx, int ny, int nz, double uc, double amp,
                            uint64_t seed, double* ux, double* uy, double* uz);
+
+// log-law initial velocity (initial.f90:101-147): host tables, the host
+// field they give, and the device initial condition built from them
+size_t loglaw_table_doubles(int nx, int ny, int nz);
+void loglaw_tables_host(int nx, int ny, int nz, double ustar, double ystar, double a9, double* tab);
+void loglaw_velocity_host(int nx, int ny, int nz, const double* tab, double* ux, double* uy, double* uz);
+cudaError_t launch_init_loglaw(const DeviceState& s, const double* tab, int nxh, cudaStream_t st);
 
 }  // namespace lbm

@@ -198,7 +198,8 @@ constexpr float kShellEps = 0.01f;
 __device__ __forceinline__ float in_band(float R2) { return 1e-5f * R2 + 1e-3f; }
 
 template <bool CLAIM>
-__global__ void __launch_bounds__(32 * kShellWarps) k_shell(DeviceParticles P, Geometry g, int* owner, int full) {
+__global__ void __launch_bounds__(32 * kShellWarps) k_shell(DeviceParticles P, Geometry g, int* owner, int full,
+                                                            unsigned* bflag) {
     const int lane = threadIdx.x & 31;
     const int p = blockIdx.x * kShellWarps + (threadIdx.x >> 5);
     if (p >= P.npart) return;                       // whole warps leave together
@@ -255,6 +256,7 @@ __global__ void __launch_bounds__(32 * kShellWarps) k_shell(DeviceParticles P, G
                         in = inside(d, P.R);
                     }
                     const uint32_t n = gnode(g, ix, iy, iz);
+                    if (!LBM_IN_BOUNDS(bflag, ix >= 0 && ix < g.NZ && n < g.NXY * (uint32_t)g.NZ, 201)) continue;
                     if (CLAIM) {
                         if (in) atomicMax(owner + n, p);        // the highest index among overlapping spheres
                     } else if (!in && owner[n] == p) {
@@ -280,7 +282,8 @@ __global__ void __launch_bounds__(32 * kShellWarps) k_shell(DeviceParticles P, G
 // that left the populations in orientation `parity`.  RT: link arithmetic and
 // q (FP64 for FP64 storage; FP32 for FP32/FP16 storage, where an FP64 q per
 // link would cost more than the fluid step at GB300's FP64 rate), node
-// offsets always from FP64 positions, sums in FP64 per node and per sphere.
+// offsets always from FP64 positions, force and torque sums of FP64 accuracy
+// per thread and FP64 per sphere.
 // qc = |d|^2 - R^2 of the node, computed once per node in FP64
 template <typename RT>
 __device__ __forceinline__ RT link_q(const double d[3], int cx, int cy, int cz, double qc) {
@@ -324,8 +327,9 @@ __device__ __forceinline__ RT link_q(const double d[3], int cx, int cy, int cz, 
 // RT: link arithmetic and q (FP64 with correctly rounded operations for FP64
 // storage, bit-consistent with the oracle; FP32 with hardware reciprocals for
 // FP32/FP16 storage, where an FP64 q per link would cost more than the fluid
-// step at GB300's FP64 rate).  Force and torque are summed in FP64 per thread
-// and per sphere.
+// step at GB300's FP64 rate).  Force and torque: per-thread sums in FP64
+// (FP64 storage) or in compensated FP32 (ForceAcc), per-sphere sums of the
+// threads' partials in FP64.
 
 // bit a of the result = bit a + cy of x
 template <typename W>
@@ -381,6 +385,16 @@ __device__ __forceinline__ IbbLink<T, RT> ibb_gather(const DeviceState& s, const
     const int ib = D.packed >> 8;
     const int dr = cz + B.S * cx;                      // row offset of c_i
     const int r0 = b + B.S * c;
+    // the staged box holds every node the link touches: rows r0 - 2dr ..
+    // r0 + dr and streamwise positions a - 2cy .. a + cy
+    if (!LBM_IN_BOUNDS(s.bounds, i >= 1 && i < Q && a >= 2 && a + 2 < B.S && b >= 2 && b + 2 < B.S && c >= 2 &&
+                                     c + 2 < B.S, 221)) {
+        L.ok1 = L.ok2 = false;
+        L.q = RT(1); L.A = L.X = L.Y = RT(0); L.mw = RT(0);
+        L.x0 = L.x1 = L.x2 = L.fcx = L.fcy = L.fcz = L.uw0 = L.uw1 = L.uw2 = RT(0);
+        L.w = nullptr;
+        return L;
+    }
     L.ok1 = (B.fluid[r0 - dr] >> (a - cy)) & 1;
     L.ok2 = L.ok1 && ((B.fluid[r0 - 2 * dr] >> (a - 2 * cy)) & 1);
     const uint32_t gx = (uint32_t)(B.wA[a] + B.rowIdx[r0]);
@@ -388,6 +402,13 @@ __device__ __forceinline__ IbbLink<T, RT> ibb_gather(const DeviceState& s, const
     uint32_t ga = 0, gb = 0;
     if (L.ok1) ga = (uint32_t)(B.wA[a - cy] + B.rowIdx[r0 - dr]);
     if (L.ok2) gb = (uint32_t)(B.wA[a - 2 * cy] + B.rowIdx[r0 - 2 * dr]);
+    if (!LBM_IN_BOUNDS(s.bounds, gx < s.N && gs < s.N && ga < s.N && gb < s.N, 222)) {
+        L.ok1 = L.ok2 = false;
+        L.q = RT(1); L.A = L.X = L.Y = RT(0); L.mw = RT(0);
+        L.x0 = L.x1 = L.x2 = L.fcx = L.fcy = L.fcz = L.uw0 = L.uw1 = L.uw2 = RT(0);
+        L.w = nullptr;
+        return L;
+    }
     const T* Pi = plane<T>(s, i);
     const T* Pib = plane<T>(s, ib);
     RT d0, d1, d2;
@@ -431,10 +452,42 @@ __device__ __forceinline__ IbbLink<T, RT> ibb_gather(const DeviceState& s, const
     return L;
 }
 
+// Per-lane sums of a sphere's force and torque.  FP64 storage sums in FP64.
+// FP32/FP16 storage computes each link's momentum in FP32 and sums it with
+// an error-free transformation (Knuth's TwoSum: s + c carries the exact sum
+// of s and x), so a lane's sum of n terms is accurate to 2u|S| + O(n^2 u^2)
+// sum|x| (u = 2^-24), i.e. to about FP64 accuracy for the ~20 links a lane
+// takes; the lanes' partial sums s + c are then reduced in FP64.
+template <typename RT>
+struct ForceAcc {
+    double s[6];
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) s[k] = 0.0;
+    }
+    __device__ __forceinline__ void add(int k, double x) { s[k] += x; }
+    __device__ __forceinline__ double total(int k) const { return s[k]; }
+};
+template <>
+struct ForceAcc<float> {
+    float s[6], c[6];
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) s[k] = c[k] = 0.f;
+    }
+    __device__ __forceinline__ void add(int k, float x) {
+        const float t = __fadd_rn(s[k], x);
+        const float z = __fsub_rn(t, s[k]);
+        c[k] = __fadd_rn(c[k], __fadd_rn(__fsub_rn(s[k], __fsub_rn(t, z)), __fsub_rn(x, z)));
+        s[k] = t;
+    }
+    __device__ __forceinline__ double total(int k) const { return (double)s[k] + (double)c[k]; }
+};
+
 // Interpolation, the returning population and the exchanged momentum and its
-// moment (added to acc[6]).
+// moment (added to acc).
 template <typename T, typename RT>
-__device__ __forceinline__ void ibb_finish(const DeviceState& s, const IbbLink<T, RT>& L, RT (&acc)[6]) {
+__device__ __forceinline__ void ibb_finish(const DeviceState& s, const IbbLink<T, RT>& L, ForceAcc<RT>& acc) {
     const RT q = L.q, A = L.A, mw = L.mw;
     RT fn;
     if (q < RT(0.5)) {
@@ -461,19 +514,22 @@ __device__ __forceinline__ void ibb_finish(const DeviceState& s, const IbbLink<T
             fn = A + mw;
         }
     }
+#ifdef LBM_BOUNDS_CHECK
+    if (L.w == nullptr) return;                        // a skipped (out-of-bounds) link
+#endif
     put_r<T, RT>(s, L.w, fn);
     // Galilean-invariant momentum exchange
     const RT sA = A + fn, dA = fn - A;
     const RT p0 = L.fcx * sA + L.uw0 * dA, p1 = L.fcy * sA + L.uw1 * dA, p2 = L.fcz * sA + L.uw2 * dA;
-    acc[0] += p0; acc[1] += p1; acc[2] += p2;
-    acc[3] += L.x1 * p2 - L.x2 * p1;
-    acc[4] += L.x2 * p0 - L.x0 * p2;
-    acc[5] += L.x0 * p1 - L.x1 * p0;
+    acc.add(0, p0); acc.add(1, p1); acc.add(2, p2);
+    acc.add(3, L.x1 * p2 - L.x2 * p1);
+    acc.add(4, L.x2 * p0 - L.x0 * p2);
+    acc.add(5, L.x0 * p1 - L.x1 * p0);
 }
 
 template <typename T, typename RT, typename W, bool Q64>
 __device__ __forceinline__ void ibb_link(const DeviceState& s, const DeviceParticles& P, int p, int parity,
-                                         const IbbBox<W>& B, uint32_t v, const RT (&UW)[6], RT (&acc)[6]) {
+                                         const IbbBox<W>& B, uint32_t v, const RT (&UW)[6], ForceAcc<RT>& acc) {
     const IbbLink<T, RT> L = ibb_gather<T, RT, W, Q64>(s, P, p, parity, B, v, UW);
     ibb_finish<T, RT>(s, L, acc);
 }
@@ -482,7 +538,7 @@ __device__ __forceinline__ void ibb_link(const DeviceState& s, const DeviceParti
 template <typename T, typename RT, typename W, bool Q64>
 __device__ __forceinline__ void ibb_link2(const DeviceState& s, const DeviceParticles& P, int p, int parity,
                                           const IbbBox<W>& B, uint32_t v1, uint32_t v2, const RT (&UW)[6],
-                                          RT (&acc)[6]) {
+                                          ForceAcc<RT>& acc) {
     const IbbLink<T, RT> L1 = ibb_gather<T, RT, W, Q64>(s, P, p, parity, B, v1, UW);
     const IbbLink<T, RT> L2 = ibb_gather<T, RT, W, Q64>(s, P, p, parity, B, v2, UW);
     ibb_finish<T, RT>(s, L1, acc);
@@ -597,7 +653,8 @@ __global__ void __launch_bounds__(kPThreads, sizeof(RT) == 8 ? 2 : 4)
                     pw |= (W)__ballot_sync(0xffffffffu, o[u][1] == p) << 32;
                     fw |= (W)__ballot_sync(0xffffffffu, o[u][1] == -1) << 32;
                 }
-                if (lane == 0 && r0 + u * nw < nrows) {
+                if (lane == 0 && r0 + u * nw < nrows &&
+                    LBM_IN_BOUNDS(s.bounds, rb[u] >= 0 && rb[u] < S && rc[u] >= 0 && rc[u] < S, 223)) {
                     own[rb[u] + S * rc[u]] = pw;
                     fluid[rb[u] + S * rc[u]] = fw;
                 }
@@ -640,7 +697,8 @@ __global__ void __launch_bounds__(kPThreads, sizeof(RT) == 8 ? 2 : 4)
             UW[3 + k] = G.W[k];
         }
     }
-    RT acc[6] = {0, 0, 0, 0, 0, 0};
+    ForceAcc<RT> acc;
+    acc.zero();
     const unsigned lt = (1u << lane) - 1u;
     uint32_t* q = queue + wid * kIbbQueue;
     int head = 0, tail = 0;
@@ -721,7 +779,7 @@ __global__ void __launch_bounds__(kPThreads, sizeof(RT) == 8 ? 2 : 4)
     __shared__ int shn[kPThreads / 32];
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
-        double v = (double)acc[k];
+        double v = acc.total(k);
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
         if (lane == 0) sh[k][wid] = v;
     }
@@ -1071,6 +1129,8 @@ __device__ __forceinline__ void refill_node(const DeviceState& s, const DevicePa
     const Geometry& g = s.g;
     const uint32_t n = P.refill_node[k];
     const int* owner = P.owner;
+    if (!LBM_IN_BOUNDS(s.bounds, n < g.NXY * (uint32_t)g.NZ && P.refill_part[k] >= 0 &&
+                                     P.refill_part[k] < P.npart, 211)) return;
     if (owner[n] != -2) return;
     const int p = P.refill_part[k];
     const int iy = (int)(n % (uint32_t)g.NX);
@@ -1217,7 +1277,7 @@ size_t particles_smem_bytes(double R) { return ibb_smem_bytes(R); }
 cudaError_t particles_claim(const DeviceState& s, const DeviceParticles& P, cudaStream_t st) {
     if (P.npart == 0) return cudaSuccess;
     k_geom<<<(P.npart + 127) / 128, 128, 0, st>>>(P);
-    k_shell<true><<<(P.npart + kShellWarps - 1) / kShellWarps, 32 * kShellWarps, 0, st>>>(P, s.g, P.owner, 1);
+    k_shell<true><<<(P.npart + kShellWarps - 1) / kShellWarps, 32 * kShellWarps, 0, st>>>(P, s.g, P.owner, 1, s.bounds);
     return cudaGetLastError();
 }
 
@@ -1254,8 +1314,8 @@ cudaError_t particles_after_step(const DeviceState& s, const DeviceParticles& P,
         k_repulsion<<<(P.npart + kRepTile - 1) / kRepTile, kRepTile, 0, st>>>(P, s.g);
     }
     k_newton<<<(P.npart + 127) / 128, 128, 0, st>>>(P, s.g, s.cd.Fx, s.cd.Fy, s.cd.Fz, have_prev);
-    k_shell<false><<<(P.npart + kShellWarps - 1) / kShellWarps, 32 * kShellWarps, 0, st>>>(P, s.g, P.owner, 0);
-    k_shell<true><<<(P.npart + kShellWarps - 1) / kShellWarps, 32 * kShellWarps, 0, st>>>(P, s.g, P.owner, 0);
+    k_shell<false><<<(P.npart + kShellWarps - 1) / kShellWarps, 32 * kShellWarps, 0, st>>>(P, s.g, P.owner, 0, s.bounds);
+    k_shell<true><<<(P.npart + kShellWarps - 1) / kShellWarps, 32 * kShellWarps, 0, st>>>(P, s.g, P.owner, 0, s.bounds);
     k_reclaim<<<std::max(1, 2 * s.sm_count), 256, 0, st>>>(P, s.g, P.owner);
     // refills: a few per sphere and step; a grid of 4 CTAs per SM strides the list
     const unsigned nb = (unsigned)std::min<long long>((P.refill_cap + 255) / 256, 4LL * std::max(s.sm_count, 1));

@@ -23,9 +23,12 @@
 // directions of HBM traffic are whole-row bulk copies, and the bytes in
 // flight are set by shared memory, not by registers.
 //
-// Every mbarrier wait is bounded; a wait that gives up sets the error flag
-// and the warp carries on with whatever the buffer holds, so the kernel always
-// terminates and the host reports the step as failed.
+// Every mbarrier wait is bounded.  A wait that gives up raises a CTA-wide
+// abort flag and the global error flag (the host then reports the step as
+// failed): from then on no warp issues another bulk load or store, every warp
+// leaves the item loop at its next item, and before the CTA exits one thread
+// waits (again bounded) for every stage's last issued load to land, so that
+// no bulk copy still targets the CTA's shared memory when it exits.
 #include <algorithm>
 
 #include "lbm_internal.h"
@@ -151,25 +154,43 @@ __device__ __forceinline__ bool push_bb(int wall, int i) {
     return (DZg(i) == 1 && (wall & 2)) || (DZg(i) == -1 && (wall & 1));
 }
 
-// Source row of population i for an item (runtime i).
+// Source row of population i for an item (runtime i).  In the
+// bounds-checked build a plane or row outside the lattice is reported at
+// `site` and replaced by row 0 of plane 0 (the results are then invalid and
+// the call fails).
 template <typename T, bool ODD>
-__device__ __forceinline__ const T* src_row(const PopPtrs<T>& P, const Geometry& g, const Item& I, int wall, int i) {
+__device__ __forceinline__ const T* src_row(const PopPtrs<T>& P, const Geometry& g, const Item& I, int wall, int i,
+                                            unsigned* bflag, unsigned site) {
     const int dz = dz_rt(i);
     const bool bb = (dz == 1 && (wall & 1)) || (dz == -1 && (wall & 2));
-    if (!ODD || bb) return P.p[i] + I.row;
-    return P.p[opp_rt(i)] + row_at(g, I.y - dy_rt(i), I.z - dz);
+    int k = i;
+    uint32_t row = I.row;
+    if (ODD && !bb) {
+        k = opp_rt(i);
+        row = row_at(g, I.y - dy_rt(i), I.z - dz);
+    }
+    if (!LBM_IN_BOUNDS(bflag, k >= 0 && k < Q && row % (uint32_t)g.NX == 0 &&
+                                  (size_t)row + g.NX <= (size_t)g.NXY * g.NZ, site))
+        return P.p[0];
+    return P.p[k] + row;
 }
 // Issued by one warp: lane i moves population i's row.  The mbarrier learns the
 // byte count from lane 0 before any copy is issued.
+// `issued` counts the loads ever issued into this stage (for the drain on
+// abort).
 template <typename T, bool ODD>
 __device__ __forceinline__ void issue_item(const PopPtrs<T>& P, const Geometry& g, uint32_t it, uint32_t stage_smem,
-                                           uint32_t bar, uint32_t row_bytes, int lane) {
-    if (lane == 0) mbar_expect_tx(bar, (uint32_t)Q * row_bytes);
+                                           uint32_t bar, uint32_t row_bytes, int lane, unsigned* issued,
+                                           unsigned* bflag) {
+    if (lane == 0) {
+        ++*issued;
+        mbar_expect_tx(bar, (uint32_t)Q * row_bytes);
+    }
     __syncwarp();
     if (lane < Q) {
         const Item I = item_of(g, it);
-        bulk_load(stage_smem + (uint32_t)lane * row_bytes, src_row<T, ODD>(P, g, I, wall_of(g, I.z), lane),
-                  row_bytes, bar);
+        bulk_load(stage_smem + (uint32_t)lane * row_bytes,
+                  src_row<T, ODD>(P, g, I, wall_of(g, I.z), lane, bflag, 301), row_bytes, bar);
     }
 }
 
@@ -221,9 +242,11 @@ __device__ __forceinline__ void pair_update(const CollideConsts<float>& C, const
 // the whole loop.
 template <typename T, bool ODD, int WALL, bool YF>
 __device__ __forceinline__ void item_pairs(const CollideConsts<float>& C, const Geometry& g, T* stage, int tid,
-                                           int nthreads) {
+                                           int nthreads, unsigned* bflag) {
     const int npairs = g.NX >> 1;
-    for (int p = tid; p < npairs; p += nthreads) pair_update<T, ODD, WALL, YF>(C, g, stage, 2 * p);
+    for (int p = tid; p < npairs; p += nthreads)
+        if (LBM_IN_BOUNDS(bflag, 2 * p + 1 < g.NX && (g.NX & 1) == 0, 303))
+            pair_update<T, ODD, WALL, YF>(C, g, stage, 2 * p);
 }
 
 // Issued by the last warp to finish an item: lane i copies result row i back
@@ -231,10 +254,10 @@ __device__ __forceinline__ void item_pairs(const CollideConsts<float>& C, const 
 // the stage (the stage is refilled next).
 template <typename T, bool ODD>
 __device__ __forceinline__ void store_item(const PopPtrs<T>& P, const Geometry& g, uint32_t it, uint32_t stage_smem,
-                                           uint32_t row_bytes, int lane) {
+                                           uint32_t row_bytes, int lane, unsigned* bflag) {
     if (lane < Q) {
         const Item I = item_of(g, it);
-        bulk_store(const_cast<T*>(src_row<T, ODD>(P, g, I, wall_of(g, I.z), lane)),
+        bulk_store(const_cast<T*>(src_row<T, ODD>(P, g, I, wall_of(g, I.z), lane, bflag, 302)),
                    stage_smem + (uint32_t)lane * row_bytes, row_bytes);
         bulk_wait_read();
     }
@@ -248,6 +271,8 @@ __global__ void __launch_bounds__(NT, 512 / NT)
 k_step_rows(PopPtrs<T> P, CollideConsts<float> C, Geometry g, int nstage, int* err) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ unsigned int done_count[kMaxStages];
+    __shared__ unsigned int issued[kMaxStages];
+    __shared__ volatile int abort_flag;
     const uint32_t row_bytes = (uint32_t)g.NX * sizeof(T);
     const uint32_t stage_bytes = (uint32_t)Q * row_bytes;
     const uint32_t bars = smem_addr(smem);                 // nstage mbarriers (8 B each)
@@ -258,34 +283,42 @@ k_step_rows(PopPtrs<T> P, CollideConsts<float> C, Geometry g, int nstage, int* e
     const int tid = threadIdx.x;
     const int lane = tid & 31;
     const unsigned nwarps = NT / 32;
+    unsigned* const bflag = reinterpret_cast<unsigned*>(err + 1);   // bounds-check site (checked build)
+    (void)bflag;
 
     if (tid == 0) {
         for (int s = 0; s < nstage; ++s) {
             mbar_init(bars + 8 * s, 1);
             done_count[s] = 0;
+            issued[s] = 0;
         }
+        abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
     if (tid < 32) {
         for (int s = 0; s < nstage; ++s) {
             const uint32_t it = blockIdx.x + (uint32_t)s * G;
-            if (it < total) issue_item<T, ODD>(P, g, it, data + s * stage_bytes, bars + 8 * s, row_bytes, lane);
+            if (it < total)
+                issue_item<T, ODD>(P, g, it, data + s * stage_bytes, bars + 8 * s, row_bytes, lane, &issued[s],
+                                   bflag);
         }
     }
-    bool failed = false;
     for (uint32_t k = 0;; ++k) {
         const uint32_t it = blockIdx.x + k * G;
-        if (it >= total) break;
+        if (it >= total || abort_flag) break;
         const int s = (int)(k % (uint32_t)nstage);
-        if (!mbar_wait(bars + 8 * s, (k / (uint32_t)nstage) & 1u)) failed = true;
+        if (!mbar_wait(bars + 8 * s, (k / (uint32_t)nstage) & 1u)) {
+            abort_flag = 1;
+            break;
+        }
         const Item I = item_of(g, it);
         const int wall = wall_of(g, I.z);
         T* stage = stage_ptr0 + (size_t)s * Q * g.NX;
-        if (wall == 0)      item_pairs<T, ODD, 0, YF>(C, g, stage, tid, NT);
-        else if (wall == 1) item_pairs<T, ODD, 1, YF>(C, g, stage, tid, NT);
-        else if (wall == 2) item_pairs<T, ODD, 2, YF>(C, g, stage, tid, NT);
-        else                item_pairs<T, ODD, 3, YF>(C, g, stage, tid, NT);
+        if (wall == 0)      item_pairs<T, ODD, 0, YF>(C, g, stage, tid, NT, bflag);
+        else if (wall == 1) item_pairs<T, ODD, 1, YF>(C, g, stage, tid, NT, bflag);
+        else if (wall == 2) item_pairs<T, ODD, 2, YF>(C, g, stage, tid, NT, bflag);
+        else                item_pairs<T, ODD, 3, YF>(C, g, stage, tid, NT, bflag);
         // this warp has finished with stage s; the last warp copies the
         // results back and refills it
         fence_proxy_async();
@@ -296,17 +329,26 @@ k_step_rows(PopPtrs<T> P, CollideConsts<float> C, Geometry g, int nstage, int* e
             last = atomicAdd(&done_count[s], 1u) == nwarps - 1;
             if (last) done_count[s] = 0;
         }
-        last = __shfl_sync(0xffffffffu, last, 0);
+        last = __shfl_sync(0xffffffffu, last, 0) && !abort_flag;
         if (last) {
             __threadfence_block();
             fence_proxy_async();
-            store_item<T, ODD>(P, g, it, data + s * stage_bytes, row_bytes, lane);
+            store_item<T, ODD>(P, g, it, data + s * stage_bytes, row_bytes, lane, bflag);
             const uint32_t nit = blockIdx.x + (k + (uint32_t)nstage) * G;
-            if (nit < total) issue_item<T, ODD>(P, g, nit, data + s * stage_bytes, bars + 8 * s, row_bytes, lane);
+            if (nit < total && !abort_flag)
+                issue_item<T, ODD>(P, g, nit, data + s * stage_bytes, bars + 8 * s, row_bytes, lane, &issued[s],
+                                   bflag);
         }
     }
     bulk_wait_all();
-    if (failed) atomicExch(err, 1);
+    __syncthreads();
+    if (abort_flag && tid == 0) {
+        // drain: the latest load into each stage completes the phase with
+        // parity (issued - 1) & 1; earlier phases have completed before it
+        for (int s = 0; s < nstage; ++s)
+            if (issued[s] > 0) (void)mbar_wait(bars + 8 * s, (issued[s] - 1u) & 1u);
+        atomicExch(err, 1);
+    }
 }
 
 template <typename T>

@@ -4,7 +4,8 @@
 //   para (para.f90)              -> parameters from key=value arguments
 //   allocarray                   -> lbm_create
 //   new run: initvel + FORCING + initpop (+ pre-relaxation) + saveinitflow
-//            (main.f90:52-107)   -> lbm_init_channel / lbm_prerelax / lbm_save_flow
+//            (main.f90:52-107)   -> lbm_init_channel or lbm_init_loglaw /
+//                                   lbm_prerelax / lbm_save_flow
 //   restart: loadcntdflow        -> lbm_load_flow (main.f90:118-121)
 //   ipart: initpartpos + beads   -> lbm_particles_place / lbm_particles_set
 //          (para.f90:339-379); the mean-density removal every 100 steps
@@ -24,7 +25,11 @@
 //   s16               rate of the third-order odd moments, overriding the set
 //   precision         fp64 | fp32 | fp16
 //   steps ndiag nstat main-loop length and output cadence
+//   ivel              initial velocity: poiseuille (the benchmark channels: laminar
+//                     profile + seeded noise), loglaw (initvel's turbulent start,
+//                     initial.f90:101-147) or rest (ivel = .false.)
 //   uc amp seed       initial Poiseuille centreline, noise amplitude, seed
+//   a9                amplitude A9 of initvel's perturbation (loglaw; 0 as shipped)
 //   prerelax          1: run the density pre-relaxation of main.f90:69-90
 //   out               output directory for diag.dat / profiles2.dat / checkpoints
 //   restart           checkpoint to continue from (endrunflow format)
@@ -175,11 +180,32 @@ int main(int argc, char** argv) {
     } else {
         const double uc = argd("uc", 0.05), amp = argd("amp", 0.05);
         const uint64_t seed = (uint64_t)argi("seed", 20240611);
-        check(lbm_init_channel(ctx, uc, amp, seed), "initvel+initpop");
+        const std::string ivel = args("ivel", "poiseuille");
+        const double a9 = argd("a9", 0.0);
+        const size_t n = (size_t)nx * ny * nz;
+        std::vector<double> u, v, w;
+        if (ivel == "loglaw") {
+            // initvel with ivel = .true. (turbulent start, initial.f90:101-147)
+            check(lbm_init_loglaw(ctx, ustar, visc / ustar, a9), "initvel+initpop");
+        } else if (ivel == "rest") {
+            // initvel with ivel = .false. (stationary start, initial.f90:97-100)
+            u.assign(n, 0.0); v.assign(n, 0.0); w.assign(n, 0.0);
+            check(lbm_initpop(ctx, u.data(), v.data(), w.data()), "initpop");
+        } else if (ivel == "poiseuille") {
+            check(lbm_init_channel(ctx, uc, amp, seed), "initvel+initpop");
+        } else {
+            std::fprintf(stderr, "ivel must be poiseuille, loglaw or rest\n");
+            return 1;
+        }
         if (argi("prerelax", 0)) {
-            const size_t n = (size_t)nx * ny * nz;
-            std::vector<double> u(n), v(n), w(n);
-            check(lbm_channel_velocity(nx, ny, nz, uc, amp, seed, u.data(), v.data(), w.data()), "initvel");
+            if (u.empty()) {
+                u.resize(n); v.resize(n); w.resize(n);
+                if (ivel == "loglaw")
+                    check(lbm_loglaw_velocity(nx, ny, nz, ustar, visc / ustar, a9, u.data(), v.data(), w.data()),
+                          "initvel");
+                else
+                    check(lbm_channel_velocity(nx, ny, nz, uc, amp, seed, u.data(), v.data(), w.data()), "initvel");
+            }
             int32_t it = 0;
             double err = 0;
             const int rc = lbm_prerelax(ctx, u.data(), v.data(), w.data(), 1e-5, 15000, &it, &err);

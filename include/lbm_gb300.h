@@ -12,6 +12,8 @@
  *   FORCING (collision.f90:515-527)              lbm_params.force[3]
  *   initpop (initial.f90:19-46)                  lbm_initpop
  *   initvel + initpop for the channel configs    lbm_init_channel (device IC)
+ *   initvel turbulent branch + initpop           lbm_init_loglaw (device IC)
+ *     (initial.f90:75-147, ivel = .true.)
  *   collision_MRT + collisionExchnge + macrovar  lbm_step
  *     (collision.f90:24-273, 281-372, 378-463;
  *      call order main.f90:157-161)
@@ -160,6 +162,28 @@ int lbm_init_channel(lbm_ctx* ctx, double uc, double amp, uint64_t seed);
 int lbm_channel_velocity(int32_t nx, int32_t ny, int32_t nz, double uc,
                          double amp, uint64_t seed, double* ux, double* uy,
                          double* uz);
+
+/* initvel's turbulent branch + initpop on the device (initial.f90:101-147,
+ * the ivel = .true. start of para.f90:59-72, and initial.f90:19-46): the
+ * law-of-the-wall streamwise profile u_y = y+ u* for y+ < 10.8, else
+ * u*(ln(y+)/0.41 + 5), y+ = (i - 1/2)/ystar for the wall-normal planes
+ * i = 1..nx/2, mirrored onto planes nx+1-i (with odd nx the middle plane
+ * stays at rest), plus initvel's perturbation with amplitude a9 (the
+ * reference's A9, 0.0 as shipped, which makes it vanish):
+ *   u_y += A9'(y+) sin(y9 + z9),  u_x += A9 u* (1 - e - y+ e/60) cos(y9 + z9),
+ *   e = exp(-y+/60), A9'(y+) = -ny/(2 pi) /ystar * A9 u* / 60^2 * y+ e,
+ *   y9 = 2 pi (j - 1/2)/ny, z9 = 2 pi (k - 1/2)/nz;
+ * then f = equilibrium at delta-rho = 0.  ystar = visc/ustar (para.f90:66).
+ * The transcendental factors are evaluated on the host (one per wall plane
+ * and per column); lbm_loglaw_velocity returns the identical field. */
+int lbm_init_loglaw(lbm_ctx* ctx, double ustar, double ystar, double a9);
+
+/* Host-side copy of the velocity field lbm_init_loglaw builds (arrays of
+ * nx*ny*nz doubles, reference layout); the velocity arrays the
+ * pre-relaxation (lbm_prerelax) needs.  Needs no context or GPU. */
+int lbm_loglaw_velocity(int32_t nx, int32_t ny, int32_t nz, double ustar,
+                        double ystar, double a9, double* ux, double* uy,
+                        double* uz);
 
 /* nsteps x (collision_MRT + periodic exchange + macrovar); synchronous. */
 int lbm_step(lbm_ctx* ctx, int32_t nsteps);

@@ -481,6 +481,53 @@ void orc_channel_velocity(int nx, int ny, int nz, double uc, double amp, uint64_
             }
 }
 
+/* initvel, turbulent branch (initial.f90:75-147, one rank: kk = k, jj = j):
+ * law-of-the-wall mean profile mirrored about the centre, then the
+ * perturbation loop with the reference's constants (A9 = a9, alpha = beta9 =
+ * 1, cc = 60).  1-based plane loops as written; each expression keeps the
+ * reference's evaluation order. */
+void orc_loglaw_velocity(int nx, int ny, int nz, double ustar, double ystar, double a9, double* ux,
+                         double* uy, double* uz) {
+    const size_t N = (size_t)nx * ny * nz;
+    const int nxh = nx / 2;
+    const double pi2 = 2.0 * (4.0 * atan(1.0));
+    const double A9 = a9, alpha = 1.0, beta9 = 1.0, cc = 60.0;
+    const double ccc1 = -((double)ny / pi2 / alpha / ystar * A9 * ustar / cc / cc);
+    for (size_t n = 0; n < N; ++n) ux[n] = uy[n] = uz[n] = 0.0;
+    for (int i = 1; i <= nxh; ++i) {
+        const double yplus = ((double)i - 0.5) / ystar;
+        double v;
+        if (yplus < 10.8) {
+            v = yplus * ustar;
+        } else {
+            double u9 = log(yplus) / 0.41 + 5.0;
+            v = u9 * ustar;
+        }
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j) {
+                uy[NODE(i - 1, j, k)] = v;
+                uy[NODE(nx - i, j, k)] = v;
+            }
+    }
+    for (int k = 1; k <= nz; ++k) {
+        const double z9 = pi2 * ((double)k - 0.5) / (double)nz;
+        for (int j = 1; j <= ny; ++j) {
+            const double y9 = pi2 * ((double)j - 0.5) / (double)ny;
+            for (int i = 1; i <= nxh; ++i) {
+                const double yplus = ((double)i - 0.5) / ystar;
+                const double ccc9 = exp(-yplus / cc);
+                double u9 = ccc1 * yplus * ccc9 * sin(alpha * y9 + beta9 * z9);
+                uy[NODE(i - 1, j - 1, k - 1)] = uy[NODE(i - 1, j - 1, k - 1)] + u9;
+                uy[NODE(nx - i, j - 1, k - 1)] = uy[NODE(nx - i, j - 1, k - 1)] + u9;
+                const double ccc10 = A9 * ustar * (1.0 - ccc9 - yplus / cc * ccc9);
+                u9 = ccc10 * cos(alpha * y9 + beta9 * z9);
+                ux[NODE(i - 1, j - 1, k - 1)] = ux[NODE(i - 1, j - 1, k - 1)] + u9;
+                ux[NODE(nx - i, j - 1, k - 1)] = ux[NODE(nx - i, j - 1, k - 1)] + u9;
+            }
+        }
+    }
+}
+
 /* =========================================================================
  * Moving spheres.  The reference declares links, fill lists and particle
  * state (var_inc.f90:120-150, para.f90:332-379, solid-node velocity in
@@ -518,6 +565,45 @@ static double min_image(double d, double L) {
     if (d >= 0.5 * L) d -= L;
     else if (d < -0.5 * L) d += L;
     return d;
+}
+
+/* Seeded sphere placement (the reference seeds its particle placement with
+ * iseedp, para.f90:362, but ships the placement code in the absent particle
+ * library).  Candidate k's attempt a draws three uniforms from the counter
+ * generator with consecutive keys; x lies in [R + wall_gap, nx - R - wall_gap],
+ * y and z anywhere in the periodic spans; a candidate is accepted when its
+ * minimal-image distance to every placed sphere is at least 2R + gap.  The
+ * overlap test here is a plain scan over all placed spheres; it accepts and
+ * rejects exactly the candidates that a cell-list search would.  Returns 0, or
+ * -1 when a sphere cannot be placed in 100000 attempts. */
+int orc_particles_place(int nx, int ny, int nz, int npart, double radius, double gap, double wall_gap,
+                        uint64_t seed, double* pos) {
+    const double lo = radius + wall_gap, hi = (double)nx - radius - wall_gap;
+    if (!(hi > lo)) return -1;
+    const double dmin = 2.0 * radius + gap;
+    uint64_t key = 0;
+    for (int k = 0; k < npart; ++k) {
+        int placed = 0;
+        for (int attempt = 0; attempt < 100000 && !placed; ++attempt) {
+            const double x = lo + (hi - lo) * 0.5 * (upm1(seed, key++) + 1.0);
+            const double y = ny * 0.5 * (upm1(seed, key++) + 1.0);
+            const double z = nz * 0.5 * (upm1(seed, key++) + 1.0);
+            int ok = 1;
+            for (int j = 0; j < k && ok; ++j) {
+                const double d0 = pos[3 * j] - x;
+                const double d1 = min_image(pos[3 * j + 1] - y, (double)ny);
+                const double d2 = min_image(pos[3 * j + 2] - z, (double)nz);
+                if (d0 * d0 + d1 * d1 + d2 * d2 < dmin * dmin) ok = 0;
+            }
+            if (!ok) continue;
+            pos[3 * k] = x;
+            pos[3 * k + 1] = y;
+            pos[3 * k + 2] = z;
+            placed = 1;
+        }
+        if (!placed) return -1;
+    }
+    return 0;
 }
 
 /* offset from sphere center to node (ix,iy,iz) and the inside test */

@@ -76,6 +76,17 @@ void orc_profiles(const double* rho, const double* ux, const double* uy,
 void orc_channel_velocity(int nx, int ny, int nz, double uc, double amp,
                           uint64_t seed, double* ux, double* uy, double* uz);
 
+/* initvel's turbulent branch (initial.f90:101-147): law-of-the-wall profile
+ * plus the perturbation with amplitude a9 (A9, 0 as shipped) */
+void orc_loglaw_velocity(int nx, int ny, int nz, double ustar, double ystar, double a9,
+                         double* ux, double* uy, double* uz);
+
+/* seeded non-overlapping sphere centres (reference axes, 3*npart): the same
+ * counter-generator draws and acceptance rule as the library's placement;
+ * returns 0, or -1 if the spheres do not fit */
+int orc_particles_place(int nx, int ny, int nz, int npart, double radius, double gap,
+                        double wall_gap, uint64_t seed, double* pos);
+
 /* ---- moving spheres (the reference declares the data but ships no
  * algorithm; this is the project's own design, restated here as
  * the checker of the GPU kernels) ---------------------------------------- */

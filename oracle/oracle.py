@@ -73,6 +73,9 @@ def lib() -> ctypes.CDLL:
             "orc_profiles": (None, [dp, dp, dp, dp, i, i, i, dp]),
             "orc_channel_velocity": (None, [i, i, i, ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
                                             dp, dp, dp]),
+            "orc_loglaw_velocity": (None, [i, i, i, ctypes.c_double, ctypes.c_double, ctypes.c_double, dp, dp, dp]),
+            "orc_particles_place": (i, [i, i, i, i, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_uint64, dp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -208,6 +211,22 @@ def channel_velocity(nx, ny, nz, uc, amp, seed):
     out = [np.empty((nx, ny, nz), dtype=np.float64, order="F") for _ in range(3)]
     lib().orc_channel_velocity(nx, ny, nz, uc, amp, ctypes.c_uint64(seed), *map(_p, out))
     return tuple(out)
+
+
+def loglaw_velocity(nx, ny, nz, ustar, ystar, a9=0.0):
+    """initvel's turbulent start (initial.f90:101-147), reference layout."""
+    out = [np.empty((nx, ny, nz), dtype=np.float64, order="F") for _ in range(3)]
+    lib().orc_loglaw_velocity(nx, ny, nz, ustar, ystar, a9, *map(_p, out))
+    return tuple(out)
+
+
+def place_spheres(nx, ny, nz, npart, radius, gap=2.0, wall_gap=1.0, seed=12345) -> np.ndarray:
+    """Seeded non-overlapping sphere centres (reference axes), shape (npart, 3)."""
+    pos = np.empty((npart, 3), dtype=np.float64)
+    rc = lib().orc_particles_place(nx, ny, nz, npart, radius, gap, wall_gap, ctypes.c_uint64(seed), _p(pos))
+    if rc != 0:
+        raise ValueError("could not place all spheres (volume fraction too high)")
+    return pos
 
 
 def poiseuille_transient(nx: int, ustar: float, visc: float, istep: int, nterms: int = 26) -> np.ndarray:

@@ -59,3 +59,23 @@ def test_reference_arm_under_torchrun_prints_one_line():
     assert len(lines) == 1
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["value"] > 0 and d["n_gpus"] == 2
+
+
+def test_reference_arm_loads_only_the_oracle():
+    """The reference arm times the oracle alone: the product library is never
+    mapped into that process, and it prints the GPU arm's metric and unit."""
+    script = (
+        "import runpy, sys\n"
+        "sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '3', '--cpu-budget', '1']\n"
+        "runpy.run_path('bench.py', run_name='__main__')\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "print('MAPPED', 'liblbm_gb300' in maps, 'liblbm_oracle' in maps)\n")
+    env = dict(os.environ, OMP_NUM_THREADS="2")
+    p = subprocess.run([sys.executable, "-c", script], capture_output=True, text=True, timeout=300, cwd=REPO, env=env)
+    assert p.returncode == 0, p.stderr[-2000:]
+    assert "MAPPED False True" in p.stdout
+    d = json.loads(next(ln for ln in p.stdout.splitlines() if ln.startswith("{")))
+    sys.path.insert(0, str(REPO))
+    import bench
+    assert d["metric"] == bench.METRIC and d["unit"] == "GLUPS" and d["higher_is_better"] is True
+    assert d["cpu_baseline"]["kind"] == "port" and "fluid nodes" in d["cpu_baseline"]["sample"]

@@ -29,9 +29,15 @@ def test_library_exports_every_declared_symbol(lib, pkg):
     assert sorted(pkg.EXPORTS) == names
 
 
-def test_library_is_built_for_sm103a(pkg):
-    data = pkg.library_path().read_bytes()
-    assert b"sm_103a" in data
+def test_library_build_targets_sm103a_only():
+    """The build recipe compiles every translation unit for sm_103a alone."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "lbm_gb300_build", Path(__file__).resolve().parents[1] / "d3q19-single-phase_gb300" / "_build.py")
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    assert b.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+    assert all(a in b.NVCC_FLAGS for a in b.ARCH)
 
 
 def test_params_init_matches_para(lib, pkg):
@@ -82,6 +88,39 @@ def test_channel_velocity_host_copy_matches_oracle(pkg, orc):
         b = orc.channel_velocity(*shape, 0.05, 0.05, seed)
         for x, y in zip(a, b):
             assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("shape,a9", [((64, 32, 16), 0.0), ((63, 20, 12), 1.5)])
+def test_loglaw_velocity_host_copy_matches_oracle(pkg, orc, shape, a9):
+    """The library's table form of initvel (transcendentals per wall plane and
+    per column) gives the bits of the oracle's literal loops."""
+    ustar, visc = 0.0035, 0.0012
+    a = pkg.loglaw_velocity(*shape, ustar, visc / ustar, a9)
+    b = orc.loglaw_velocity(*shape, ustar, visc / ustar, a9)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
+def test_loglaw_velocity_rejects_bad_arguments(lib):
+    buf = (ctypes.c_double * 64)()
+    assert lib.lbm_loglaw_velocity(4, 4, 4, ctypes.c_double(0.0), ctypes.c_double(1.0), ctypes.c_double(0.0),
+                                   buf, buf, buf) == -1
+    assert lib.lbm_loglaw_velocity(4, 4, 4, ctypes.c_double(0.1), ctypes.c_double(float("nan")),
+                                   ctypes.c_double(0.0), buf, buf, buf) == -1
+    assert lib.lbm_init_loglaw(None, ctypes.c_double(0.1), ctypes.c_double(1.0), ctypes.c_double(0.0)) == -1
+
+
+def test_oracle_sphere_placement_matches_library(pkg, orc):
+    """The oracle restates the seeded placement (its plain all-pairs overlap
+    scan against the library's cell list): the same centres bit for bit, so
+    the CPU baseline runs the same geometry without the product library."""
+    for args, seed in (((64, 64, 64, 16, 8.0), 12345), ((64, 128, 128, 256, 4.0), 7),
+                       ((128, 256, 128, 256, 8.0), 99)):
+        a = orc.place_spheres(*args, gap=2.0, wall_gap=1.0, seed=seed)
+        b = pkg.place_spheres(*args, gap=2.0, wall_gap=1.0, seed=seed)
+        assert np.array_equal(a, b)
+    with pytest.raises(ValueError):
+        orc.place_spheres(16, 16, 16, 50, 6.0)
 
 
 def test_channel_configs(pkg):

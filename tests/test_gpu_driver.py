@@ -5,9 +5,10 @@ Particle checkpoints are the reference's endrunpart2D files
 
 Checks: a sphere run through the driver equals the same calls made through
 the Python binding (same checkpoint header; populations and sphere state equal
-to rounding: the momentum exchange sums link forces with FP64 atomics, whose
-order varies from run to run, so two identical runs agree to the last bits
-only, relative L-inf <= 1e-12 / 1e-10); a run stopped
+to rounding: the bounce-back kernel lists a sphere's candidate rows with a
+shared-memory counter, so which lane sums which links -- and the rounding of
+the per-sphere force sums -- varies from run to run, and two identical runs
+agree to the last bits only, relative L-inf <= 1e-12 / 1e-10); a run stopped
 and continued from its endrunflow/endrunpart checkpoints equals the
 uninterrupted run across an odd restart step and the every-100-steps mean
 density removal (relative L-inf <= 1e-11 in the populations, 1e-10 in the

@@ -62,6 +62,30 @@ def test_device_initial_condition_is_bitwise_oracle_initpop(pkg, orc):
         assert np.array_equal(lat.download_f(), g)
 
 
+@pytest.mark.parametrize("shape,a9", [((8, 40, 6), 0.0), ((9, 24, 10), 1.5), ((64, 32, 16), 0.7)])
+def test_device_loglaw_initial_condition_is_bitwise_oracle(pkg, orc, shape, a9):
+    """initvel's turbulent start (initial.f90:101-147) + initpop on the device
+    equals the oracle's literal restatement bit for bit, the perturbation
+    (A9 != 0) and an odd wall-normal size (untouched middle plane) included;
+    lbm_prerelax takes the host copy of the same field."""
+    ustar = 0.0035
+    ystar = 0.0012 / ustar
+    u = orc.loglaw_velocity(*shape, ustar, ystar, a9)
+    want = orc.initpop(*u)
+    with pkg.Lattice(stable_run(pkg, shape)) as lat:
+        lat.init_loglaw(ustar, ystar, a9)
+        assert np.array_equal(lat.download_f(), want)
+    for prec in ("fp32", "fp16"):
+        with pkg.Lattice(stable_run(pkg, shape, precision=prec)) as lat:
+            lat.init_loglaw(ustar, ystar, a9)
+            g = lat.download_f()
+        # one rounding of each stored deviation: half an ulp of the storage type
+        # (FP16 holds 2^15 (f - w), 11 significant bits; subnormals below 2^-14)
+        rel_ulp = 2.0**-24 if prec == "fp32" else 2.0**-11
+        floor = 0.0 if prec == "fp32" else 2.0**-25 / 2**15
+        assert (np.abs(g - want) <= 1.001 * rel_ulp * np.abs(want) + floor).all()
+
+
 @pytest.mark.parametrize("nsteps", [1, 2, 3, 8])
 def test_steps_match_oracle_fp64(pkg, orc, nsteps):
     shape = (6, 12, 5)

@@ -290,6 +290,33 @@ def test_channel_velocity_generator(orc):
     assert np.abs(ux).max() <= amp * uc and np.abs(uz).max() <= amp * uc
 
 
+def test_loglaw_velocity_is_initvel_turbulent_start(orc):
+    """initvel's ivel branch (initial.f90:101-147) by hand in numpy: the law
+    of the wall (u+ = y+ below y+ = 10.8, ln(y+)/0.41 + 5 above), mirrored
+    onto the upper half, the middle plane of an odd channel at rest, and the
+    perturbation with A9 from the reference's formulas."""
+    nx, ny, nz, ustar, visc = 41, 12, 10, 0.0035, 0.0012
+    ystar = visc / ustar
+    ux, uy, uz = orc.loglaw_velocity(nx, ny, nz, ustar, ystar, 0.0)
+    assert not ux.any() and not uz.any()
+    yp = (np.arange(1, nx // 2 + 1) - 0.5) / ystar
+    prof = np.where(yp < 10.8, yp * ustar, (np.log(yp) / 0.41 + 5.0) * ustar)
+    assert np.allclose(uy[: nx // 2, 3, 4], prof, rtol=1e-15, atol=0)
+    assert np.array_equal(uy[::-1], uy)
+    assert not uy[nx // 2].any()
+    a9 = 1.5
+    px, py, _ = orc.loglaw_velocity(nx, ny, nz, ustar, ystar, a9)
+    pi2 = 2 * np.pi
+    j, k = 5, 7
+    arg = pi2 * (j + 1 - 0.5) / ny + pi2 * (k + 1 - 0.5) / nz
+    e = np.exp(-yp / 60.0)
+    ccc1 = -ny / pi2 / ystar * a9 * ustar / 60.0 / 60.0
+    assert np.allclose(py[: nx // 2, j, k], prof + ccc1 * yp * e * np.sin(arg), rtol=1e-13, atol=0)
+    assert np.allclose(px[: nx // 2, j, k], a9 * ustar * (1 - e - yp / 60.0 * e) * np.cos(arg), rtol=1e-12,
+                       atol=1e-18)
+    assert np.array_equal(px[::-1], px)
+
+
 def test_oracle_reproduces_golden_fixture(orc):
     """The committed fixture (tests/golden/make_golden.py) pins the oracle."""
     import importlib.util
