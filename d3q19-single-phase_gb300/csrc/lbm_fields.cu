@@ -181,19 +181,6 @@ __device__ __forceinline__ void equilibrium_rn(double ux, double uy, double uz, 
 }
 
 template <typename T>
-__global__ void k_initpop(DeviceState s, const double* __restrict__ ux, const double* __restrict__ uy,
-                          const double* __restrict__ uz, int z0) {
-    const RefNode r = ref_node(s.g, z0);
-    if (!r.ok) return;
-    const size_t src = ref_lin(s.g, r.ix, r.iy, r.iz - z0);
-    double f[Q];
-    equilibrium_rn(ux[src], uy[src], uz[src], f);
-    const uint32_t n = gpu_lin(s.g, r.ix, r.iy, r.iz);
-#pragma unroll
-    for (int i = 0; i < Q; ++i) put<T>(s, i, n, f[i]);
-}
-
-template <typename T>
 __global__ void k_init_channel(DeviceState s, double uc, double amp, uint64_t seed) {
     const RefNode r = ref_node(s.g, 0);
     if (!r.ok) return;
@@ -204,6 +191,65 @@ __global__ void k_init_channel(DeviceState s, double uc, double amp, uint64_t se
     const uint32_t n = gpu_lin(s.g, r.ix, r.iy, r.iz);
 #pragma unroll
     for (int i = 0; i < Q; ++i) put<T>(s, i, n, f[i]);
+}
+
+// Reference-layout fields <-> SoA nodes through shared-memory tiles.  The
+// reference layout runs along x (wall-normal) fastest, the population planes
+// along y (streamwise), so a kernel that walks either one strides through the
+// other by nx*8 bytes per thread.  These kernels take a tile of 32 (x) x 32 (y)
+// nodes at one z: the FP64 field side moves along x (coalesced 256-byte
+// rows), the population side along y (coalesced plane rows), and the tile is
+// turned around in shared memory.  FP64 storage computes in FP64 with the
+// explicitly rounded operations of the oracle (same bits); FP32/FP16 storage
+// computes in FP32, which is exact to well below its storage precision.
+constexpr int kTile = 32, kTileRows = 8;
+
+__device__ __forceinline__ void equilibrium_f(float ux, float uy, float uz, float f[Q]) {
+    const float usqr = 1.5f * (ux * ux + uy * uy + uz * uz);
+    f[0] = (float)W0 * (-usqr);
+#pragma unroll
+    for (int i = 1; i < Q; ++i) {
+        const float G = (float)CXf(i) * ux + (float)CYf(i) * uy + (float)CZf(i) * uz;
+        f[i] = (float)weight(i) * (3.f * G + 4.5f * G * G - usqr);
+    }
+}
+
+template <typename T, typename R>
+__global__ void __launch_bounds__(kTile * kTileRows)
+k_initpop_t(DeviceState s, const double* __restrict__ ux, const double* __restrict__ uy,
+            const double* __restrict__ uz, int z0) {
+    __shared__ double U[3][kTile][kTile + 1];              // [y][x]
+    const int nx = s.g.NZ, ny = s.g.NX;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int ix0 = blockIdx.y * kTile, iy0 = blockIdx.x * kTile, iz = z0 + blockIdx.z;
+    const size_t base = (size_t)nx * ny * blockIdx.z;      // chunk-relative z plane
+    for (int r = ty; r < kTile; r += kTileRows) {
+        const int iy = iy0 + r, ix = ix0 + tx;
+        if (iy < ny && ix < nx) {
+            const size_t o = base + (size_t)ix + (size_t)nx * iy;
+            U[0][r][tx] = ux[o];
+            U[1][r][tx] = uy[o];
+            U[2][r][tx] = uz[o];
+        }
+    }
+    __syncthreads();
+    for (int r = ty; r < kTile; r += kTileRows) {
+        const int ix = ix0 + r, iy = iy0 + tx;
+        if (ix >= nx || iy >= ny) continue;
+        const uint32_t n = gpu_lin(s.g, ix, iy, iz);
+        if constexpr (sizeof(R) == 8) {
+            double f[Q];
+            equilibrium_rn(U[0][tx][r], U[1][tx][r], U[2][tx][r], f);
+#pragma unroll
+            for (int i = 0; i < Q; ++i) put<T>(s, i, n, f[i]);
+        } else {
+            float f[Q];
+            equilibrium_f((float)U[0][tx][r], (float)U[1][tx][r], (float)U[2][tx][r], f);
+            const float S = s.cf.S;
+#pragma unroll
+            for (int i = 0; i < Q; ++i) st_pop(pop_plane<T>(s, i) + n, f[i] * S);
+        }
+    }
 }
 
 // Log-law initial velocity (initvel's turbulent branch, initial.f90:101-147)
@@ -254,36 +300,63 @@ __device__ __forceinline__ void macro_of(const R f[Q], const R F[3], R& rho, R& 
     rho = r; ux = a + R(0.5) * F[0]; uy = b + R(0.5) * F[1]; uz = c + R(0.5) * F[2];
 }
 
-template <typename T>
-__global__ void k_macro(DeviceState s, int parity, double* rho, double* ux, double* uy,
-                        double* uz, int z0) {
-    const RefNode r = ref_node(s.g, z0);
-    if (!r.ok) return;
-    double f[Q];
-    gather_natural<T>(s, parity, r.iy, r.iz, r.ix, f);
-    const double F[3] = {(double)s.cd.Fx, (double)s.cd.Fy, (double)s.cd.Fz};
-    double d, a, b, c;
-    macro_of<double>(f, F, d, a, b, c);
-    const int own = s.owner ? s.owner[gpu_lin(s.g, r.ix, r.iy, r.iz)] : -1;
-    if (own >= 0) {
-        // solid node: rigid-body velocity and rho = rhopart (collision.f90:420-458)
-        const double* X = s.ppos + 3 * own;
-        const double* U = s.pvel + 3 * own;
-        const double* W = s.pomg + 3 * own;
-        auto mi = [](double v, double L) { return v >= 0.5 * L ? v - L : (v < -0.5 * L ? v + L : v); };
-        const double x0 = (r.ix + 0.5) - X[0];
-        const double y0 = mi((r.iy + 0.5) - X[1], (double)s.g.NX);
-        const double z0c = mi((r.iz + 0.5) - X[2], (double)s.g.NY);
-        a = U[0] + (W[1] * z0c - W[2] * y0);
-        b = U[1] + (W[2] * x0 - W[0] * z0c);
-        c = U[2] + (W[0] * y0 - W[1] * x0);
-        d = s.prho;
+// macrovar through a shared-memory tile (see k_initpop_t): populations read
+// along y, the four FP64 fields written along x.
+template <typename T, typename R>
+__global__ void __launch_bounds__(kTile * kTileRows)
+k_macro_t(DeviceState s, int parity, double* rho, double* ux, double* uy, double* uz, int z0) {
+    __shared__ double M[4][kTile][kTile + 1];              // [x][y]
+    const int nx = s.g.NZ, ny = s.g.NX;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int ix0 = blockIdx.y * kTile, iy0 = blockIdx.x * kTile, iz = z0 + blockIdx.z;
+    for (int r = ty; r < kTile; r += kTileRows) {
+        const int ix = ix0 + r, iy = iy0 + tx;
+        if (ix >= nx || iy >= ny) continue;
+        double d, a, b, c;
+        if constexpr (sizeof(R) == 8) {
+            double f[Q];
+            gather_natural<T>(s, parity, iy, iz, ix, f);
+            const double F[3] = {(double)s.cd.Fx, (double)s.cd.Fy, (double)s.cd.Fz};
+            macro_of<double>(f, F, d, a, b, c);
+        } else {
+            float f[Q];
+            gather_natural_r<T, float>(s, parity, iy, iz, ix, f);
+            const float F[3] = {s.cf.Fx, s.cf.Fy, s.cf.Fz};
+            float fd, fa, fb, fc;
+            macro_of<float>(f, F, fd, fa, fb, fc);
+            d = fd; a = fa; b = fb; c = fc;
+        }
+        const int own = s.owner ? s.owner[gpu_lin(s.g, ix, iy, iz)] : -1;
+        if (own >= 0) {
+            // solid node: rigid-body velocity and rho = rhopart (collision.f90:420-458)
+            const double* X = s.ppos + 3 * own;
+            const double* U = s.pvel + 3 * own;
+            const double* W = s.pomg + 3 * own;
+            auto mi = [](double v, double L) { return v >= 0.5 * L ? v - L : (v < -0.5 * L ? v + L : v); };
+            const double x0 = (ix + 0.5) - X[0];
+            const double y0 = mi((iy + 0.5) - X[1], (double)s.g.NX);
+            const double z0c = mi((iz + 0.5) - X[2], (double)s.g.NY);
+            a = U[0] + (W[1] * z0c - W[2] * y0);
+            b = U[1] + (W[2] * x0 - W[0] * z0c);
+            c = U[2] + (W[0] * y0 - W[1] * x0);
+            d = s.prho;
+        }
+        M[0][r][tx] = d;
+        M[1][r][tx] = a;
+        M[2][r][tx] = b;
+        M[3][r][tx] = c;
     }
-    const size_t o = ref_lin(s.g, r.ix, r.iy, r.iz - z0);
-    if (rho) rho[o] = d;
-    if (ux) ux[o] = a;
-    if (uy) uy[o] = b;
-    if (uz) uz[o] = c;
+    __syncthreads();
+    const size_t base = (size_t)nx * ny * blockIdx.z;
+    for (int r = ty; r < kTile; r += kTileRows) {
+        const int iy = iy0 + r, ix = ix0 + tx;
+        if (iy >= ny || ix >= nx) continue;
+        const size_t o = base + (size_t)ix + (size_t)nx * iy;
+        if (rho) rho[o] = M[0][tx][r];
+        if (ux) ux[o] = M[1][tx][r];
+        if (uy) uy[o] = M[2][tx][r];
+        if (uz) uz[o] = M[3][tx][r];
+    }
 }
 
 // Strain rate from the non-equilibrium part of the populations, the two ways
@@ -877,9 +950,20 @@ cudaError_t launch_store_to_aos(const DeviceState& s, int parity, double* aos, i
     LBM_DISPATCH(s.prec, (k_store_to_aos<T><<<ref_grid(s.g, nzc, kBx), kBx, 0, st>>>(s, parity, aos, z0)))
 }
 
+dim3 tile_grid(const Geometry& g, int nzc) {
+    return dim3((unsigned)((g.NX + kTile - 1) / kTile), (unsigned)((g.NZ + kTile - 1) / kTile), (unsigned)nzc);
+}
+
 cudaError_t launch_initpop(const DeviceState& s, const double* ux, const double* uy,
                            const double* uz, int z0, int nzc, cudaStream_t st) {
-    LBM_DISPATCH(s.prec, (k_initpop<T><<<ref_grid(s.g, nzc, kBx), kBx, 0, st>>>(s, ux, uy, uz, z0)))
+    const dim3 blk(kTile, kTileRows);
+    switch (s.prec) {
+        case LBM_PREC_FP64: k_initpop_t<double, double><<<tile_grid(s.g, nzc), blk, 0, st>>>(s, ux, uy, uz, z0); break;
+        case LBM_PREC_FP32: k_initpop_t<float, float><<<tile_grid(s.g, nzc), blk, 0, st>>>(s, ux, uy, uz, z0); break;
+        case LBM_PREC_FP16: k_initpop_t<__half, float><<<tile_grid(s.g, nzc), blk, 0, st>>>(s, ux, uy, uz, z0); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
 }
 
 cudaError_t launch_init_channel(const DeviceState& s, double uc, double amp, uint64_t seed,
@@ -899,7 +983,14 @@ cudaError_t launch_owner_to_ref(const DeviceState& s, const int* owner, int32_t*
 
 cudaError_t launch_macro(const DeviceState& s, int parity, double* rho, double* ux, double* uy,
                          double* uz, int z0, int nzc, cudaStream_t st) {
-    LBM_DISPATCH(s.prec, (k_macro<T><<<ref_grid(s.g, nzc, kBx), kBx, 0, st>>>(s, parity, rho, ux, uy, uz, z0)))
+    const dim3 blk(kTile, kTileRows), grid = tile_grid(s.g, nzc);
+    switch (s.prec) {
+        case LBM_PREC_FP64: k_macro_t<double, double><<<grid, blk, 0, st>>>(s, parity, rho, ux, uy, uz, z0); break;
+        case LBM_PREC_FP32: k_macro_t<float, float><<<grid, blk, 0, st>>>(s, parity, rho, ux, uy, uz, z0); break;
+        case LBM_PREC_FP16: k_macro_t<__half, float><<<grid, blk, 0, st>>>(s, parity, rho, ux, uy, uz, z0); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
 }
 
 cudaError_t launch_strain(const DeviceState& s, int parity, double* m1, double* m2, int z0, int nzc,

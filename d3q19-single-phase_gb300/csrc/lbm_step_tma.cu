@@ -25,10 +25,11 @@
 //
 // Every mbarrier wait is bounded.  A wait that gives up raises a CTA-wide
 // abort flag and the global error flag (the host then reports the step as
-// failed): from then on no warp issues another bulk load or store, every warp
-// leaves the item loop at its next item, and before the CTA exits one thread
-// waits (again bounded) for every stage's last issued load to land, so that
-// no bulk copy still targets the CTA's shared memory when it exits.
+// failed) and its warp leaves the item loop: from then on no stage is stored
+// or refilled, so every other warp gives up at its next wait (bounded too)
+// and leaves as well, and before the CTA exits one thread waits (again
+// bounded) for every stage's last issued load to land, so that no bulk copy
+// still targets the CTA's shared memory when it exits.
 #include <algorithm>
 
 #include "lbm_internal.h"
@@ -163,6 +164,7 @@ __device__ __forceinline__ const T* src_row(const PopPtrs<T>& P, const Geometry&
                                             unsigned* bflag, unsigned site) {
     const int dz = dz_rt(i);
     const bool bb = (dz == 1 && (wall & 1)) || (dz == -1 && (wall & 2));
+#ifdef LBM_BOUNDS_CHECK
     int k = i;
     uint32_t row = I.row;
     if (ODD && !bb) {
@@ -173,6 +175,12 @@ __device__ __forceinline__ const T* src_row(const PopPtrs<T>& P, const Geometry&
                                   (size_t)row + g.NX <= (size_t)g.NXY * g.NZ, site))
         return P.p[0];
     return P.p[k] + row;
+#else
+    (void)bflag;
+    (void)site;
+    if (!ODD || bb) return P.p[i] + I.row;
+    return P.p[opp_rt(i)] + row_at(g, I.y - dy_rt(i), I.z - dz);
+#endif
 }
 // Issued by one warp: lane i moves population i's row.  The mbarrier learns the
 // byte count from lane 0 before any copy is issued.
@@ -306,9 +314,11 @@ k_step_rows(PopPtrs<T> P, CollideConsts<float> C, Geometry g, int nstage, int* e
     }
     for (uint32_t k = 0;; ++k) {
         const uint32_t it = blockIdx.x + k * G;
-        if (it >= total || abort_flag) break;
+        if (it >= total) break;
         const int s = (int)(k % (uint32_t)nstage);
         if (!mbar_wait(bars + 8 * s, (k / (uint32_t)nstage) & 1u)) {
+            // no stage is refilled after this, so every other warp leaves
+            // the loop at its next wait (bounded as well)
             abort_flag = 1;
             break;
         }
@@ -329,13 +339,13 @@ k_step_rows(PopPtrs<T> P, CollideConsts<float> C, Geometry g, int nstage, int* e
             last = atomicAdd(&done_count[s], 1u) == nwarps - 1;
             if (last) done_count[s] = 0;
         }
-        last = __shfl_sync(0xffffffffu, last, 0) && !abort_flag;
-        if (last) {
+        last = __shfl_sync(0xffffffffu, last, 0);
+        if (last && !abort_flag) {
             __threadfence_block();
             fence_proxy_async();
             store_item<T, ODD>(P, g, it, data + s * stage_bytes, row_bytes, lane, bflag);
             const uint32_t nit = blockIdx.x + (k + (uint32_t)nstage) * G;
-            if (nit < total && !abort_flag)
+            if (nit < total)
                 issue_item<T, ODD>(P, g, nit, data + s * stage_bytes, bars + 8 * s, row_bytes, lane, &issued[s],
                                    bflag);
         }

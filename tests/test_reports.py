@@ -47,6 +47,34 @@ def test_precision_sweep_report(grid, shape, spheres, steps, fp16_drag):
     assert np.isclose(np.abs(lp - ref).max() / np.abs(ref).max(), r["errors"]["fp16"]["mean_profile_rel_err"])
 
 
+def test_precision_sweep_from_developed_turbulence():
+    """The same comparison from developed turbulence (precision_sweep.py
+    --start developed): a particle-free FP32 DNS of the 512 x 256 x 256
+    channel is run 200000 steps from a streak/vortex trigger, its populations
+    start all runs, the 2048 spheres are added and every run covers 6000
+    steps.  The FP64 Reynolds shear stress peaks at ~0.9 u*^2 in the window
+    (0.75 at the end of the spin-up).  FP32 and FP16 storage stay within 1%
+    of FP64 in the mean profile, the Reynolds stress and the mean drag; the
+    chaos floor (a second FP64 run from populations perturbed by 1e-12) is
+    far below, so the FP16 figures are precision errors, not decorrelation.
+    All runs share the mean-density change of the first removal (the DNS
+    state's mean density over the fluid nodes, -1.8e-7)."""
+    r = json.loads((GOLDEN / "precision_sweep_512x256x256_developed_report.json").read_text())
+    assert r["start"] == "developed" and r["spinup"]["steps"] == 200000
+    assert r["spinup"]["history"][-1][1] >= 0.6
+    assert max(x["peak_stress"] for x in r["series"]["fp64"]) >= 0.6
+    for p in ("fp64", "fp64_perturbed", "fp32", "fp16"):
+        assert r["runs"][p]["fail"] is None and r["runs"][p]["steps_done"] == r["steps"] == 6000
+    for p in ("fp32", "fp16"):
+        e = r["errors"][p]
+        assert e["mean_profile_rel_err"] < 0.01 and e["reynolds_stress_rel_err"] < 0.01
+        assert e["drag_mean_rel_err"] < 0.01
+    floor = r["errors"]["fp64_perturbed"]
+    assert floor["reynolds_stress_rel_err"] < 1e-5 < r["errors"]["fp16"]["reynolds_stress_rel_err"]
+    d64, d32 = r["runs"]["fp64"]["mean_density_drift"], r["runs"]["fp32"]["mean_density_drift"]
+    assert abs(d64 - d32) < 1e-9
+
+
 def _sweep_module():
     import importlib.util
     path = Path(__file__).resolve().parents[1] / "d3q19-single-phase_gb300" / "precision_sweep.py"
