@@ -16,10 +16,11 @@ Printed JSON line (rank 0):
              nodes inside spheres are not counted, as the reference skips
              them in its collision, collision.f90:54), device-resident state,
              CUDA-event timed; `all_nodes_glups` counts every lattice node
-  e2e        GLUPS through the C ABI with host buffers: initpop from pinned
-             host velocity arrays, the steps (one synchronous lbm_step call
-             each, lbm_diag every 250 steps), macrovar back to pinned host
-             arrays -- all inside the timed region
+  e2e        fluid-node GLUPS through the C ABI with host buffers: initpop
+             from pinned host velocity arrays, the steps (one synchronous
+             lbm_step call each, lbm_diag every 250 steps), macrovar back to
+             pinned host arrays -- all inside the timed region, after one
+             untimed pass of the same calls
   roofline   38 populations x 2 B per fluid node per step over the measured
              HBM copy bandwidth, for the step kernel and for the whole step;
              traffic from the committed ncu capture
@@ -467,6 +468,13 @@ def e2e_run(pkg, torch, cfg, prec, steps, device, world, pos=None, pflags=0):
     lat = pkg.Lattice(cfg.params(prec, device=device))
     ndiag = 250
     diag_bytes = (cfg.wall * 64 * pkg.PROFILE_COLS + 1024 * 5) * 8
+    # untimed warm-up of the same calls: the first device access to each host
+    # page of the buffers costs far more than later ones on this platform
+    lat.initpop(arrs[0], arrs[1], arrs[2])
+    if pos is not None:
+        lat.set_particles(pos, cfg.radius, 2.0, flags=pflags)
+    lat.step(1)
+    lib.lbm_macrovar(lat._ctx, *(pkg._dptr(a) for a in arrs))
     barrier(world)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -486,14 +494,15 @@ def e2e_run(pkg, torch, cfg, prec, steps, device, world, pos=None, pflags=0):
         pbytes = 5 * pos.size * 8
     dt = time.perf_counter() - t0
     dt = allmax(world, dt)
+    nf = lat.diag().nfluid                       # fluid nodes (after the run)
     lat.close()
-    return {"value": round(world * N * steps / dt / 1e9, 4), "unit": "GLUPS",
+    return {"value": round(world * nf * steps / dt / 1e9, 4), "unit": "GLUPS",
             "h2d_bytes_per_step": int((3 * N * 8 + (pos.size * 8 if pos is not None else 0)) / steps),
             "d2h_bytes_per_step": int((4 * N * 8 + ndiags * diag_bytes + pbytes) / steps),
             "path": ("lbm_initpop(host u)" + (" + lbm_particles_set(host)" if pos is not None else "")
                      + " -> lbm_step(1) x steps (+lbm_diag every 250) -> lbm_macrovar(host)"
                      + (" + lbm_particles_get(host)" if pos is not None else "")),
-            "seconds": round(dt, 3)}
+            "seconds": round(dt, 3), "warmup": "one untimed pass of the same calls"}
 
 
 def main():

@@ -25,8 +25,8 @@
 //
 // Every mbarrier wait is bounded.  A wait that gives up raises a CTA-wide
 // abort flag and the global error flag (the host then reports the step as
-// failed) and its warp leaves the item loop: from then on no stage is stored
-// or refilled, so every other warp gives up at its next wait (bounded too)
+// failed) and its warp leaves the item loop: from then on no stage is
+// refilled, so every other warp gives up at its next wait (bounded too)
 // and leaves as well, and before the CTA exits one thread waits (again
 // bounded) for every stage's last issued load to land, so that no bulk copy
 // still targets the CTA's shared memory when it exits.
@@ -190,16 +190,14 @@ template <typename T, bool ODD>
 __device__ __forceinline__ void issue_item(const PopPtrs<T>& P, const Geometry& g, uint32_t it, uint32_t stage_smem,
                                            uint32_t bar, uint32_t row_bytes, int lane, unsigned* issued,
                                            unsigned* bflag) {
-    if (lane == 0) {
-        ++*issued;
-        mbar_expect_tx(bar, (uint32_t)Q * row_bytes);
-    }
+    if (lane == 0) mbar_expect_tx(bar, (uint32_t)Q * row_bytes);
     __syncwarp();
     if (lane < Q) {
         const Item I = item_of(g, it);
         bulk_load(stage_smem + (uint32_t)lane * row_bytes,
                   src_row<T, ODD>(P, g, I, wall_of(g, I.z), lane, bflag, 301), row_bytes, bar);
     }
+    if (lane == 0) ++*issued;          // off the refill's critical path: read only by the drain
 }
 
 // Two adjacent nodes (x, x+1), x even, of one item; the results go back into
@@ -340,12 +338,16 @@ k_step_rows(PopPtrs<T> P, CollideConsts<float> C, Geometry g, int nstage, int* e
             if (last) done_count[s] = 0;
         }
         last = __shfl_sync(0xffffffffu, last, 0);
-        if (last && !abort_flag) {
+        if (last) {
             __threadfence_block();
             fence_proxy_async();
+            // every warp has passed this stage's wait, so its load had landed:
+            // storing it is safe even after an abort elsewhere; only the
+            // refill is withheld then
+            const int ab = abort_flag;
             store_item<T, ODD>(P, g, it, data + s * stage_bytes, row_bytes, lane, bflag);
             const uint32_t nit = blockIdx.x + (k + (uint32_t)nstage) * G;
-            if (nit < total)
+            if (nit < total && !ab)
                 issue_item<T, ODD>(P, g, nit, data + s * stage_bytes, bars + 8 * s, row_bytes, lane, &issued[s],
                                    bflag);
         }
