@@ -475,6 +475,11 @@ def e2e_run(pkg, torch, cfg, prec, steps, device, world, pos=None, pflags=0):
         lat.set_particles(pos, cfg.radius, 2.0, flags=pflags)
     lat.step(1)
     lib.lbm_macrovar(lat._ctx, *(pkg._dptr(a) for a in arrs))
+    # macrovar wrote (rho, ux, uy, uz) over the velocity inputs: refill them
+    rc = lib.lbm_channel_velocity(cfg.wall, cfg.stream, cfg.span, cfg.uc, cfg.amp, cfg.seed,
+                                  *(pkg._dptr(a) for a in arrs[:3]))
+    if rc != 0:
+        raise RuntimeError("lbm_channel_velocity failed")
     barrier(world)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
