@@ -405,7 +405,7 @@ def run_gpu(args, world, rank, local):
             "data": "synthetic (seeded Poiseuille + uniform noise initial state)",
             "config": {"workload": wname, "storage": prec, "nodes": N, "fluid_nodes": round(NF),
                        "grid_stream_span_wall": [cfg.stream, cfg.span, cfg.wall], "visc": cfg.visc,
-                       "ustar": cfg.ustar, "h": cfg.h, "mrt": "MRTtype 1 (para.f90)" + (f", s16={cfg.s16} (sphere-laden)" if cfg.s16 else ""),
+                       "ustar": cfg.ustar, "h": cfg.h, "mrt": "MRTtype 1 (para.f90)" + (f", s16={cfg.s16}" if cfg.s16 else ""),
                        "link_fractions": "fp64" if (args.qfp64 or prec == "fp64") else "fp32",
                        "l2": f"populations {N * 19 * BYTES[prec] / 1e9:.1f} GB >> 129 MB L2, no flush needed",
                        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},

@@ -381,11 +381,8 @@ class ChannelConfig:
     seed: int = 20240611
     spheres: int = 0
     radius: float = 0.0
-    # Sphere-laden channels relax the third-order odd moments (m_x, m_y, m_z)
-    # at 1.2 instead of MRTtype 1's 1.98: at tau ~ 0.507 the interpolated
-    # bounce-back on R = 8 spheres grows an instability at s16 = 1.98 (the
-    # 1024x512x512 run blew up near step 550; fixed spheres near step 275) and
-    # stays bounded at 1.2.
+    # rate of the third-order odd moments (m_x, m_y, m_z) when it should
+    # differ from the MRT type's; None keeps MRTtype 1's 1.98 (para.f90)
     s16: float | None = None
 
     @property
@@ -408,13 +405,13 @@ CHANNEL_CONFIGS = {
     "channel-128x64x64": ChannelConfig("channel-128x64x64", 128, 64, 64, visc=0.0012, ustar=0.0035, h=32, steps=2000),
     # particle-laden channel, Re_tau ~ 181 (fluid part)
     "spheres-256x128x128": ChannelConfig("spheres-256x128x128", 256, 128, 128, visc=0.0012, ustar=0.0034, h=64,
-                        steps=5000, spheres=256, radius=4.0, s16=1.2),
+                        steps=5000, spheres=256, radius=4.0),
     # precision sweep, Re_tau ~ 181
     "spheres-512x256x256": ChannelConfig("spheres-512x256x256", 512, 256, 256, visc=0.0024, ustar=0.0034, h=128,
-                        steps=20000, spheres=2048, radius=8.0, s16=1.2),
+                        steps=20000, spheres=2048, radius=8.0),
     # large channel, FP32 compute / FP16 storage, Re_tau ~ 363
     "spheres-1024x512x512": ChannelConfig("spheres-1024x512x512", 1024, 512, 512, visc=0.0024, ustar=0.0034, h=256,
-                        steps=2000, precision="fp16", spheres=16384, radius=8.0, s16=1.2),
+                        steps=2000, precision="fp16", spheres=16384, radius=8.0),
 }
 
 

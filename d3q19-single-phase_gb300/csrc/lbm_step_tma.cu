@@ -25,11 +25,11 @@
 //
 // Every mbarrier wait is bounded.  A wait that gives up raises a CTA-wide
 // abort flag and the global error flag (the host then reports the step as
-// failed) and its warp leaves the item loop: from then on no stage is
-// refilled, so every other warp gives up at its next wait (bounded too)
-// and leaves as well, and before the CTA exits one thread waits (again
-// bounded) for every stage's last issued load to land, so that no bulk copy
-// still targets the CTA's shared memory when it exits.
+// failed), and that lane waits no more: from then on no stage is refilled,
+// so every other lane gives up at its next wait (bounded too), the loop
+// runs out on whatever the stages hold, and before the CTA exits one thread
+// waits (again bounded) for every stage's last issued load to land, so that
+// no bulk copy still targets the CTA's shared memory when it exits.
 #include <algorithm>
 
 #include "lbm_internal.h"
@@ -310,15 +310,19 @@ k_step_rows(PopPtrs<T> P, CollideConsts<float> C, Geometry g, int nstage, int* e
                                    bflag);
         }
     }
+    bool failed = false;
     for (uint32_t k = 0;; ++k) {
         const uint32_t it = blockIdx.x + k * G;
         if (it >= total) break;
         const int s = (int)(k % (uint32_t)nstage);
-        if (!mbar_wait(bars + 8 * s, (k / (uint32_t)nstage) & 1u)) {
-            // no stage is refilled after this, so every other warp leaves
-            // the loop at its next wait (bounded as well)
+        // A lane whose wait gave up raises the abort flag and waits no more
+        // (it computes on whatever the stages hold; the step is reported as
+        // failed).  No stage is refilled after an abort, so every other lane
+        // gives up at its next wait, bounded as well.  All lanes keep running
+        // the same instructions, so the warp-wide shuffles stay complete.
+        if (!failed && !mbar_wait(bars + 8 * s, (k / (uint32_t)nstage) & 1u)) {
+            failed = true;
             abort_flag = 1;
-            break;
         }
         const Item I = item_of(g, it);
         const int wall = wall_of(g, I.z);

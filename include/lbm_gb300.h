@@ -290,8 +290,9 @@ int lbm_load_flow(lbm_ctx* ctx, const char* path, int32_t kind,
  * The reference declares particle state, links and fill lists
  * (var_inc.f90:120-150, para.f90:332-379, macrovar's solid branch
  * collision.f90:420-458) but ships no particle algorithm.  With spheres set,
- * every lbm_step also does: interpolated bounce-back (quadratic Bouzidi,
- * moving wall) and Galilean-invariant momentum exchange on every boundary
+ * every lbm_step also does: interpolated bounce-back (Bouzidi, quadratic for
+ * q < 1/2 and linear for q >= 1/2, moving wall) and Galilean-invariant
+ * momentum exchange on every boundary
  * link, soft-sphere repulsion (sphere-sphere and sphere-wall), the FP64
  * Newton-Euler update (driven by the average of this step's and the previous
  * step's force and torque), the geometry update and

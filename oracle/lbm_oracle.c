@@ -539,10 +539,11 @@ void orc_loglaw_velocity(int nx, int ny, int nz, double ustar, double ystar, dou
  *     periodic y and z);
  *   - link (x_f, i): fluid x_f with x_f + c_i inside sphere p; q in (0,1] is
  *     the fraction of c_i from x_f to the surface;
- *   - interpolated bounce-back after streaming: quadratic Bouzidi,
- *     Firdaouss & Lallemand (2001) with the moving-wall term
- *     -6 w_i c_i.u_w, falling back to linear, then to simple bounce-back,
- *     when the stencil leaves the fluid or the domain;
+ *   - interpolated bounce-back after streaming (Bouzidi, Firdaouss &
+ *     Lallemand 2001): quadratic for q < 1/2, linear for q >= 1/2, with the
+ *     moving-wall term -6 w_i c_i.u_w (Lallemand & Luo 2003); falling back to
+ *     linear, then to simple bounce-back, when the stencil leaves the fluid
+ *     or the domain;
  *   - momentum exchange in the Galilean-invariant form of Wen et al. (2014),
  *     on the stored deviations (the rest-state term 2 w_i rho0 c_i, a pure
  *     geometry sum over the surface, is left out);
@@ -731,11 +732,9 @@ static int ibb_pass(const orc_params* p, orc_particles* P, double* F, int nx, in
                                 fn = A + mw;
                             }
                         } else {
-                            if (ok2) {
-                                const double D = F[(size_t)ib + Q * n1], E = F[(size_t)ib + Q * n2];
-                                const double k = 1.0 / (q * (2.0 * q + 1.0));
-                                fn = k * A + (2.0 * q - 1.0) / q * D - (2.0 * q - 1.0) / (2.0 * q + 1.0) * E + k * mw;
-                            } else if (ok1) {
+                            /* linear for q >= 1/2 (the quadratic form's extrapolating third
+                             * coefficient destabilises narrow gaps at s16 = 1.98) */
+                            if (ok1) {
                                 const double D = F[(size_t)ib + Q * n1];
                                 fn = (A + mw) / (2.0 * q) + (2.0 * q - 1.0) / (2.0 * q) * D;
                             } else {
