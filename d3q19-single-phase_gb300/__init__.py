@@ -64,7 +64,7 @@ EXPORTS = (
     "lbm_dissipation",
     "lbm_timing_enable", "lbm_timing_get", "lbm_step_launches", "lbm_strain",
     "lbm_mlp_create", "lbm_mlp_destroy", "lbm_mlp_get", "lbm_mlp_set", "lbm_mlp_set_data", "lbm_mlp_train",
-    "lbm_mlp_gradient", "lbm_mlp_predict", "lbm_les_set", "lbm_les_nut", "lbm_les_training_data",
+    "lbm_mlp_gradient", "lbm_mlp_predict", "lbm_les_set", "lbm_les_wall_damping", "lbm_les_nut", "lbm_les_training_data",
     "lbm_les_features",
 )
 
@@ -164,6 +164,7 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
         "lbm_mlp_gradient": (ctypes.c_int, [ctx, ctypes.c_int32, ctypes.POINTER(ctypes.c_double), fp]),
         "lbm_mlp_predict": (ctypes.c_int, [ctx, fp, ctypes.c_int64, fp]),
         "lbm_les_set": (ctypes.c_int, [ctx, fp, fp, ctypes.c_double, ctypes.c_double]),
+        "lbm_les_wall_damping": (ctypes.c_int, [ctx, ctypes.c_double]),
         "lbm_les_nut": (ctypes.c_int, [ctx, dp]),
         "lbm_les_features": (ctypes.c_int, [ctx, ctypes.c_double, ctypes.c_double, fp]),
         "lbm_les_training_data": (ctypes.c_int, [ctx, ctypes.c_int32, ctypes.c_double, ctypes.c_double, fp, fp, dp]),
@@ -545,6 +546,10 @@ class Lattice:
         n = np.ascontiguousarray(norm, dtype=np.float32).reshape(MLP_NORM)
         self._les = (p, n)
         self._call("lbm_les_set", _fptr(p), _fptr(n), ustar, h)
+
+    def les_wall_damping(self, aplus: float) -> None:
+        """van Driest damping (1 - exp(-y+/A+))^2 of the closure's nu_t (0: off)."""
+        self._call("lbm_les_wall_damping", ctypes.c_double(aplus))
 
     def les_training_data(self, factor: int, ustar: float, h: float):
         """(X[nc][7], y[nc], ubar[3][nxc][nyc][nzc]) of the box-filtered state."""

@@ -662,6 +662,13 @@ int lbm_strain(lbm_ctx* c, double* m1, double* m2) {
     return sync(c);
 }
 
+int lbm_les_wall_damping(lbm_ctx* c, double aplus) {
+    if (check_ctx(c)) return LBM_ERR_INVALID_ARG;
+    if (!(aplus >= 0.0) || !std::isfinite(aplus)) return fail(LBM_ERR_INVALID_ARG, "A+ must be finite and >= 0");
+    c->s.les_aplus = (float)aplus;
+    return LBM_OK;
+}
+
 int lbm_les_set(lbm_ctx* c, const float* params, const float* norm, double ustar, double h) {
     if (check_ctx(c)) return LBM_ERR_INVALID_ARG;
     if (int rc = set_device(c)) return rc;

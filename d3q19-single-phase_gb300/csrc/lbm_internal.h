@@ -117,6 +117,7 @@ struct DeviceState {
     float* les_s9;
     double les_nu;
     float les_ustar, les_h;
+    float les_aplus;     // van Driest damping constant A+ of nu_t (0: off)
 };
 
 // launchers (lbm_step.cu)

@@ -144,7 +144,12 @@ __device__ __forceinline__ void les_collide(R f[Q], const CollideConsts<R>& C, c
     for (int k = 0; k < 6; ++k) Sf[k] = (float)S6[k];
     const float dwall = fminf((float)z + 0.5f, (float)s.g.NZ - (float)z - 0.5f);
     closure_features(Sf, dwall, (float)s.les_nu, s.les_ustar, s.les_h, x);
-    const float r = mlp_infer(Ws, Ws + kMlpParams, x);
+    float r = mlp_infer(Ws, Ws + kMlpParams, x);
+    if (s.les_aplus > 0.f) {
+        // van Driest damping (1 - exp(-y+/A+))^2 of the predicted nu_t
+        const float e = 1.f - expf(-(dwall * s.les_ustar / (float)s.les_nu) / s.les_aplus);
+        r *= e * e;
+    }
     const R s9 = R(1) / (R(3) * (R)s.les_nu * (R(1) + (R)r) + R(0.5));
     s.les_s9[n] = (float)s9;
     CollideConsts<R> cl = C;

@@ -63,7 +63,7 @@ def mean_profile(lat, ustar):
     return pkg.statistics(lat.profiles(), ustar)["mean"][:, 1] * ustar
 
 
-def les_run(params, norm, ub, cfg, steps, sample_every, closure):
+def les_run(params, norm, ub, cfg, steps, sample_every, closure, aplus=0.0):
     """Coarse LES from the filtered velocity ub (reference axes).  Returns
     (time-averaged mean u_stream(x), ms per step, failure step or None,
     mean nu_t/nu profile or None)."""
@@ -79,6 +79,7 @@ def les_run(params, norm, ub, cfg, steps, sample_every, closure):
         lat.initpop(*[np.asfortranarray(u) for u in ub])
         if closure:
             lat.les_set(params, norm, cfg["ustar"], cfg["h"] / cfg["factor"])
+            lat.les_wall_damping(aplus)
         t0 = time.perf_counter()
         done = 0
         while done < steps:
@@ -124,6 +125,8 @@ def main():
                          "held-out explained variance 0.67 at filter 4) or from a coarse lattice seeded "
                          "with the filtered snapshot, the inference path (0.23)")
     ap.add_argument("--fixtures", type=Path, default=None, help="write the held-out test fixtures here")
+    ap.add_argument("--aplus", type=float, default=26.0,
+                    help="also run the closure with van Driest damping of nu_t near the walls (A+; 0: skip)")
     args = ap.parse_args()
     args.out.mkdir(parents=True, exist_ok=True)
     stream, span, wall = args.grid
@@ -229,9 +232,12 @@ def main():
         # ---- coarse LES with and without the closure, same window as the DNS --------
         ref = box_profile(prof_dns, f)
         res = {}
-        for name, closure in (("closure", True), ("plain_mrt", False)):
+        variants = [("closure", True, 0.0), ("plain_mrt", False, 0.0)]
+        if args.aplus > 0:
+            variants.insert(1, ("closure_wall_damped", True, args.aplus))
+        for name, closure, aplus in variants:
             p_les, ms, fail, nut = les_run(params, norm, ub0[f], cfg, args.window // f, max(sample_fine // f, 1),
-                                           closure)
+                                           closure, aplus)
             err = None if p_les is None else float(np.abs(p_les - ref).max() / np.abs(ref).max())
             res[name] = {"mean_profile_rel_err": err, "ms_per_step": ms, "failed_at_step": fail,
                          "profile": None if p_les is None else p_les.tolist(),

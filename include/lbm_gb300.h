@@ -400,6 +400,12 @@ int lbm_mlp_predict(lbm_mlp* m, const float* X, int64_t n, float* out);
  * 1/2).  params == NULL turns it off.  FP32/FP64 storage, particle-free
  * channels; steps use the one-node-per-thread kernels while it is on. */
 int lbm_les_set(lbm_ctx* ctx, const float* params, const float* norm, double ustar, double h);
+/* Near-wall damping of the closure's eddy viscosity (no counterpart in the
+ * reference, whose LES has no closure): nu_t is multiplied by
+ * (1 - exp(-y+/A+))^2, y+ = d u* / nu with d the cell centre's wall distance
+ * (van Driest 1956; A+ = 26 is the classical constant).  aplus = 0 (the
+ * default) turns it off. */
+int lbm_les_wall_damping(lbm_ctx* ctx, double aplus);
 /* nu_t / nu of the last collision per node (host, nx*ny*nz doubles, reference
  * layout). */
 int lbm_les_nut(lbm_ctx* ctx, double* nut);

@@ -499,7 +499,8 @@ def closure_features(S, dwall, nu, ustar, h):
 OPP = np.array([int(np.flatnonzero((CX == -CX[i]) & (CY == -CY[i]) & (CZ == -CZ[i]))[0]) for i in range(Q)])
 
 
-def les_step(p: OrcParams, f: np.ndarray, s9prev: np.ndarray, params, norm, ustar: float, h: float):
+def les_step(p: OrcParams, f: np.ndarray, s9prev: np.ndarray, params, norm, ustar: float, h: float,
+             aplus: float = 0.0):
     """One coarse-LES step with the closure, FP64: per node the strain from the
     non-equilibrium moments with s9prev, the features and the network give
     s9 = s13 = 1/(3 nu (1 + nu_t/nu) + 1/2); collide_node with those rates;
@@ -511,6 +512,9 @@ def les_step(p: OrcParams, f: np.ndarray, s9prev: np.ndarray, params, norm, usta
     dwall = np.minimum(np.arange(nx) + 0.5, nx - np.arange(nx) - 0.5)[:, None, None]
     X = closure_features(S, dwall, nu, ustar, h).reshape(-1, 7)
     r, _ = mlp_forward(params, norm, X)
+    if aplus > 0.0:                      # van Driest damping of nu_t
+        yp = np.broadcast_to(dwall * ustar / nu, (nx, ny, nz)).reshape(-1)
+        r = r * (1.0 - np.exp(-yp / aplus)) ** 2
     s9 = (1.0 / (3.0 * nu * (1.0 + r) + 0.5)).reshape(nx, ny, nz)
     rho, ux, uy, uz = macrovar(p, f)
     post = np.empty_like(f)

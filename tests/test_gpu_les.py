@@ -165,26 +165,32 @@ def les_case(pkg, orc, shape=(10, 12, 8), precision="fp64"):
     return run, p, f0
 
 
-def test_les_closure_steps_match_oracle(pkg, orc):
+@pytest.mark.parametrize("aplus", [0.0, 26.0])
+def test_les_closure_steps_match_oracle(pkg, orc, aplus):
     """Two steps (both AA parities) of the coarse LES with the closure fused
     into the collision: populations and nu_t against the FP64 oracle (the GPU
-    evaluates features and network in FP32)."""
+    evaluates features and network in FP32), without and with the van Driest
+    damping of nu_t near the walls."""
     run, p, f0 = les_case(pkg, orc)
     params, norm = closure_net(orc)
     ustar, h = 0.005, 5.0
     s9 = np.full(f0.shape[1:], p.s9)
     fo = f0
     for _ in range(2):
-        fo, s9 = orc.les_step(p, fo, s9, params.astype(np.float64), norm.astype(np.float64), ustar, h)
+        fo, s9 = orc.les_step(p, fo, s9, params.astype(np.float64), norm.astype(np.float64), ustar, h, aplus)
     nu = (1.0 / p.s9 - 0.5) / 3.0
     nut_o = (1.0 / s9 - 0.5) / 3.0 / nu - 1.0
     with pkg.Lattice(run) as lat:
         lat.upload_f(f0)
         lat.les_set(params, norm, ustar, h)
+        lat.les_wall_damping(aplus)
         lat.step(2)
         g = lat.download_f()
         nut = lat.les_nut()
-    assert nut_o.min() > 0.1                          # the closure acts
+    if aplus == 0.0:
+        assert nut_o.min() > 0.1                      # the closure acts
+    else:                                             # damped most in the wall cells
+        assert nut_o[0].mean() < nut_o[nut_o.shape[0] // 2].mean()
     assert rel(nut, nut_o) < 1e-4
     assert rel(g - f0, fo - f0) < 1e-5
 
