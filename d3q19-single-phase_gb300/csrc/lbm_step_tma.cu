@@ -184,11 +184,12 @@ __device__ __forceinline__ const T* src_row(const PopPtrs<T>& P, const Geometry&
 }
 // Issued by one warp: lane i moves population i's row.  The mbarrier learns the
 // byte count from lane 0 before any copy is issued.
-// `issued` counts the loads ever issued into this stage (for the drain on
-// abort).
+// `issued` (a register of the issuing warp) records the loads this warp put
+// into stage s for the drain on abort: bit s flips per load (the count's
+// parity), bit 8 + s is set once one was issued.
 template <typename T, bool ODD>
 __device__ __forceinline__ void issue_item(const PopPtrs<T>& P, const Geometry& g, uint32_t it, uint32_t stage_smem,
-                                           uint32_t bar, uint32_t row_bytes, int lane, unsigned* issued,
+                                           uint32_t bar, uint32_t row_bytes, int lane, int s, unsigned& issued,
                                            unsigned* bflag) {
     if (lane == 0) mbar_expect_tx(bar, (uint32_t)Q * row_bytes);
     __syncwarp();
@@ -197,7 +198,7 @@ __device__ __forceinline__ void issue_item(const PopPtrs<T>& P, const Geometry& 
         bulk_load(stage_smem + (uint32_t)lane * row_bytes,
                   src_row<T, ODD>(P, g, I, wall_of(g, I.z), lane, bflag, 301), row_bytes, bar);
     }
-    if (lane == 0) ++*issued;          // off the refill's critical path: read only by the drain
+    issued = (issued ^ (1u << s)) | (1u << (8 + s));
 }
 
 // Two adjacent nodes (x, x+1), x even, of one item; the results go back into
@@ -277,7 +278,7 @@ __global__ void __launch_bounds__(NT, 512 / NT)
 k_step_rows(PopPtrs<T> P, CollideConsts<float> C, Geometry g, int nstage, int* err) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ unsigned int done_count[kMaxStages];
-    __shared__ unsigned int issued[kMaxStages];
+    __shared__ unsigned int issued_par, issued_any;
     __shared__ volatile int abort_flag;
     const uint32_t row_bytes = (uint32_t)g.NX * sizeof(T);
     const uint32_t stage_bytes = (uint32_t)Q * row_bytes;
@@ -291,14 +292,15 @@ k_step_rows(PopPtrs<T> P, CollideConsts<float> C, Geometry g, int nstage, int* e
     const unsigned nwarps = NT / 32;
     unsigned* const bflag = reinterpret_cast<unsigned*>(err + 1);   // bounds-check site (checked build)
     (void)bflag;
+    unsigned issued = 0;                                   // loads this warp issued, per stage
 
     if (tid == 0) {
         for (int s = 0; s < nstage; ++s) {
             mbar_init(bars + 8 * s, 1);
             done_count[s] = 0;
-            issued[s] = 0;
         }
         abort_flag = 0;
+        issued_par = issued_any = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
@@ -306,7 +308,7 @@ k_step_rows(PopPtrs<T> P, CollideConsts<float> C, Geometry g, int nstage, int* e
         for (int s = 0; s < nstage; ++s) {
             const uint32_t it = blockIdx.x + (uint32_t)s * G;
             if (it < total)
-                issue_item<T, ODD>(P, g, it, data + s * stage_bytes, bars + 8 * s, row_bytes, lane, &issued[s],
+                issue_item<T, ODD>(P, g, it, data + s * stage_bytes, bars + 8 * s, row_bytes, lane, s, issued,
                                    bflag);
         }
     }
@@ -352,17 +354,22 @@ k_step_rows(PopPtrs<T> P, CollideConsts<float> C, Geometry g, int nstage, int* e
             store_item<T, ODD>(P, g, it, data + s * stage_bytes, row_bytes, lane, bflag);
             const uint32_t nit = blockIdx.x + (k + (uint32_t)nstage) * G;
             if (nit < total && !ab)
-                issue_item<T, ODD>(P, g, nit, data + s * stage_bytes, bars + 8 * s, row_bytes, lane, &issued[s],
+                issue_item<T, ODD>(P, g, nit, data + s * stage_bytes, bars + 8 * s, row_bytes, lane, s, issued,
                                    bflag);
         }
     }
     bulk_wait_all();
+    if (lane == 0 && issued) {          // unconditionally: an abort may come later
+        atomicXor(&issued_par, issued & 0xffu);
+        atomicOr(&issued_any, issued >> 8);
+    }
     __syncthreads();
     if (abort_flag && tid == 0) {
-        // drain: the latest load into each stage completes the phase with
-        // parity (issued - 1) & 1; earlier phases have completed before it
+        // drain: with n loads issued into a stage in all, the latest completes
+        // the phase with parity (n - 1) & 1; earlier phases have completed
+        // before it (a stage is refilled only after every warp consumed it)
         for (int s = 0; s < nstage; ++s)
-            if (issued[s] > 0) (void)mbar_wait(bars + 8 * s, (issued[s] - 1u) & 1u);
+            if ((issued_any >> s) & 1u) (void)mbar_wait(bars + 8 * s, ((issued_par >> s) & 1u) ^ 1u);
         atomicExch(err, 1);
     }
 }
