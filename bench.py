@@ -92,9 +92,13 @@ def committed_traffic(workload: str) -> dict | None:
     if out.get("workload") != workload:
         return None
     try:
-        return {k: float(out[k]) for k in ("even_bytes", "odd_bytes")}
+        res = {k: float(out[k]) for k in ("even_bytes", "odd_bytes")}
     except (KeyError, ValueError):
         return None
+    if "measured_on" in out:
+        res["basis"] = (f"ncu dram__bytes of {out['measured_on']}, x {out.get('scale', '?')} "
+                        "(profiles/dram_traffic.txt)")
+    return res
 
 
 class ClockSampler:
@@ -349,6 +353,7 @@ def run_gpu(args, world, rank, local):
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "frac": round(achieved / peaks["hbm_gbs"], 4),
             "traffic": (round((traffic["even_bytes"] + traffic["odd_bytes"]) / 2) if traffic else None),
+            "traffic_basis": traffic.get("basis") if traffic else None,
             "peak_source": f"{peaks['source']} (MEASURED_PEAKS.json hbm_gbs)",
             "kernel": ("k_step_rows" if prec != "fp64" and not args.simple else "k_step_even/odd")
                       + " (even/odd AA launches alternate)",
