@@ -330,6 +330,30 @@ def test_row_pipelined_kernels_match_simple_kernels(pkg, orc, prec, shape):
     assert rel_linf(out[0][-1], fo) < (1e-5 if prec == "fp32" else 5e-3)
 
 
+@pytest.mark.parametrize("prec", ["fp32", "fp16"])
+def test_row_kernels_production_rows_match_oracle(pkg, orc, prec):
+    """Rows of 1024 streamwise nodes, as in the large channel (FP16: two CTAs
+    of 256 threads per SM with two stages each; FP32: one CTA of 512 threads),
+    on a 1.6 M-node channel from the seeded Poiseuille start: 10 steps against
+    the FP64 oracle (its OpenMP push), within the storage precision."""
+    shape = (32, 1024, 48)                      # wall-normal, streamwise, spanwise
+    run = stable_run(pkg, shape, force_y=2e-6, precision=prec)
+    u = orc.channel_velocity(*shape, 0.05, 0.05, 31)
+    f0 = orc.initpop(*u)
+    p64 = orc.params_from(stable_run(pkg, shape, force_y=2e-6))
+    fo = orc.run_omp(p64, f0.copy(order="F"), 10, orc.max_threads())    # fused two-lattice push, OpenMP
+    _, _, uy_o, _ = orc.macrovar(p64, fo)
+    with pkg.Lattice(run) as lat:
+        lat.upload_f(f0)
+        lat.step(10)
+        g = lat.download_f()
+        rho, ux, uy, uz = lat.macrovar()
+    tol = 1e-5 if prec == "fp32" else 5e-3
+    assert rel_linf(g, fo) < tol
+    assert rel_linf(uy, uy_o) < tol
+    assert abs(float(g.sum() - fo.sum())) < tol * np.abs(fo).sum()
+
+
 def test_row_kernels_full_size_config4_properties(pkg):
     """1024 x 512 x 512 FP16 store (the large channel): no NaN, mass drift and
     mean profile against the one-node-per-thread kernels after 20 steps."""
