@@ -525,8 +525,13 @@ class Lattice:
         self._call("lbm_device_bytes", ctypes.byref(n))
         return n.value
 
-    def prerelax(self, ux, uy, uz, eps: float = 1e-5, maxit: int = 15000) -> tuple[int, float]:
-        a, b, c = (self._field(v, n) for v, n in ((ux, "ux"), (uy, "uy"), (uz, "uz")))
+    def prerelax(self, ux=None, uy=None, uz=None, eps: float = 1e-5, maxit: int = 15000) -> tuple[int, float]:
+        """main.f90:69-90 with the velocity frozen at (ux, uy, uz), or, all
+        None, at the velocity of the current populations (device only)."""
+        if ux is None and uy is None and uz is None:
+            a = b = c = None
+        else:
+            a, b, c = (self._field(v, n) for v, n in ((ux, "ux"), (uy, "uy"), (uz, "uz")))
         it = ctypes.c_int32()
         err = ctypes.c_double()
         self._call("lbm_prerelax", _dptr(a), _dptr(b), _dptr(c), eps, maxit, ctypes.byref(it), ctypes.byref(err))

@@ -584,7 +584,8 @@ int lbm_set_step_count(lbm_ctx* c, int64_t n) {
 
 int lbm_prerelax(lbm_ctx* c, const double* ux, const double* uy, const double* uz, double eps,
                  int32_t maxit, int32_t* iters, double* err) {
-    if (check_ctx(c) || !ux || !uy || !uz) return fail(LBM_ERR_INVALID_ARG, "null argument");
+    const bool from_f = !ux && !uy && !uz;      // frozen velocity from the current populations
+    if (check_ctx(c) || (!from_f && (!ux || !uy || !uz))) return fail(LBM_ERR_INVALID_ARG, "null argument");
     if (!(eps >= 0.0) || maxit < 0) return fail(LBM_ERR_INVALID_ARG, "bad eps or maxit");
     if (int rc = set_device(c)) return rc;
     const size_t N = c->s.N;
@@ -593,7 +594,8 @@ int lbm_prerelax(lbm_ctx* c, const double* ux, const double* uy, const double* u
     if (!c->d_max) CK(cudaMalloc(&c->d_max, sizeof(unsigned long long)));
     const int k = chunk_planes(c, 3);
     const size_t pp = plane_nodes(c->p);
-    for (int z0 = 0; z0 < c->p.nz; z0 += k) {
+    if (from_f) CK(launch_uf_from_f(c->s, c->parity, c->d_uf, c->stream));
+    for (int z0 = 0; !from_f && z0 < c->p.nz; z0 += k) {
         const int nzc = std::min(k, c->p.nz - z0);
         const size_t n = (size_t)nzc * pp;
         double* du = c->d_stage;

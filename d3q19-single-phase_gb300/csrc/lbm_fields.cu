@@ -527,6 +527,28 @@ __global__ void k_ref_to_gpu_vec(Geometry g, size_t N, const double* __restrict_
     uf[n] = ux[src]; uf[N + n] = uy[src]; uf[2 * N + n] = uz[src];
 }
 
+// Frozen velocity of the pre-relaxation from the populations themselves:
+// sum_i c_i f_i of the natural populations (GPU layout, 3 planes of N).  For
+// a state that initpop's equilibrium at delta-rho = 0 produced, this is the
+// velocity it was built from (sum_i w_i c_i c_i = I/3, the other terms are
+// odd in c), to rounding.
+template <typename T>
+__global__ void k_uf_from_f(DeviceState s, int parity, double* __restrict__ uf) {
+    const RefNode r = ref_node(s.g, 0);
+    if (!r.ok) return;
+    double f[Q];
+    gather_natural<T>(s, parity, r.iy, r.iz, r.ix, f);
+    double a = 0.0, b = 0.0, c = 0.0;
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        if (CXf(i)) a += CXf(i) * f[i];
+        if (CYf(i)) b += CYf(i) * f[i];
+        if (CZf(i)) c += CZf(i) * f[i];
+    }
+    const uint32_t n = gpu_lin(s.g, r.ix, r.iy, r.iz);
+    uf[n] = a; uf[s.N + n] = b; uf[2 * s.N + n] = c;
+}
+
 constexpr int kRedThreads = 256;
 
 // Plane sums for statistc2: block (b, Z) covers part of plane Z (ref x = Z+1).
@@ -1016,6 +1038,10 @@ cudaError_t launch_closure_targets(const double* F9, int nxc, int nyc, int nzc, 
 cudaError_t launch_les_features(const DeviceState& s, int parity, float ustar, float h, float* X,
                                 cudaStream_t st) {
     LBM_DISPATCH(s.prec, (k_les_features<T><<<ref_grid(s.g, s.g.NY, kBx), kBx, 0, st>>>(s, parity, ustar, h, X, 0)))
+}
+
+cudaError_t launch_uf_from_f(const DeviceState& s, int parity, double* uf, cudaStream_t st) {
+    LBM_DISPATCH(s.prec, (k_uf_from_f<T><<<ref_grid(s.g, s.g.NY, kBx), kBx, 0, st>>>(s, parity, uf)))
 }
 
 cudaError_t launch_ref_to_gpu_vec(const DeviceState& s, const double* ux, const double* uy,

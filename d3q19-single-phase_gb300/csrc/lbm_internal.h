@@ -164,6 +164,8 @@ cudaError_t launch_les_features(const DeviceState& s, int parity, float ustar, f
 // then applied
 cudaError_t launch_remove_mean_density(const DeviceState& s, int parity, double* acc, cudaStream_t st);
 cudaError_t launch_remove_mean_apply(const DeviceState& s, const double* acc, cudaStream_t st);
+// pre-relaxation's frozen velocity from the current natural populations
+cudaError_t launch_uf_from_f(const DeviceState& s, int parity, double* uf, cudaStream_t st);
 cudaError_t launch_ref_to_gpu_vec(const DeviceState& s, const double* ux,
                                   const double* uy, const double* uz,
                                   double* uf, int z0, int nzc, cudaStream_t st);

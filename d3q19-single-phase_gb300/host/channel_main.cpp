@@ -198,17 +198,11 @@ int main(int argc, char** argv) {
             return 1;
         }
         if (argi("prerelax", 0)) {
-            if (u.empty()) {
-                u.resize(n); v.resize(n); w.resize(n);
-                if (ivel == "loglaw")
-                    check(lbm_loglaw_velocity(nx, ny, nz, ustar, visc / ustar, a9, u.data(), v.data(), w.data()),
-                          "initvel");
-                else
-                    check(lbm_channel_velocity(nx, ny, nz, uc, amp, seed, u.data(), v.data(), w.data()), "initvel");
-            }
+            // the velocity stays frozen at the initial condition's, which the
+            // library reads back from the populations (no host sweep)
             int32_t it = 0;
             double err = 0;
-            const int rc = lbm_prerelax(ctx, u.data(), v.data(), w.data(), 1e-5, 15000, &it, &err);
+            const int rc = lbm_prerelax(ctx, nullptr, nullptr, nullptr, 1e-5, 15000, &it, &err);
             if (rc != LBM_OK && rc != LBM_ERR_NOT_CONVERGED) check(rc, "prerelax");
             std::printf(" final relaxation => %d %.6E\n", it, err);
             int32_t istat = 0;

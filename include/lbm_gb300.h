@@ -218,7 +218,11 @@ int lbm_set_step_count(lbm_ctx* ctx, int64_t nsteps);
  * (ux,uy,uz) (arrays (nx,ny,nz)): repeat {rho = sum f (rhoupdat);
  * collision with the frozen velocity} until max|rho - rho_prev| <= eps or the
  * iteration counter exceeds maxit.  iters/err receive the final counter and
- * residual.  Returns LBM_ERR_NOT_CONVERGED only if maxit was exceeded. */
+ * residual.  Returns LBM_ERR_NOT_CONVERGED only if maxit was exceeded.
+ * ux = uy = uz = NULL freezes the velocity of the current populations
+ * instead (sum_i c_i f_i, which is the initial velocity itself right after
+ * lbm_initpop, lbm_init_channel or lbm_init_loglaw), so a device initial
+ * condition needs no host velocity arrays. */
 int lbm_prerelax(lbm_ctx* ctx, const double* ux, const double* uy,
                  const double* uz, double eps, int32_t maxit, int32_t* iters,
                  double* err);

@@ -166,6 +166,27 @@ def test_prerelax_matches_oracle(pkg, orc):
         assert rel_linf(lat.download_f(), fo) < 1e-12
 
 
+def test_prerelax_with_velocity_from_the_populations(pkg, orc):
+    """Pre-relaxation with the frozen velocity read back from the populations
+    (no host arrays) equals the one given initvel's host arrays: the log-law
+    start with a density disturbance in the rest population (which carries no
+    momentum), same iteration count, populations to rounding."""
+    shape = (12, 16, 8)
+    run = stable_run(pkg, shape)
+    ustar = 0.0035
+    u = orc.loglaw_velocity(*shape, ustar, 0.0012 / ustar, 1.5)
+    f = orc.initpop(*u)
+    f[0] += 1e-3 * np.random.default_rng(4).standard_normal(f.shape[1:])
+    out = []
+    for host in (True, False):
+        with pkg.Lattice(run) as lat:
+            lat.upload_f(f)
+            it, err = lat.prerelax(*(u if host else (None, None, None)), eps=1e-8, maxit=5000)
+            out.append((it, err, lat.download_f()))
+    assert out[0][0] == out[1][0] and out[0][0] > 1
+    assert rel_linf(out[1][2], out[0][2]) < 1e-12
+
+
 def test_prerelax_limit_reports_not_converged(pkg, orc):
     shape = (4, 8, 4)
     run = stable_run(pkg, shape)
