@@ -110,6 +110,11 @@ def test_loglaw_velocity_rejects_bad_arguments(lib):
     assert lib.lbm_init_loglaw(None, ctypes.c_double(0.1), ctypes.c_double(1.0), ctypes.c_double(0.0)) == -1
 
 
+def test_les_wall_damping_rejects_bad_arguments(lib):
+    assert lib.lbm_les_wall_damping(None, ctypes.c_double(26.0)) == -1
+    assert lib.lbm_prerelax(None, None, None, None, ctypes.c_double(1e-5), 10, None, None) == -1
+
+
 def test_oracle_sphere_placement_matches_library(pkg, orc):
     """The oracle restates the seeded placement (its plain all-pairs overlap
     scan against the library's cell list): the same centres bit for bit, so
