@@ -10,7 +10,9 @@
 // tensor cores through mma.sync m16n8k16 with BF16 operands rounded from the
 // FP32 values and FP32 accumulation; an FP32 FMA path of the same structure
 // serves the gradient checks.  The products are 128x32x32 tiles, so a training
-// step is bound by launch latency and the atomics, not by the tensor-core rate.
+// step is bound by the latency of a tile's chain of stages (two waves of 512
+// tiles at two CTAs per SM), not by the tensor-core rate; the gradient atomics
+// take about 3% of it (measured against a copy without them).
 //
 // Loss: mean squared error of nu_t / nu against the targets.
 #include <cuda_bf16.h>

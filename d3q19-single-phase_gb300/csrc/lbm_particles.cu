@@ -363,14 +363,30 @@ struct IbbBox {
     float R2f;                    // R^2 in FP32
 };
 
-// A link between its gathers and its finish: geometry, wall velocity and the
-// populations read.
+// A link between its gathers and its finish: its packed coordinates (with
+// the partner flags), q, the populations read and the address of the
+// returning population.  The finish recomputes the rest of the geometry from
+// (a, b, c, i) and q, so a lane can keep several links in flight.
 template <typename T, typename RT>
 struct IbbLink {
-    RT q, x0, x1, x2, fcx, fcy, fcz, uw0, uw1, uw2, mw, A, X, Y;
+    uint32_t v;                   // a | b << 8 | c << 16 | i << 24 | ok1 << 29 | ok2 << 30
+    RT q, A, X, Y;
     T* w;                         // storage of the returning population
-    bool ok1, ok2;
 };
+constexpr uint32_t kOk1 = 1u << 29, kOk2 = 1u << 30;
+
+// Offset from the sphere's centre to the fluid node of staged coordinates
+// (a, b, c): FP64 from the position for FP64 storage, the staged FP32 table
+// otherwise.
+template <typename RT, typename W>
+__device__ __forceinline__ void ibb_offset(const DeviceParticles& P, const Geometry& g, int p, const IbbBox<W>& B,
+                                           int a, int b, int c, RT d[3]) {
+    if constexpr (sizeof(RT) == 8) {
+        offset(P, g, p, B.xlo + c, B.wA[a], B.wZ[b], d);
+    } else {
+        d[0] = B.tC[c]; d[1] = B.tA[a]; d[2] = B.tB[b];
+    }
+}
 
 // Gathers of one link: entry (a, b, c, i) = staged coordinates of the fluid
 // node and the direction.  X and Y are the interpolation partners: (B, C) at
@@ -379,7 +395,7 @@ struct IbbLink {
 // read).
 template <typename T, typename RT, typename W, bool Q64>
 __device__ __forceinline__ IbbLink<T, RT> ibb_gather(const DeviceState& s, const DeviceParticles& P, int p,
-                                                     int parity, const IbbBox<W>& B, uint32_t v, const RT (&UW)[6]) {
+                                                     int parity, const IbbBox<W>& B, uint32_t v) {
     IbbLink<T, RT> L;
     const int a = v & 255, b = (v >> 8) & 255, c = (v >> 16) & 255, i = (int)(v >> 24);
     const IbbDir D = B.dir[i];
@@ -387,75 +403,55 @@ __device__ __forceinline__ IbbLink<T, RT> ibb_gather(const DeviceState& s, const
     const int ib = D.packed >> 8;
     const int dr = cz + B.S * cx;                      // row offset of c_i
     const int r0 = b + B.S * c;
+    L.v = v;
+    L.q = RT(1); L.A = L.X = L.Y = RT(0);
+    L.w = nullptr;
     // the staged box holds every node the link touches: rows r0 - 2dr ..
     // r0 + dr and streamwise positions a - 2cy .. a + cy
     if (!LBM_IN_BOUNDS(s.bounds, i >= 1 && i < Q && a >= 2 && a + 2 < B.S && b >= 2 && b + 2 < B.S && c >= 2 &&
-                                     c + 2 < B.S, 221)) {
-        L.ok1 = L.ok2 = false;
-        L.q = RT(1); L.A = L.X = L.Y = RT(0); L.mw = RT(0);
-        L.x0 = L.x1 = L.x2 = L.fcx = L.fcy = L.fcz = L.uw0 = L.uw1 = L.uw2 = RT(0);
-        L.w = nullptr;
+                                     c + 2 < B.S, 221))
         return L;
-    }
-    L.ok1 = (B.fluid[r0 - dr] >> (a - cy)) & 1;
-    L.ok2 = L.ok1 && ((B.fluid[r0 - 2 * dr] >> (a - 2 * cy)) & 1);
+    bool ok1 = (B.fluid[r0 - dr] >> (a - cy)) & 1;
+    bool ok2 = ok1 && ((B.fluid[r0 - 2 * dr] >> (a - 2 * cy)) & 1);
     const uint32_t gx = (uint32_t)(B.wA[a] + B.rowIdx[r0]);
     const uint32_t gs = (uint32_t)(B.wA[a + cy] + B.rowIdx[r0 + dr]);
     uint32_t ga = 0, gb = 0;
-    if (L.ok1) ga = (uint32_t)(B.wA[a - cy] + B.rowIdx[r0 - dr]);
-    if (L.ok2) gb = (uint32_t)(B.wA[a - 2 * cy] + B.rowIdx[r0 - 2 * dr]);
-    if (!LBM_IN_BOUNDS(s.bounds, gx < s.N && gs < s.N && ga < s.N && gb < s.N, 222)) {
-        L.ok1 = L.ok2 = false;
-        L.q = RT(1); L.A = L.X = L.Y = RT(0); L.mw = RT(0);
-        L.x0 = L.x1 = L.x2 = L.fcx = L.fcy = L.fcz = L.uw0 = L.uw1 = L.uw2 = RT(0);
-        L.w = nullptr;
+    if (ok1) ga = (uint32_t)(B.wA[a - cy] + B.rowIdx[r0 - dr]);
+    if (ok2) gb = (uint32_t)(B.wA[a - 2 * cy] + B.rowIdx[r0 - 2 * dr]);
+    if (!LBM_IN_BOUNDS(s.bounds, gx < s.N && gs < s.N && ga < s.N && gb < s.N, 222))
         return L;
-    }
     const T* Pi = plane<T>(s, i);
     const T* Pib = plane<T>(s, ib);
-    RT d0, d1, d2;
     if constexpr (sizeof(RT) == 8) {
         double dd[3];
-        offset(P, s.g, p, B.xlo + c, B.wA[a], B.wZ[b], dd);
+        ibb_offset<RT, W>(P, s.g, p, B, a, b, c, dd);
         L.q = link_q<double>(dd, cx, cy, cz, __dsub_rn(norm2_rn(dd), __dmul_rn(P.R, P.R)));
-        d0 = dd[0]; d1 = dd[1]; d2 = dd[2];
-        L.fcx = cx; L.fcy = cy; L.fcz = cz;
+    } else if constexpr (Q64) {
+        double dd[3];
+        offset(P, s.g, p, B.xlo + c, B.wA[a], B.wZ[b], dd);
+        L.q = (float)link_q<double>(dd, cx, cy, cz, __dsub_rn(norm2_rn(dd), __dmul_rn(P.R, P.R)));
     } else {
-        L.fcx = D.fcx; L.fcy = D.fcy; L.fcz = D.fcz;
-        d0 = B.tC[c]; d1 = B.tA[a]; d2 = B.tB[b];
-        if constexpr (Q64) {
-            double dd[3];
-            offset(P, s.g, p, B.xlo + c, B.wA[a], B.wZ[b], dd);
-            L.q = (float)link_q<double>(dd, cx, cy, cz, __dsub_rn(norm2_rn(dd), __dmul_rn(P.R, P.R)));
-        } else {
-            const float qc = d0 * d0 + d1 * d1 + d2 * d2 - B.R2f;
-            const float qb = d0 * L.fcx + d1 * L.fcy + d2 * L.fcz;
-            const float disc = qb * qb - qc * D.qa;
-            const float sq = disc > 0.f ? disc * rsqrtf(disc) : 0.f;
-            float q = (-qb - sq) * D.inv_qa;
-            L.q = q < 1e-6f ? 1e-6f : (q > 1.f ? 1.f : q);
-        }
+        const float d0 = B.tC[c], d1 = B.tA[a], d2 = B.tB[b];
+        const float qc = d0 * d0 + d1 * d1 + d2 * d2 - B.R2f;
+        const float qb = d0 * D.fcx + d1 * D.fcy + d2 * D.fcz;
+        const float disc = qb * qb - qc * D.qa;
+        const float sq = disc > 0.f ? disc * rsqrtf(disc) : 0.f;
+        float q = (-qb - sq) * D.inv_qa;
+        L.q = q < 1e-6f ? 1e-6f : (q > 1.f ? 1.f : q);
     }
-    L.x0 = d0 + L.q * L.fcx; L.x1 = d1 + L.q * L.fcy; L.x2 = d2 + L.q * L.fcz;
-    L.uw0 = UW[0] + (UW[4] * L.x2 - UW[5] * L.x1);
-    L.uw1 = UW[1] + (UW[5] * L.x0 - UW[3] * L.x2);
-    L.uw2 = UW[2] + (UW[3] * L.x1 - UW[4] * L.x0);
-    RT mw6;
-    if constexpr (sizeof(RT) == 8) mw6 = -6.0 * (i <= 6 ? W1 : W2);
-    else mw6 = D.mw6;
-    L.mw = mw6 * ((L.fcx * L.uw0 + L.fcy * L.uw1) + L.fcz * L.uw2);
     const bool near = L.q < RT(0.5);
     // q >= 1/2 takes the linear form: Bouzidi's quadratic q >= 1/2 form
     // extrapolates (coefficient -(2q-1)/(2q+1) on the second partner) and at
     // tau ~ 0.507 with MRTtype 1's s16 = 1.98 it drives a growing mode in
     // narrow gaps between spheres
-    if (!near) L.ok2 = false;
+    if (!near) ok2 = false;
     const T* pX = near ? (parity ? Pib + ga : Pi + gx) : (parity ? Pi + gx : Pib + ga);
     const T* pY = near ? (parity ? Pib + gb : Pi + ga) : (parity ? Pi + ga : Pib + gb);
     L.w = const_cast<T*>(parity ? Pi + gs : Pib + gx);
     L.A = pop_r<T, RT>(s, parity ? Pib + gx : Pi + gs);
-    L.X = L.ok1 ? pop_r<T, RT>(s, pX) : RT(0);
-    L.Y = L.ok2 ? pop_r<T, RT>(s, pY) : RT(0);
+    L.X = ok1 ? pop_r<T, RT>(s, pX) : RT(0);
+    L.Y = ok2 ? pop_r<T, RT>(s, pY) : RT(0);
+    L.v = v | (ok1 ? kOk1 : 0u) | (ok2 ? kOk2 : 0u);
     return L;
 }
 
@@ -492,17 +488,41 @@ struct ForceAcc<float> {
 };
 
 // Interpolation, the returning population and the exchanged momentum and its
-// moment (added to acc).
-template <typename T, typename RT>
-__device__ __forceinline__ void ibb_finish(const DeviceState& s, const IbbLink<T, RT>& L, ForceAcc<RT>& acc) {
-    const RT q = L.q, A = L.A, mw = L.mw;
+// moment (added to acc).  The wall point x_f + q c_i, its velocity and the
+// moving-wall term come from the link's coordinates and q.
+template <typename T, typename RT, typename W>
+__device__ __forceinline__ void ibb_finish(const DeviceState& s, const DeviceParticles& P, int p,
+                                           const IbbBox<W>& B, const IbbLink<T, RT>& L, const RT (&UW)[6],
+                                           ForceAcc<RT>& acc) {
+#ifdef LBM_BOUNDS_CHECK
+    if (L.w == nullptr) return;                        // a skipped (out-of-bounds) link
+#endif
+    const int a = L.v & 255, b = (L.v >> 8) & 255, c = (L.v >> 16) & 255, i = (int)((L.v >> 24) & 31u);
+    const bool ok1 = (L.v & kOk1) != 0, ok2 = (L.v & kOk2) != 0;
+    const IbbDir D = B.dir[i];
+    RT fcx, fcy, fcz, mw6;
+    if constexpr (sizeof(RT) == 8) {
+        fcx = (D.packed & 3) - 1; fcy = ((D.packed >> 2) & 3) - 1; fcz = ((D.packed >> 4) & 3) - 1;
+        mw6 = -6.0 * (i <= 6 ? W1 : W2);
+    } else {
+        fcx = D.fcx; fcy = D.fcy; fcz = D.fcz;
+        mw6 = D.mw6;
+    }
+    RT d[3];
+    ibb_offset<RT, W>(P, s.g, p, B, a, b, c, d);
+    const RT q = L.q, A = L.A;
+    const RT x0 = d[0] + q * fcx, x1 = d[1] + q * fcy, x2 = d[2] + q * fcz;
+    const RT uw0 = UW[0] + (UW[4] * x2 - UW[5] * x1);
+    const RT uw1 = UW[1] + (UW[5] * x0 - UW[3] * x2);
+    const RT uw2 = UW[2] + (UW[3] * x1 - UW[4] * x0);
+    const RT mw = mw6 * ((fcx * uw0 + fcy * uw1) + fcz * uw2);
     RT fn;
     if (q < RT(0.5)) {
-        if (L.ok2) fn = q * (RT(1) + RT(2) * q) * A + (RT(1) - RT(4) * q * q) * L.X + q * (RT(2) * q - RT(1)) * L.Y + mw;
-        else if (L.ok1) fn = RT(2) * q * A + (RT(1) - RT(2) * q) * L.X + mw;
+        if (ok2) fn = q * (RT(1) + RT(2) * q) * A + (RT(1) - RT(4) * q * q) * L.X + q * (RT(2) * q - RT(1)) * L.Y + mw;
+        else if (ok1) fn = RT(2) * q * A + (RT(1) - RT(2) * q) * L.X + mw;
         else fn = A + mw;
     } else {
-        if (L.ok1) {
+        if (ok1) {
             if constexpr (sizeof(RT) == 8) {
                 fn = (A + mw) / (RT(2) * q) + (RT(2) * q - RT(1)) / (RT(2) * q) * L.X;
             } else {
@@ -513,41 +533,36 @@ __device__ __forceinline__ void ibb_finish(const DeviceState& s, const IbbLink<T
             fn = A + mw;
         }
     }
-#ifdef LBM_BOUNDS_CHECK
-    if (L.w == nullptr) return;                        // a skipped (out-of-bounds) link
-#endif
     put_r<T, RT>(s, L.w, fn);
     // Galilean-invariant momentum exchange
     const RT sA = A + fn, dA = fn - A;
-    const RT p0 = L.fcx * sA + L.uw0 * dA, p1 = L.fcy * sA + L.uw1 * dA, p2 = L.fcz * sA + L.uw2 * dA;
+    const RT p0 = fcx * sA + uw0 * dA, p1 = fcy * sA + uw1 * dA, p2 = fcz * sA + uw2 * dA;
     acc.add(0, p0); acc.add(1, p1); acc.add(2, p2);
-    acc.add(3, L.x1 * p2 - L.x2 * p1);
-    acc.add(4, L.x2 * p0 - L.x0 * p2);
-    acc.add(5, L.x0 * p1 - L.x1 * p0);
+    acc.add(3, x1 * p2 - x2 * p1);
+    acc.add(4, x2 * p0 - x0 * p2);
+    acc.add(5, x0 * p1 - x1 * p0);
 }
 
-template <typename T, typename RT, typename W, bool Q64>
-__device__ __forceinline__ void ibb_link(const DeviceState& s, const DeviceParticles& P, int p, int parity,
-                                         const IbbBox<W>& B, uint32_t v, const RT (&UW)[6], ForceAcc<RT>& acc) {
-    const IbbLink<T, RT> L = ibb_gather<T, RT, W, Q64>(s, P, p, parity, B, v, UW);
-    ibb_finish<T, RT>(s, L, acc);
-}
-
-// two links per lane: both gathers in flight before either finish
-template <typename T, typename RT, typename W, bool Q64>
-__device__ __forceinline__ void ibb_link2(const DeviceState& s, const DeviceParticles& P, int p, int parity,
-                                          const IbbBox<W>& B, uint32_t v1, uint32_t v2, const RT (&UW)[6],
+// NL links per lane: all gathers in flight before the first finish
+template <typename T, typename RT, typename W, bool Q64, int NL>
+__device__ __forceinline__ void ibb_links(const DeviceState& s, const DeviceParticles& P, int p, int parity,
+                                          const IbbBox<W>& B, const uint32_t (&v)[NL], const RT (&UW)[6],
                                           ForceAcc<RT>& acc) {
-    const IbbLink<T, RT> L1 = ibb_gather<T, RT, W, Q64>(s, P, p, parity, B, v1, UW);
-    const IbbLink<T, RT> L2 = ibb_gather<T, RT, W, Q64>(s, P, p, parity, B, v2, UW);
-    ibb_finish<T, RT>(s, L1, acc);
-    ibb_finish<T, RT>(s, L2, acc);
+    IbbLink<T, RT> L[NL];
+#pragma unroll
+    for (int k = 0; k < NL; ++k) L[k] = ibb_gather<T, RT, W, Q64>(s, P, p, parity, B, v[k]);
+#pragma unroll
+    for (int k = 0; k < NL; ++k) ibb_finish<T, RT, W>(s, P, p, B, L[k], UW, acc);
 }
 
 constexpr int kIbbQueue = 256;        // link queue entries per warp (a power of 2)
+constexpr int kIbbLinks = 2;         // links per lane in flight (kIbbQueue >= 64 kIbbLinks)
+constexpr int kIbbStageRows = 16;     // owner rows in flight per warp while staging
 
 // shared-memory plan of k_ibb for spheres of radius R with row words of
-// wbits bits; bytes == 0 when the staged rows do not fit one word
+// wbits bits; bytes == 0 when the staged rows do not fit one word.  The
+// staging buffers (kIbbStageRows owner rows of wbits ints per warp) share
+// their space with the link queues, which are used only afterwards.
 struct IbbPlan { int S, own_off, fluid_off, row_off, tab_off, dir_off, list_off, queue_off, bytes; };
 __host__ __device__ inline IbbPlan ibb_plan(double R, int wbits) {
     IbbPlan pl;
@@ -561,8 +576,20 @@ __host__ __device__ inline IbbPlan ibb_plan(double R, int wbits) {
     pl.dir_off = (pl.dir_off + 15) & ~15;
     pl.list_off = pl.dir_off + Q * (int)sizeof(IbbDir);
     pl.queue_off = (pl.list_off + SS * 2 + 15) & ~15;
-    pl.bytes = pl.S <= wbits ? pl.queue_off + (kPThreads / 32) * kIbbQueue * 4 : 0;
+    const int queue_bytes = (kPThreads / 32) * kIbbQueue * 4;
+    const int stage_bytes = (kPThreads / 32) * kIbbStageRows * wbits * 4;
+    pl.bytes = pl.S <= wbits ? pl.queue_off + (queue_bytes > stage_bytes ? queue_bytes : stage_bytes) : 0;
     return pl;
+}
+
+// 4-byte asynchronous copy global -> shared (completes at cp_async_wait_all
+// of the issuing thread)
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
 }
 
 template <typename T, typename RT, typename W, bool Q64>
@@ -618,46 +645,53 @@ __global__ void __launch_bounds__(kPThreads, sizeof(RT) == 8 ? 2 : 4)
         d.pad = 0;
         dir[i] = d;
     }
-    __syncthreads();                                     // the staging reads wZ
-    // staging: one warp per row, lane j holds nodes a = j (and j + 32)
+    __syncthreads();                                     // the staging reads wZ, tB, tC
+    // staging: a warp takes kIbbStageRows consecutive rows at a time; lane j
+    // copies nodes a = j (and j + 32) of each into the warp's buffer with
+    // asynchronous copies (all rows in flight at once, no registers held),
+    // then the rows become the two masks by ballots over the lane's own
+    // copies.  Rows beyond R + 4.5 of the centre are not read (masks 0): the
+    // links start on rows within R + 1.5 and read the masks at most two rows
+    // further in each of b and c (2 sqrt 2 < 3).
     {
         const int* __restrict__ owner = P.owner;
         const int nrows = SB * SC;
         const int a0 = wrapi(ya + lane, g.NX);
         const int a1 = sizeof(W) == 8 ? wrapi(ya + lane + 32, g.NX) : 0;
-        int b = wid % SB, c = wid / SB;                  // row r = b + SB * c, r += nw
-        const int sb = nw % SB, sc = nw / SB;
-        constexpr int U = 8;                             // rows in flight per warp
-        for (int r0 = wid; r0 < nrows; r0 += U * nw) {
-            int o[U][2], rb[U], rc[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                rb[u] = b; rc[u] = c;
-                o[u][0] = o[u][1] = -3;
+        constexpr int WI = 8 * (int)sizeof(W);           // ints per buffered row
+        int* const buf = reinterpret_cast<int*>(ibb_smem + pl.queue_off) + wid * kIbbStageRows * WI;
+        const float lim = (ext + 3.f) * (ext + 3.f);
+        for (int r0 = wid * kIbbStageRows; r0 < nrows; r0 += nw * kIbbStageRows) {
+            const int nr = min(kIbbStageRows, nrows - r0);
+            const int b0 = r0 % SB, c0 = r0 / SB;
+            unsigned read = 0;                           // bit u: row r0 + u was copied
+            for (int u = 0, b = b0, c = c0; u < nr; ++u) {
                 const int ix = xc + c;
-                if (r0 + u * nw < nrows && ix >= 0 && ix < g.NZ) {
-                    const uint32_t rowbase = (uint32_t)g.NX * (uint32_t)wZ[b] + (uint32_t)NXY * (uint32_t)ix;
-                    if (lane < SA) o[u][0] = __ldg(owner + rowbase + a0);
-                    if (sizeof(W) == 8 && lane + 32 < SA) o[u][1] = __ldg(owner + rowbase + a1);
+                if (ix >= 0 && ix < g.NZ && tB[b] * tB[b] + tC[c] * tC[c] <= lim) {
+                    read |= 1u << u;
+                    const int* row = owner + ((size_t)g.NX * (uint32_t)wZ[b] + (size_t)NXY * (uint32_t)ix);
+                    if (lane < SA) cp_async4(buf + u * WI + lane, row + a0);
+                    if (sizeof(W) == 8 && lane + 32 < SA) cp_async4(buf + u * WI + 32 + lane, row + a1);
                 }
-                b += sb; c += sc;
-                if (b >= SB) { b -= SB; ++c; }
+                if (++b == SB) { b = 0; ++c; }
             }
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const unsigned po = __ballot_sync(0xffffffffu, o[u][0] == p);
-                const unsigned fo = __ballot_sync(0xffffffffu, o[u][0] == -1);
-                W pw = (W)po, fw = (W)fo;
+            cp_async_wait_all();
+            for (int u = 0, b = b0, c = c0; u < nr; ++u) {
+                const bool rv = (read >> u) & 1u;
+                const int o0 = (rv && lane < SA) ? buf[u * WI + lane] : -3;
+                W pw = (W)__ballot_sync(0xffffffffu, o0 == p), fw = (W)__ballot_sync(0xffffffffu, o0 == -1);
                 if constexpr (sizeof(W) == 8) {
-                    pw |= (W)__ballot_sync(0xffffffffu, o[u][1] == p) << 32;
-                    fw |= (W)__ballot_sync(0xffffffffu, o[u][1] == -1) << 32;
+                    const int o1 = (rv && lane + 32 < SA) ? buf[u * WI + 32 + lane] : -3;
+                    pw |= (W)__ballot_sync(0xffffffffu, o1 == p) << 32;
+                    fw |= (W)__ballot_sync(0xffffffffu, o1 == -1) << 32;
                 }
-                if (lane == 0 && r0 + u * nw < nrows &&
-                    LBM_IN_BOUNDS(s.bounds, rb[u] >= 0 && rb[u] < S && rc[u] >= 0 && rc[u] < S, 223)) {
-                    own[rb[u] + S * rc[u]] = pw;
-                    fluid[rb[u] + S * rc[u]] = fw;
+                if (lane == 0 && LBM_IN_BOUNDS(s.bounds, b < S && c < S, 223)) {
+                    own[b + S * c] = pw;
+                    fluid[b + S * c] = fw;
                 }
+                if (++b == SB) { b = 0; ++c; }
             }
+            __syncwarp();                                // the buffer is refilled next
         }
     }
     __syncthreads();
@@ -749,29 +783,33 @@ __global__ void __launch_bounds__(kPThreads, sizeof(RT) == 8 ? 2 : 4)
                     tail += __popc(bal);
                     if (tail - head >= 32) {
                         __syncwarp();
-                        const uint32_t v = q[(head + lane) & (kIbbQueue - 1)];
+                        const uint32_t v[1] = {q[(head + lane) & (kIbbQueue - 1)]};
                         head += 32;
                         __syncwarp();
-                        ibb_link<T, RT, W, Q64>(s, P, p, parity, Bx, v, UW, acc);
+                        ibb_links<T, RT, W, Q64, 1>(s, P, p, parity, Bx, v, UW, acc);
                     }
                 }
             }
-            while (tail - head >= 64) {
+            while (tail - head >= 32 * kIbbLinks) {
                 __syncwarp();
-                const uint32_t v1 = q[(head + lane) & (kIbbQueue - 1)];
-                const uint32_t v2 = q[(head + 32 + lane) & (kIbbQueue - 1)];
-                head += 64;
+                uint32_t v[kIbbLinks];
+#pragma unroll
+                for (int k = 0; k < kIbbLinks; ++k) v[k] = q[(head + 32 * k + lane) & (kIbbQueue - 1)];
+                head += 32 * kIbbLinks;
                 __syncwarp();
-                ibb_link2<T, RT, W, Q64>(s, P, p, parity, Bx, v1, v2, UW, acc);
+                ibb_links<T, RT, W, Q64, kIbbLinks>(s, P, p, parity, Bx, v, UW, acc);
             }
         }
         __syncwarp();
-        if (tail - head >= 32) {
-            const uint32_t v = q[(head + lane) & (kIbbQueue - 1)];
+        while (tail - head >= 32) {
+            const uint32_t v[1] = {q[(head + lane) & (kIbbQueue - 1)]};
             head += 32;
-            ibb_link<T, RT, W, Q64>(s, P, p, parity, Bx, v, UW, acc);
+            ibb_links<T, RT, W, Q64, 1>(s, P, p, parity, Bx, v, UW, acc);
         }
-        if (lane < tail - head) ibb_link<T, RT, W, Q64>(s, P, p, parity, Bx, q[(head + lane) & (kIbbQueue - 1)], UW, acc);
+        if (lane < tail - head) {
+            const uint32_t v[1] = {q[(head + lane) & (kIbbQueue - 1)]};
+            ibb_links<T, RT, W, Q64, 1>(s, P, p, parity, Bx, v, UW, acc);
+        }
     }
     // per-sphere FP64 reduction: warp shuffles, then across warps
     __shared__ double sh[6][kPThreads / 32];
