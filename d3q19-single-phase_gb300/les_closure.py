@@ -7,7 +7,8 @@ library builds the closure's training pairs (features of the filtered strain,
 target eddy viscosity from the subgrid stress).  The network is trained with
 the library's own kernels (forward, backward, Adam; BF16 tensor-core
 products).  A coarse MRT LES with the network fused into the collision then
-starts from the last filtered snapshot, and plain MRT on the same coarse grid
+starts from the last filtered snapshot (rounded to FP16, the state the test
+fixtures keep), and plain MRT on the same coarse grid
 from the same state, while the DNS continues from that state over the same
 physical time; the mean streamwise profiles averaged over the second half of
 that window are compared (the DNS profile box-averaged to the coarse cells).
@@ -179,7 +180,10 @@ def main():
                     X = lattice_features(f, ub)
                 data[f][0].append(X)
                 data[f][1].append(y)
-                ub0[f] = ub
+                # the LES runs start from the last snapshot rounded to FP16:
+                # the state committed with the test fixtures, from which a
+                # test repeats the same runs
+                ub0[f] = ub.astype(np.float16).astype(np.float32)
         # the LES runs start from this state (the last snapshot); the DNS
         # continues over the same physical time for the comparison
         prof = np.zeros(wall)
@@ -259,7 +263,12 @@ def main():
                 les_closure_profile=np.array(res["closure"]["profile"] or []),
                 les_plain_profile=np.array(res["plain_mrt"]["profile"] or []),
                 ustar=cfg0["ustar"], h_coarse=cfg0["h"] / f, visc_coarse=cfg0["visc"] / f,
-                grid_coarse=np.array([wall // f, stream // f, span // f]))
+                grid_coarse=np.array([wall // f, stream // f, span // f]),
+                les_start_velocity=ub0[f].astype(np.float16), les_steps=args.window // f,
+                les_sample_every=max(sample_fine // f, 1), aplus=args.aplus,
+                les_errors=np.array([res[k]["mean_profile_rel_err"] if res[k]["mean_profile_rel_err"] is not None
+                                     else np.nan for k in ("closure", "closure_wall_damped", "plain_mrt")
+                                     if k in res]))
         print(json.dumps({"factor": f, **{k: out[k] for k in ("data", "training", "gpu_time_ratio_dns_over_les")},
                           "les": {k: {kk: vv for kk, vv in v.items() if kk not in ("profile", "nut_over_nu_profile")}
                                   for k, v in res.items()}}), flush=True)

@@ -289,3 +289,41 @@ def test_trained_closure_runs_a_coarse_les(pkg):
     assert st.nonfinite == 0
     assert nut.min() > -1e-4 and 0 < nut.mean() < 1.0          # nu_t from the FP32 rate: round-off only
     assert np.abs(mean - prof).max() < 0.1 * prof.max()
+
+
+def _les_closure_module():
+    import importlib.util
+    path = Path(__file__).resolve().parents[1] / "d3q19-single-phase_gb300" / "les_closure.py"
+    spec = importlib.util.spec_from_file_location("les_closure", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def test_closure_a_posteriori_gain_over_plain_mrt(pkg):
+    """A posteriori, on the GPU: from the committed start state (the last
+    filtered snapshot of the 512x256x256 channel DNS, filter 4, in FP16) the
+    coarse 128x64x64 LES with the committed network damped at the walls
+    (van Driest, the fixture's A+) and plain MRT on the same grid each run
+    the committed window (les_closure.py's own runs: 100 000 coarse steps,
+    profiles averaged over the second half).  The closure's mean streamwise
+    profile is closer to the box-averaged DNS profile than plain MRT's by
+    more than a point, and within 4% of the DNS centreline (the committed
+    pipeline run: 3.3% against 5.5%; the runs are bit-reproducible with one
+    build, so the test repeats those numbers)."""
+    d = np.load(GOLDEN / "closure_channel_512x256x256_filter4.npz")
+    les = _les_closure_module()
+    f = 4
+    cfg = dict(visc=float(d["visc_coarse"]) * f, ustar=float(d["ustar"]), h=float(d["h_coarse"]) * f, factor=f)
+    ub = d["les_start_velocity"].astype(np.float32)
+    ref = d["dns_window_profile"]
+    steps, every = int(d["les_steps"]), int(d["les_sample_every"])
+    err = {}
+    for name, closure, aplus in (("damped", True, float(d["aplus"])), ("plain", False, 0.0)):
+        prof, _, fail, _ = les.les_run(d["params"], d["norm"], ub, cfg, steps, every, closure, aplus)
+        assert fail is None, name
+        err[name] = float(np.abs(prof - ref).max() / np.abs(ref).max())
+    print(f"a-posteriori max deviation: damped closure {err['damped']:.4f}, plain MRT {err['plain']:.4f} "
+          f"(pipeline run: {d['les_errors'][1]:.4f}, {d['les_errors'][2]:.4f})")
+    assert err["damped"] < err["plain"] - 0.01
+    assert err["damped"] < 0.04

@@ -82,9 +82,9 @@ def test_closure_a_posteriori_report():
     snapshot over the DNS's continued window; mean streamwise profiles
     averaged over the second half against the box-averaged DNS.  At filter 4
     the wall-damped closure lowers the largest deviation from the DNS below
-    that of plain MRT by more than the spread between two DNS trajectories
-    (~2 points), at >= 20x less GPU time than the DNS; at filter 8 the
-    closure over-damps the coarse wall cells and plain MRT stays better."""
+    that of plain MRT by more than a point, at >= 20x less GPU time than the
+    DNS; at filter 8 the closure over-damps the coarse wall cells and plain
+    MRT stays better."""
     r = json.loads((GOLDEN / "closure_channel_512x256x256_report.json").read_text())
     f4, f8 = r["factors"]["4"], r["factors"]["8"]
     err = {k: v["mean_profile_rel_err"] for k, v in f4["les"].items()}
