@@ -36,6 +36,7 @@ struct lbm_ctx {
     int* d_err = nullptr;      // set by a kernel whose bounded wait gave up
     DeviceParticles P{};       // spheres (npart == 0: none)
     lbm_particle_params pp{};
+    lbm::SideStream side;      // the sphere pass's second stream (created with the spheres)
     int have_prev = 0;         // previous-step force and torque available
     int order_age = 0;         // steps since the spheres' spatial order was sorted
     unsigned long long* d_count = nullptr;
@@ -404,6 +405,12 @@ int lbm_destroy(lbm_ctx* c) {
     cudaFree(c->d_les);
     cudaFree(c->d_s9);
     cudaFree(c->d_mass);
+    if (c->side.st) {
+        cudaStreamSynchronize(c->side.st);
+        cudaStreamDestroy(c->side.st);
+    }
+    if (c->side.fork) cudaEventDestroy(c->side.fork);
+    if (c->side.join) cudaEventDestroy(c->side.join);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return LBM_OK;
@@ -531,7 +538,7 @@ int lbm_step_async(lbm_ctx* c, int32_t nsteps) {
                 c->nlaunch += kReorderKernels;
                 c->order_age = 0;
             }
-            CK(particles_after_step(c->s, c->P, c->parity, c->have_prev, c->stream));
+            CK(particles_after_step(c->s, c->P, c->parity, c->have_prev, c->stream, c->side));
             c->nlaunch += particles_kernels_per_step(c->P);
             c->have_prev = 1;
             // main.f90:163-167: with particles, every 100 steps the mean
@@ -1030,6 +1037,14 @@ int lbm_particles_set(lbm_ctx* c, const lbm_particle_params* pp, const double* p
     if (!P.counters) CK(cudaMalloc(&P.counters, 4 * sizeof(unsigned)));
     if (!c->d_count) CK(cudaMalloc(&c->d_count, sizeof(unsigned long long)));
     if (!c->d_mass) CK(cudaMalloc(&c->d_mass, 2 * sizeof(double)));
+    if (!c->side.st) {
+        // the sphere pass's second stream; set only once all three exist
+        if (!c->side.fork) CK(cudaEventCreateWithFlags(&c->side.fork, cudaEventDisableTiming));
+        if (!c->side.join) CK(cudaEventCreateWithFlags(&c->side.join, cudaEventDisableTiming));
+        cudaStream_t st = nullptr;
+        CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        c->side.st = st;
+    }
     const int cap = std::max(4096, 64 * n);
     if (P.refill_cap < cap) {
         cudaFree(P.refill_node);

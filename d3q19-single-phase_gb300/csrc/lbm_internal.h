@@ -201,8 +201,16 @@ __host__ __device__ inline double uniform_pm1(uint64_t seed, uint64_t key) {
 // dynamic shared memory of the bounce-back kernel for spheres of radius R
 size_t particles_smem_bytes(double R);
 cudaError_t particles_claim(const DeviceState& s, const DeviceParticles& P, cudaStream_t st);
+// A second stream of the context with two events: the sphere pass forks the
+// repulsion (which needs only the positions) onto it, concurrent with the
+// bounce-back kernel, and joins it back before the Newton-Euler update.
+// st == nullptr: everything runs on the main stream.
+struct SideStream {
+    cudaStream_t st = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
 cudaError_t particles_after_step(const DeviceState& s, const DeviceParticles& P, int parity, int have_prev,
-                                 cudaStream_t st);
+                                 cudaStream_t st, const SideStream& side);
 // kernels that one particles_after_step launches
 int particles_kernels_per_step(const DeviceParticles& P);
 // re-sort the spheres into the bounce-back kernel's spatial order from their

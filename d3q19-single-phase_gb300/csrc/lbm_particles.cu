@@ -16,8 +16,10 @@
 //     al. 2014) is reduced per sphere with warp shuffles into FP64 force and
 //     torque;
 //  3. k_bin + k_repulsion_cells (a cell list; k_repulsion, all pairs, for
-//     small domains): soft-sphere repulsion summed in sphere-index order;
-//     k_newton, one thread per sphere: the FP64 Newton-Euler update
+//     small domains): soft-sphere repulsion summed in sphere-index order, on
+//     the context's second stream while k_ibb runs (it needs only the
+//     positions); k_newton, one thread per sphere, after both: the FP64
+//     Newton-Euler update
 //     (average of this step's and the previous step's force and torque);
 //  4. k_shell<release>, then k_shell<claim>: node ownership follows the new
 //     positions along the thin shell swept by each surface; nodes that leave
@@ -1320,10 +1322,30 @@ cudaError_t particles_claim(const DeviceState& s, const DeviceParticles& P, cuda
 
 // Everything that follows a fluid step when spheres are present.
 cudaError_t particles_after_step(const DeviceState& s, const DeviceParticles& P, int parity, int have_prev,
-                                 cudaStream_t st) {
+                                 cudaStream_t st, const SideStream& side) {
     if (P.npart == 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(P.counters, 0, 2 * sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
+    // the repulsion reads only the positions and writes only P.rep, the cell
+    // list and counters[2], none of which the bounce-back kernel touches: it
+    // runs on the side stream while k_ibb runs
+    cudaStream_t rs = st;
+    if (side.st) {
+        if ((e = cudaEventRecord(side.fork, st)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(side.st, side.fork, 0)) != cudaSuccess) return e;
+        rs = side.st;
+    }
+    if (P.ncell > 0) {
+        e = cudaMemsetAsync(P.cell_count, 0, (size_t)P.ncell * sizeof(int), rs);
+        if (e == cudaSuccess) e = cudaMemsetAsync(P.counters + 2, 0, sizeof(unsigned), rs);
+        if (e != cudaSuccess) return e;
+        k_bin<<<(P.npart + 255) / 256, 256, 0, rs>>>(P, s.g);
+        k_repulsion_cells<<<(P.npart + kRepWarps - 1) / kRepWarps, 32 * kRepWarps, 0, rs>>>(P, s.g);
+    } else {
+        k_repulsion<<<(P.npart + kRepTile - 1) / kRepTile, kRepTile, 0, rs>>>(P, s.g);
+    }
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (side.st && (e = cudaEventRecord(side.join, side.st)) != cudaSuccess) return e;
     const size_t smem = ibb_smem_bytes(P.R);
     const bool w32 = ibb_plan(P.R, 32).bytes != 0;
     switch (s.prec) {
@@ -1341,15 +1363,7 @@ cudaError_t particles_after_step(const DeviceState& s, const DeviceParticles& P,
             break;
     }
     if (e != cudaSuccess) return e;
-    if (P.ncell > 0) {
-        e = cudaMemsetAsync(P.cell_count, 0, (size_t)P.ncell * sizeof(int), st);
-        if (e == cudaSuccess) e = cudaMemsetAsync(P.counters + 2, 0, sizeof(unsigned), st);
-        if (e != cudaSuccess) return e;
-        k_bin<<<(P.npart + 255) / 256, 256, 0, st>>>(P, s.g);
-        k_repulsion_cells<<<(P.npart + kRepWarps - 1) / kRepWarps, 32 * kRepWarps, 0, st>>>(P, s.g);
-    } else {
-        k_repulsion<<<(P.npart + kRepTile - 1) / kRepTile, kRepTile, 0, st>>>(P, s.g);
-    }
+    if (side.st && (e = cudaStreamWaitEvent(st, side.join, 0)) != cudaSuccess) return e;
     k_newton<<<(P.npart + 127) / 128, 128, 0, st>>>(P, s.g, s.cd.Fx, s.cd.Fy, s.cd.Fz, have_prev);
     k_shell<false><<<(P.npart + kShellWarps - 1) / kShellWarps, 32 * kShellWarps, 0, st>>>(P, s.g, P.owner, 0, s.bounds);
     k_shell<true><<<(P.npart + kShellWarps - 1) / kShellWarps, 32 * kShellWarps, 0, st>>>(P, s.g, P.owner, 0, s.bounds);

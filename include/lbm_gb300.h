@@ -43,7 +43,10 @@
  *    double precision, the reference's -r8 REAL.
  *  - Host pointers are borrowed only for the duration of a call.  Calls are
  *    synchronous at the ABI edge unless named *_async.  One host thread per
- *    context; one GPU and one CUDA stream per context.
+ *    context; one GPU and one CUDA stream per context (lbm_stream): every
+ *    call's work is ordered on it.  With spheres, the sphere pass forks the
+ *    repulsion onto a second stream of the context and joins it back on the
+ *    context's stream before the Newton-Euler update.
  */
 #ifndef LBM_GB300_H
 #define LBM_GB300_H
