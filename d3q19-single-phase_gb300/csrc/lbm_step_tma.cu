@@ -32,6 +32,7 @@
 // no bulk copy still targets the CTA's shared memory when it exits.
 #include <algorithm>
 
+#include "lbm_f32x2.cuh"
 #include "lbm_internal.h"
 
 namespace lbm {
@@ -84,22 +85,16 @@ __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wa
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 // storage <-> arithmetic helpers for an aligned pair / a single element
-__device__ __forceinline__ void ld_pair(const __half* p, float& a, float& b) {
-    const float2 v = __half22float2(*reinterpret_cast<const __half2*>(p));
-    a = v.x; b = v.y;
+__device__ __forceinline__ F2 ld_pair(const __half* p) {
+    return F2(__half22float2(*reinterpret_cast<const __half2*>(p)));
 }
-__device__ __forceinline__ void ld_pair(const float* p, float& a, float& b) {
-    const float2 v = *reinterpret_cast<const float2*>(p);
-    a = v.x; b = v.y;
-}
+__device__ __forceinline__ F2 ld_pair(const float* p) { return F2(*reinterpret_cast<const float2*>(p)); }
 __device__ __forceinline__ float ld_one(const __half* p) { return __half2float(*p); }
 __device__ __forceinline__ float ld_one(const float* p) { return *p; }
-__device__ __forceinline__ void st_pair(__half* p, float a, float b) {
-    *reinterpret_cast<__half2*>(p) = __floats2half2_rn(a, b);
+__device__ __forceinline__ void st_pair(__half* p, F2 v) {
+    *reinterpret_cast<__half2*>(p) = __float22half2_rn(v.v);
 }
-__device__ __forceinline__ void st_pair(float* p, float a, float b) {
-    *reinterpret_cast<float2*>(p) = make_float2(a, b);
-}
+__device__ __forceinline__ void st_pair(float* p, F2 v) { *reinterpret_cast<float2*>(p) = v.v; }
 __device__ __forceinline__ void st_one(__half* p, float a) { *p = __float2half_rn(a); }
 __device__ __forceinline__ void st_one(float* p, float a) { *p = a; }
 
@@ -210,37 +205,52 @@ __device__ __forceinline__ void issue_item(const PopPtrs<T>& P, const Geometry& 
 // node read slot opp(i).  Every thread therefore overwrites only stage
 // positions that it has read itself, and the finished stage holds the item's
 // results row for row, to be copied back to the addresses it was loaded from.
+// F2 holds the pair's populations (node x, node x+1).  The FP16 odd step
+// relaxes both nodes with packed FP32 instructions (C2): its x-shifted
+// populations cost single-element shared-memory accesses, which leave it
+// bound by instruction issue, and the packed collision halves the
+// floating-point instructions (3.69 -> 3.39 ms per launch on the large
+// channel).  The memory-bound kernels (FP16 even, FP32) keep the scalar
+// collision per node (C), which measured 0.4% (FP16 even) and 1.7% (FP32)
+// faster than the packed one.
 template <typename T, bool ODD, int WALL, bool YF>
-__device__ __forceinline__ void pair_update(const CollideConsts<float>& C, const Geometry& g, T* stage, int x) {
+__device__ __forceinline__ void pair_update(const CollideConsts<float>& C, const CollideConsts<F2>& C2,
+                                            const Geometry& g, T* stage, int x) {
+    constexpr bool kPacked = ODD && sizeof(T) == 2;
     const int NX = g.NX;
     const int xm1 = (x == 0) ? NX - 1 : x - 1;
     const int xp2 = (x + 2 == NX) ? 0 : x + 2;
-    float fa[Q], fb[Q];
+    F2 f[Q];
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
         const T* r = stage + i * NX;
         const int sh = (ODD && !pull_bb(WALL, i)) ? DXg(i) : 0;   // f_i(x) = row[x - sh]
-        if (sh == 0) {
-            ld_pair(r + x, fa[i], fb[i]);
-        } else if (sh == 1) {
-            fa[i] = ld_one(r + xm1); fb[i] = ld_one(r + x);
-        } else {
-            fa[i] = ld_one(r + x + 1); fb[i] = ld_one(r + xp2);
-        }
+        if (sh == 0) f[i] = ld_pair(r + x);
+        else if (sh == 1) f[i] = F2(ld_one(r + xm1), ld_one(r + x));
+        else f[i] = F2(ld_one(r + x + 1), ld_one(r + xp2));
     }
-    float rho, jx, jy, jz;
-    collide<float, false, YF>(fa, C, 0.f, 0.f, 0.f, rho, jx, jy, jz);
-    collide<float, false, YF>(fb, C, 0.f, 0.f, 0.f, rho, jx, jy, jz);
+    if constexpr (kPacked) {
+        F2 rho, jx, jy, jz;
+        collide<F2, false, YF>(f, C2, F2(0.f), F2(0.f), F2(0.f), rho, jx, jy, jz);
+    } else {
+        float fa[Q], fb[Q], rho, jx, jy, jz;
+#pragma unroll
+        for (int i = 0; i < Q; ++i) { fa[i] = f[i].v.x; fb[i] = f[i].v.y; }
+        collide<float, false, YF>(fa, C, 0.f, 0.f, 0.f, rho, jx, jy, jz);
+        collide<float, false, YF>(fb, C, 0.f, 0.f, 0.f, rho, jx, jy, jz);
+#pragma unroll
+        for (int i = 0; i < Q; ++i) f[i] = F2(fa[i], fb[i]);
+    }
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
         const int sh = (ODD && !push_bb(WALL, i)) ? DXg(i) : 0;
         T* d = stage + OPPf(i) * NX;
         if (sh == 0) {
-            st_pair(d + x, fa[i], fb[i]);
+            st_pair(d + x, f[i]);
         } else if (sh == 1) {
-            st_one(d + x + 1, fa[i]); st_one(d + xp2, fb[i]);
+            st_one(d + x + 1, f[i].v.x); st_one(d + xp2, f[i].v.y);
         } else {
-            st_one(d + xm1, fa[i]); st_one(d + x, fb[i]);
+            st_one(d + xm1, f[i].v.x); st_one(d + x, f[i].v.y);
         }
     }
 }
@@ -248,12 +258,12 @@ __device__ __forceinline__ void pair_update(const CollideConsts<float>& C, const
 // All pairs of an item handled by this thread; the wall case is fixed for
 // the whole loop.
 template <typename T, bool ODD, int WALL, bool YF>
-__device__ __forceinline__ void item_pairs(const CollideConsts<float>& C, const Geometry& g, T* stage, int tid,
-                                           int nthreads, unsigned* bflag) {
+__device__ __forceinline__ void item_pairs(const CollideConsts<float>& C, const CollideConsts<F2>& C2,
+                                           const Geometry& g, T* stage, int tid, int nthreads, unsigned* bflag) {
     const int npairs = g.NX >> 1;
     for (int p = tid; p < npairs; p += nthreads)
         if (LBM_IN_BOUNDS(bflag, 2 * p + 1 < g.NX && (g.NX & 1) == 0, 303))
-            pair_update<T, ODD, WALL, YF>(C, g, stage, 2 * p);
+            pair_update<T, ODD, WALL, YF>(C, C2, g, stage, 2 * p);
 }
 
 // Issued by the last warp to finish an item: lane i copies result row i back
@@ -275,7 +285,7 @@ constexpr int kMaxStages = 5;
 
 template <typename T, bool ODD, bool YF, int NT>
 __global__ void __launch_bounds__(NT, 512 / NT)
-k_step_rows(PopPtrs<T> P, CollideConsts<float> C, Geometry g, int nstage, int* err) {
+k_step_rows(PopPtrs<T> P, CollideConsts<float> C, CollideConsts<F2> C2, Geometry g, int nstage, int* err) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ unsigned int done_count[kMaxStages];
     __shared__ unsigned int issued_par, issued_any;
@@ -329,10 +339,10 @@ k_step_rows(PopPtrs<T> P, CollideConsts<float> C, Geometry g, int nstage, int* e
         const Item I = item_of(g, it);
         const int wall = wall_of(g, I.z);
         T* stage = stage_ptr0 + (size_t)s * Q * g.NX;
-        if (wall == 0)      item_pairs<T, ODD, 0, YF>(C, g, stage, tid, NT, bflag);
-        else if (wall == 1) item_pairs<T, ODD, 1, YF>(C, g, stage, tid, NT, bflag);
-        else if (wall == 2) item_pairs<T, ODD, 2, YF>(C, g, stage, tid, NT, bflag);
-        else                item_pairs<T, ODD, 3, YF>(C, g, stage, tid, NT, bflag);
+        if (wall == 0)      item_pairs<T, ODD, 0, YF>(C, C2, g, stage, tid, NT, bflag);
+        else if (wall == 1) item_pairs<T, ODD, 1, YF>(C, C2, g, stage, tid, NT, bflag);
+        else if (wall == 2) item_pairs<T, ODD, 2, YF>(C, C2, g, stage, tid, NT, bflag);
+        else                item_pairs<T, ODD, 3, YF>(C, C2, g, stage, tid, NT, bflag);
         // this warp has finished with stage s; the last warp copies the
         // results back and refills it
         fence_proxy_async();
@@ -407,11 +417,27 @@ RowPlan plan_rows(const Geometry& g) {
     return r;
 }
 
+// the FP32 collision constants, each duplicated into both lanes
+CollideConsts<F2> pair_consts(const CollideConsts<float>& c) {
+    CollideConsts<F2> r;
+    r.S = c.S; r.invS = c.invS;
+    r.Fx = c.Fx; r.Fy = c.Fy; r.Fz = c.Fz;
+    r.hFx = c.hFx; r.hFy = c.hFy; r.hFz = c.hFz;
+    r.ajx = c.ajx; r.ajy = c.ajy; r.ajz = c.ajz;
+    r.fqx = c.fqx; r.fqy = c.fqy; r.fqz = c.fqz;
+    r.thFx = c.thFx; r.thFy = c.thFy; r.thFz = c.thFz;
+    r.ke = c.ke; r.keps = c.keps; r.kq = c.kq; r.kp = c.kp; r.kpi = c.kpi; r.kxy = c.kxy; r.km = c.km;
+    r.kw = c.kw; r.kwi = c.kwi;
+    r.oeps = c.oeps; r.oepsj = c.oepsj; r.oxx = c.oxx;
+    return r;
+}
+
 template <typename T, bool YF, int NT>
 void launch_rows_nt(const DeviceState& s, const PopPtrs<T>& P, int parity, int* err, const RowPlan& r,
                     unsigned grid, cudaStream_t st) {
-    if (parity == 0) k_step_rows<T, false, YF, NT><<<grid, NT, r.smem, st>>>(P, s.cf, s.g, r.nstage, err);
-    else             k_step_rows<T, true, YF, NT><<<grid, NT, r.smem, st>>>(P, s.cf, s.g, r.nstage, err);
+    const CollideConsts<F2> c2 = pair_consts(s.cf);
+    if (parity == 0) k_step_rows<T, false, YF, NT><<<grid, NT, r.smem, st>>>(P, s.cf, c2, s.g, r.nstage, err);
+    else             k_step_rows<T, true, YF, NT><<<grid, NT, r.smem, st>>>(P, s.cf, c2, s.g, r.nstage, err);
 }
 
 template <typename T>
