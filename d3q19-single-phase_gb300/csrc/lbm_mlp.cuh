@@ -58,6 +58,40 @@ __host__ __device__ inline float mlp_infer(const float* P, const float* norm, co
     return mlp_softplus(z3);
 }
 
+#ifdef __CUDACC__
+// mlp_infer on the GPU with the hidden units taken two at a time: one packed
+// FP32 fused multiply-add (fma.rn.f32x2, sm_100 and later) advances units j
+// and j+1, each lane with the scalar version's operation and order, so the
+// result is the same bit for bit with half the multiply-add instructions.
+// P must be 8-byte aligned (weight pairs are read as float2).
+__device__ __forceinline__ float mlp_infer_pairs(const float* P, const float* norm, const float* x) {
+    float xn[kMlpIn];
+#pragma unroll
+    for (int i = 0; i < kMlpIn; ++i) xn[i] = (x[i] - norm[i]) * norm[kMlpIn + i];
+    float h1[kMlpH];
+#pragma unroll
+    for (int j = 0; j < kMlpH; j += 2) {
+        float2 z = *reinterpret_cast<const float2*>(P + kOffB1 + j);
+#pragma unroll
+        for (int i = 0; i < kMlpIn; ++i)
+            z = __ffma2_rn(make_float2(xn[i], xn[i]), *reinterpret_cast<const float2*>(P + kOffW1 + i * kMlpH + j), z);
+        h1[j] = mlp_silu(z.x);
+        h1[j + 1] = mlp_silu(z.y);
+    }
+    float z3 = P[kOffB3];
+#pragma unroll 1
+    for (int j = 0; j < kMlpH; j += 2) {
+        float2 z = *reinterpret_cast<const float2*>(P + kOffB2 + j);
+#pragma unroll
+        for (int i = 0; i < kMlpH; ++i)
+            z = __ffma2_rn(make_float2(h1[i], h1[i]), *reinterpret_cast<const float2*>(P + kOffW2 + i * kMlpH + j), z);
+        z3 += mlp_silu(z.x) * P[kOffW3 + j];
+        z3 += mlp_silu(z.y) * P[kOffW3 + j + 1];
+    }
+    return mlp_softplus(z3);
+}
+#endif
+
 }  // namespace lbm
 
 namespace lbm {

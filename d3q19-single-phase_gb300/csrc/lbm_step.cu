@@ -144,7 +144,7 @@ __device__ __forceinline__ void les_collide(R f[Q], const CollideConsts<R>& C, c
     for (int k = 0; k < 6; ++k) Sf[k] = (float)S6[k];
     const float dwall = fminf((float)z + 0.5f, (float)s.g.NZ - (float)z - 0.5f);
     closure_features(Sf, dwall, (float)s.les_nu, s.les_ustar, s.les_h, x);
-    float r = mlp_infer(Ws, Ws + kMlpParams, x);
+    float r = mlp_infer_pairs(Ws, Ws + kMlpParams, x);
     if (s.les_aplus > 0.f) {
         // van Driest damping (1 - exp(-y+/A+))^2 of the predicted nu_t
         const float e = 1.f - expf(-(dwall * s.les_ustar / (float)s.les_nu) / s.les_aplus);
@@ -162,7 +162,7 @@ __device__ __forceinline__ void les_collide(R f[Q], const CollideConsts<R>& C, c
 
 template <typename T, typename R, bool YF>
 __global__ void __launch_bounds__(kBlockX) k_les_even(PopPtrs<T> P, CollideConsts<R> C, DeviceState s) {
-    __shared__ float Ws[kMlpParams + kMlpNorm];
+    __shared__ __align__(16) float Ws[kMlpParams + kMlpNorm];
     for (int e = threadIdx.x; e < kMlpParams + kMlpNorm; e += blockDim.x) Ws[e] = s.les_w[e];
     __syncthreads();
     const Geometry& g = s.g;
@@ -196,7 +196,7 @@ __device__ __forceinline__ void les_odd_node(const PopPtrs<T>& P, const CollideC
 
 template <typename T, typename R, bool YF>
 __global__ void __launch_bounds__(kBlockX) k_les_odd(PopPtrs<T> P, CollideConsts<R> C, DeviceState s) {
-    __shared__ float Ws[kMlpParams + kMlpNorm];
+    __shared__ __align__(16) float Ws[kMlpParams + kMlpNorm];
     for (int e = threadIdx.x; e < kMlpParams + kMlpNorm; e += blockDim.x) Ws[e] = s.les_w[e];
     __syncthreads();
     const Geometry& g = s.g;
