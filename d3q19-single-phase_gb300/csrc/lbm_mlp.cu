@@ -251,7 +251,7 @@ __global__ void k_adam(float* __restrict__ P, float* __restrict__ G, float* __re
 
 __global__ void k_mlp_predict(const float* __restrict__ P, const float* __restrict__ norm,
                               const float* __restrict__ X, int64_t n, float* __restrict__ out) {
-    __shared__ float Ps[kMlpParams];
+    __shared__ __align__(16) float Ps[kMlpParams];
     __shared__ float Ns[kMlpNorm];
     for (int e = threadIdx.x; e < kMlpParams; e += blockDim.x) Ps[e] = P[e];
     for (int e = threadIdx.x; e < kMlpNorm; e += blockDim.x) Ns[e] = norm[e];
@@ -261,7 +261,7 @@ __global__ void k_mlp_predict(const float* __restrict__ P, const float* __restri
     float x[kMlpIn];
 #pragma unroll
     for (int k = 0; k < kMlpIn; ++k) x[k] = X[i * kMlpIn + k];
-    out[i] = mlp_infer(Ps, Ns, x);
+    out[i] = mlp_infer_pairs(Ps, Ns, x);
 }
 
 // deterministic initial weights: uniform(-a, a) with a = sqrt(6 / (fan_in +
