@@ -317,10 +317,11 @@ __device__ __forceinline__ RT link_q(const double d[3], int cx, int cy, int cz, 
 // with per-axis tables of the FP32 offset from the sphere centre and of the
 // node index.  The links of direction c_i in row (b, c) are then one word
 // operation: fluid(b, c) & owned(b + c_iz, c + c_ix) shifted by c_iy.  The
-// work is cut into units (direction, wall-normal plane) dealt to the warps;
-// lane j takes the row b = j of the plane, and the set bits of the lanes are
-// streamed through a 64-entry queue per warp, so that every lane of a warp
-// processes a link, mostly of one direction at neighbouring streamwise nodes.
+// rows within R + 1.5 of the centre are listed, and the work is cut into
+// units (direction, 32 listed rows) dealt to the warps; lane j takes listed
+// row j of the unit, and the set bits of the lanes are streamed through a
+// 256-entry queue per warp, so that every lane of a warp processes links --
+// two at a time, both links' loads in flight before either is finished.
 //
 // With the AA orientation the six accesses of a link touch the four nodes
 // x_f + c_i (solid), x_f, x_f - c_i, x_f - 2c_i in the planes i and opp(i):
