@@ -394,17 +394,19 @@ PopPtrs<T> pop_ptrs(const DeviceState& s) {
 
 constexpr size_t kSmemPerSM = 224 * 1024;    // dynamic shared memory planned per SM
 
-// Launch shape of the row kernels for a row of NX elements of T:
-// 512 threads (one CTA per SM), or 256 threads with two CTAs per SM when each
-// thread then handles at least two pairs per item and two stages still fit.
+// Launch shape of the row kernels for a row of NX elements of T: two CTAs
+// of 256 threads per SM whenever two stages per CTA fit, else one CTA of 512
+// threads (rows of more than ~1.4 K FP16 or ~700 FP32 nodes).  Two CTAs keep
+// twice the items in flight; with one CTA of 512 threads a row of up to 512
+// pairs leaves threads idle in every item (the 512x256x256 channel ran at 32
+// GLUPS in FP16 and 32 in FP32 that way, 54 and 42 with two CTAs).
 struct RowPlan { int threads, ctas_per_sm, nstage; size_t smem; };
 
 template <typename T>
 RowPlan plan_rows(const Geometry& g) {
     const size_t stage = (size_t)Q * g.NX * sizeof(T);
     RowPlan r;
-    const int pairs = g.NX / 2;
-    if (pairs >= 512 && 2 * (128 + 2 * stage) <= kSmemPerSM) {
+    if (2 * (128 + 2 * stage) <= kSmemPerSM) {
         r.threads = 256;
         r.ctas_per_sm = 2;
     } else {
