@@ -129,11 +129,14 @@ struct Item {
     int y, z;
     uint32_t row;                  // NX*(y + NY*z)
 };
+// item it: rows y .. y + K - 1 (y a multiple of K) at wall-normal z
+template <int K>
 __device__ __forceinline__ Item item_of(const Geometry& g, uint32_t it) {
     Item I;
-    I.y = it % g.NY;
-    I.z = it / g.NY;
-    I.row = (uint32_t)g.NX * it;
+    const uint32_t ny = (uint32_t)g.NY / K;
+    I.y = K * (int)(it % ny);
+    I.z = (int)(it / ny);
+    I.row = (uint32_t)g.NX * ((uint32_t)I.y + (uint32_t)g.NY * (uint32_t)I.z);
     return I;
 }
 __device__ __forceinline__ uint32_t row_at(const Geometry& g, int y, int z) {
@@ -156,25 +159,25 @@ __device__ __forceinline__ bool push_bb(int wall, int i) {
 // the call fails).
 template <typename T, bool ODD>
 __device__ __forceinline__ const T* src_row(const PopPtrs<T>& P, const Geometry& g, const Item& I, int wall, int i,
-                                            unsigned* bflag, unsigned site) {
+                                            int r, unsigned* bflag, unsigned site) {
     const int dz = dz_rt(i);
     const bool bb = (dz == 1 && (wall & 1)) || (dz == -1 && (wall & 2));
 #ifdef LBM_BOUNDS_CHECK
     int k = i;
-    uint32_t row = I.row;
+    uint32_t row = I.row + (uint32_t)r * (uint32_t)g.NX;
     if (ODD && !bb) {
         k = opp_rt(i);
-        row = row_at(g, I.y - dy_rt(i), I.z - dz);
+        row = row_at(g, I.y + r - dy_rt(i), I.z - dz);
     }
-    if (!LBM_IN_BOUNDS(bflag, k >= 0 && k < Q && row % (uint32_t)g.NX == 0 &&
+    if (!LBM_IN_BOUNDS(bflag, k >= 0 && k < Q && I.y + r < g.NY && row % (uint32_t)g.NX == 0 &&
                                   (size_t)row + g.NX <= (size_t)g.NXY * g.NZ, site))
         return P.p[0];
     return P.p[k] + row;
 #else
     (void)bflag;
     (void)site;
-    if (!ODD || bb) return P.p[i] + I.row;
-    return P.p[opp_rt(i)] + row_at(g, I.y - dy_rt(i), I.z - dz);
+    if (!ODD || bb) return P.p[i] + I.row + (uint32_t)r * (uint32_t)g.NX;
+    return P.p[opp_rt(i)] + row_at(g, I.y + r - dy_rt(i), I.z - dz);
 #endif
 }
 // Issued by one warp: lane i moves population i's row.  The mbarrier learns the
@@ -182,16 +185,31 @@ __device__ __forceinline__ const T* src_row(const PopPtrs<T>& P, const Geometry&
 // `issued` (a register of the issuing warp) records the loads this warp put
 // into stage s for the drain on abort: bit s flips per load (the count's
 // parity), bit 8 + s is set once one was issued.
-template <typename T, bool ODD>
+// With K = 2 the slot holds the item's two rows of population i, one bulk
+// copy when their source rows are adjacent in memory, two when the
+// periodic y wrap separates them.
+template <typename T, bool ODD, int K>
 __device__ __forceinline__ void issue_item(const PopPtrs<T>& P, const Geometry& g, uint32_t it, uint32_t stage_smem,
                                            uint32_t bar, uint32_t row_bytes, int lane, int s, unsigned& issued,
                                            unsigned* bflag) {
-    if (lane == 0) mbar_expect_tx(bar, (uint32_t)Q * row_bytes);
+    if (lane == 0) mbar_expect_tx(bar, (uint32_t)(Q * K) * row_bytes);
     __syncwarp();
     if (lane < Q) {
-        const Item I = item_of(g, it);
-        bulk_load(stage_smem + (uint32_t)lane * row_bytes,
-                  src_row<T, ODD>(P, g, I, wall_of(g, I.z), lane, bflag, 301), row_bytes, bar);
+        const Item I = item_of<K>(g, it);
+        const int wall = wall_of(g, I.z);
+        const uint32_t dst = stage_smem + (uint32_t)(lane * K) * row_bytes;
+        const T* s0 = src_row<T, ODD>(P, g, I, wall, lane, 0, bflag, 301);
+        if constexpr (K == 1) {
+            bulk_load(dst, s0, row_bytes, bar);
+        } else {
+            const T* s1 = src_row<T, ODD>(P, g, I, wall, lane, 1, bflag, 301);
+            if (s1 == s0 + g.NX) {
+                bulk_load(dst, s0, 2 * row_bytes, bar);
+            } else {
+                bulk_load(dst, s0, row_bytes, bar);
+                bulk_load(dst + row_bytes, s1, row_bytes, bar);
+            }
+        }
     }
     issued = (issued ^ (1u << s)) | (1u << (8 + s));
 }
@@ -215,7 +233,7 @@ __device__ __forceinline__ void issue_item(const PopPtrs<T>& P, const Geometry& 
 // faster than the packed one.
 template <typename T, bool ODD, int WALL, bool YF>
 __device__ __forceinline__ void pair_update(const CollideConsts<float>& C, const CollideConsts<F2>& C2,
-                                            const Geometry& g, T* stage, int x) {
+                                            const Geometry& g, T* stage, int ss, int x) {
     constexpr bool kPacked = ODD && sizeof(T) == 2;
     const int NX = g.NX;
     const int xm1 = (x == 0) ? NX - 1 : x - 1;
@@ -223,7 +241,7 @@ __device__ __forceinline__ void pair_update(const CollideConsts<float>& C, const
     F2 f[Q];
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
-        const T* r = stage + i * NX;
+        const T* r = stage + i * ss;
         const int sh = (ODD && !pull_bb(WALL, i)) ? DXg(i) : 0;   // f_i(x) = row[x - sh]
         if (sh == 0) f[i] = ld_pair(r + x);
         else if (sh == 1) f[i] = F2(ld_one(r + xm1), ld_one(r + x));
@@ -244,7 +262,7 @@ __device__ __forceinline__ void pair_update(const CollideConsts<float>& C, const
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
         const int sh = (ODD && !push_bb(WALL, i)) ? DXg(i) : 0;
-        T* d = stage + OPPf(i) * NX;
+        T* d = stage + OPPf(i) * ss;
         if (sh == 0) {
             st_pair(d + x, f[i]);
         } else if (sh == 1) {
@@ -257,25 +275,43 @@ __device__ __forceinline__ void pair_update(const CollideConsts<float>& C, const
 
 // All pairs of an item handled by this thread; the wall case is fixed for
 // the whole loop.
-template <typename T, bool ODD, int WALL, bool YF>
+// pair p of the item: row p / (NX / 2) of its K rows, nodes 2 (p mod NX/2)
+// and the next; slot i of the stage holds population i's K rows
+template <typename T, bool ODD, int WALL, bool YF, int K>
 __device__ __forceinline__ void item_pairs(const CollideConsts<float>& C, const CollideConsts<F2>& C2,
                                            const Geometry& g, T* stage, int tid, int nthreads, unsigned* bflag) {
-    const int npairs = g.NX >> 1;
-    for (int p = tid; p < npairs; p += nthreads)
-        if (LBM_IN_BOUNDS(bflag, 2 * p + 1 < g.NX && (g.NX & 1) == 0, 303))
-            pair_update<T, ODD, WALL, YF>(C, C2, g, stage, 2 * p);
+    const int half = g.NX >> 1;
+    const int npairs = K * half;
+    for (int p = tid; p < npairs; p += nthreads) {
+        const int rk = (K == 1 || p < half) ? 0 : 1;
+        const int x = 2 * (p - rk * half);
+        if (LBM_IN_BOUNDS(bflag, x + 1 < g.NX && (g.NX & 1) == 0, 303))
+            pair_update<T, ODD, WALL, YF>(C, C2, g, stage + rk * g.NX, K * g.NX, x);
+    }
 }
 
 // Issued by the last warp to finish an item: lane i copies result row i back
 // to the row that slot i was loaded from, then waits until the copy has read
 // the stage (the stage is refilled next).
-template <typename T, bool ODD>
+template <typename T, bool ODD, int K>
 __device__ __forceinline__ void store_item(const PopPtrs<T>& P, const Geometry& g, uint32_t it, uint32_t stage_smem,
                                            uint32_t row_bytes, int lane, unsigned* bflag) {
     if (lane < Q) {
-        const Item I = item_of(g, it);
-        bulk_store(const_cast<T*>(src_row<T, ODD>(P, g, I, wall_of(g, I.z), lane, bflag, 302)),
-                   stage_smem + (uint32_t)lane * row_bytes, row_bytes);
+        const Item I = item_of<K>(g, it);
+        const int wall = wall_of(g, I.z);
+        const uint32_t src = stage_smem + (uint32_t)(lane * K) * row_bytes;
+        T* d0 = const_cast<T*>(src_row<T, ODD>(P, g, I, wall, lane, 0, bflag, 302));
+        if constexpr (K == 1) {
+            bulk_store(d0, src, row_bytes);
+        } else {
+            T* d1 = const_cast<T*>(src_row<T, ODD>(P, g, I, wall, lane, 1, bflag, 302));
+            if (d1 == d0 + g.NX) {
+                bulk_store(d0, src, 2 * row_bytes);
+            } else {
+                bulk_store(d0, src, row_bytes);
+                bulk_store(d1, src + row_bytes, row_bytes);
+            }
+        }
         bulk_wait_read();
     }
     __syncwarp();
@@ -283,7 +319,7 @@ __device__ __forceinline__ void store_item(const PopPtrs<T>& P, const Geometry& 
 
 constexpr int kMaxStages = 5;
 
-template <typename T, bool ODD, bool YF, int NT>
+template <typename T, bool ODD, bool YF, int NT, int K>
 __global__ void __launch_bounds__(NT, 512 / NT)
 k_step_rows(PopPtrs<T> P, CollideConsts<float> C, CollideConsts<F2> C2, Geometry g, int nstage, int* err) {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -291,11 +327,11 @@ k_step_rows(PopPtrs<T> P, CollideConsts<float> C, CollideConsts<F2> C2, Geometry
     __shared__ unsigned int issued_par, issued_any;
     __shared__ volatile int abort_flag;
     const uint32_t row_bytes = (uint32_t)g.NX * sizeof(T);
-    const uint32_t stage_bytes = (uint32_t)Q * row_bytes;
+    const uint32_t stage_bytes = (uint32_t)(Q * K) * row_bytes;
     const uint32_t bars = smem_addr(smem);                 // nstage mbarriers (8 B each)
     const uint32_t data = bars + 128;                       // stage buffers, 16-B aligned
     T* const stage_ptr0 = reinterpret_cast<T*>(smem + 128);
-    const uint32_t total = (uint32_t)g.NY * (uint32_t)g.NZ;
+    const uint32_t total = (uint32_t)g.NY / K * (uint32_t)g.NZ;
     const uint32_t G = gridDim.x;
     const int tid = threadIdx.x;
     const int lane = tid & 31;
@@ -318,7 +354,7 @@ k_step_rows(PopPtrs<T> P, CollideConsts<float> C, CollideConsts<F2> C2, Geometry
         for (int s = 0; s < nstage; ++s) {
             const uint32_t it = blockIdx.x + (uint32_t)s * G;
             if (it < total)
-                issue_item<T, ODD>(P, g, it, data + s * stage_bytes, bars + 8 * s, row_bytes, lane, s, issued,
+                issue_item<T, ODD, K>(P, g, it, data + s * stage_bytes, bars + 8 * s, row_bytes, lane, s, issued,
                                    bflag);
         }
     }
@@ -336,13 +372,13 @@ k_step_rows(PopPtrs<T> P, CollideConsts<float> C, CollideConsts<F2> C2, Geometry
             failed = true;
             abort_flag = 1;
         }
-        const Item I = item_of(g, it);
+        const Item I = item_of<K>(g, it);
         const int wall = wall_of(g, I.z);
-        T* stage = stage_ptr0 + (size_t)s * Q * g.NX;
-        if (wall == 0)      item_pairs<T, ODD, 0, YF>(C, C2, g, stage, tid, NT, bflag);
-        else if (wall == 1) item_pairs<T, ODD, 1, YF>(C, C2, g, stage, tid, NT, bflag);
-        else if (wall == 2) item_pairs<T, ODD, 2, YF>(C, C2, g, stage, tid, NT, bflag);
-        else                item_pairs<T, ODD, 3, YF>(C, C2, g, stage, tid, NT, bflag);
+        T* stage = stage_ptr0 + (size_t)s * (Q * K) * g.NX;
+        if (wall == 0)      item_pairs<T, ODD, 0, YF, K>(C, C2, g, stage, tid, NT, bflag);
+        else if (wall == 1) item_pairs<T, ODD, 1, YF, K>(C, C2, g, stage, tid, NT, bflag);
+        else if (wall == 2) item_pairs<T, ODD, 2, YF, K>(C, C2, g, stage, tid, NT, bflag);
+        else                item_pairs<T, ODD, 3, YF, K>(C, C2, g, stage, tid, NT, bflag);
         // this warp has finished with stage s; the last warp copies the
         // results back and refills it
         fence_proxy_async();
@@ -361,10 +397,10 @@ k_step_rows(PopPtrs<T> P, CollideConsts<float> C, CollideConsts<F2> C2, Geometry
             // storing it is safe even after an abort elsewhere; only the
             // refill is withheld then
             const int ab = abort_flag;
-            store_item<T, ODD>(P, g, it, data + s * stage_bytes, row_bytes, lane, bflag);
+            store_item<T, ODD, K>(P, g, it, data + s * stage_bytes, row_bytes, lane, bflag);
             const uint32_t nit = blockIdx.x + (k + (uint32_t)nstage) * G;
             if (nit < total && !ab)
-                issue_item<T, ODD>(P, g, nit, data + s * stage_bytes, bars + 8 * s, row_bytes, lane, s, issued,
+                issue_item<T, ODD, K>(P, g, nit, data + s * stage_bytes, bars + 8 * s, row_bytes, lane, s, issued,
                                    bflag);
         }
     }
@@ -399,13 +435,18 @@ constexpr size_t kSmemPerSM = 224 * 1024;    // dynamic shared memory planned pe
 // threads (rows of more than ~1.4 K FP16 or ~700 FP32 nodes).  Two CTAs keep
 // twice the items in flight; with one CTA of 512 threads a row of up to 512
 // pairs leaves threads idle in every item (the 512x256x256 channel ran at 32
-// GLUPS in FP16 and 32 in FP32 that way, 54 and 42 with two CTAs).
-struct RowPlan { int threads, ctas_per_sm, nstage; size_t smem; };
+// GLUPS in FP16 and 32 in FP32 that way, 54 and 42 with two CTAs).  Rows
+// of up to 512 nodes with an even spanwise count are taken two per item
+// (k = 2) when two CTAs with two such stages fit: an item of one short row
+// gives a thread one pair, too little work between the item's waits.
+struct RowPlan { int threads, ctas_per_sm, nstage, k; size_t smem; };
 
 template <typename T>
 RowPlan plan_rows(const Geometry& g) {
-    const size_t stage = (size_t)Q * g.NX * sizeof(T);
+    const size_t stage1 = (size_t)Q * g.NX * sizeof(T);
     RowPlan r;
+    r.k = (g.NX <= 512 && (g.NY & 1) == 0 && 2 * (128 + 2 * 2 * stage1) <= kSmemPerSM) ? 2 : 1;
+    const size_t stage = (size_t)r.k * stage1;
     if (2 * (128 + 2 * stage) <= kSmemPerSM) {
         r.threads = 256;
         r.ctas_per_sm = 2;
@@ -434,45 +475,50 @@ CollideConsts<F2> pair_consts(const CollideConsts<float>& c) {
     return r;
 }
 
-template <typename T, bool YF, int NT>
+template <typename T, bool YF, int NT, int K>
 void launch_rows_nt(const DeviceState& s, const PopPtrs<T>& P, int parity, int* err, const RowPlan& r,
                     unsigned grid, cudaStream_t st) {
     const CollideConsts<F2> c2 = pair_consts(s.cf);
-    if (parity == 0) k_step_rows<T, false, YF, NT><<<grid, NT, r.smem, st>>>(P, s.cf, c2, s.g, r.nstage, err);
-    else             k_step_rows<T, true, YF, NT><<<grid, NT, r.smem, st>>>(P, s.cf, c2, s.g, r.nstage, err);
+    if (parity == 0) k_step_rows<T, false, YF, NT, K><<<grid, NT, r.smem, st>>>(P, s.cf, c2, s.g, r.nstage, err);
+    else             k_step_rows<T, true, YF, NT, K><<<grid, NT, r.smem, st>>>(P, s.cf, c2, s.g, r.nstage, err);
 }
 
 template <typename T>
 cudaError_t rows_impl(const DeviceState& s, int parity, int* err, cudaStream_t st) {
     const RowPlan r = plan_rows<T>(s.g);
     const PopPtrs<T> P = pop_ptrs<T>(s);
-    const uint32_t total = (uint32_t)s.g.NY * (uint32_t)s.g.NZ;
+    const uint32_t total = (uint32_t)s.g.NY / (uint32_t)r.k * (uint32_t)s.g.NZ;
     const unsigned grid = (unsigned)std::min<uint32_t>(total, (uint32_t)(s.sm_count * r.ctas_per_sm));
     const bool yf = s.cf.Fx == 0.0f && s.cf.Fz == 0.0f;
-    if (r.threads == 256) {
-        if (yf) launch_rows_nt<T, true, 256>(s, P, parity, err, r, grid, st);
-        else    launch_rows_nt<T, false, 256>(s, P, parity, err, r, grid, st);
+    if (r.threads == 256 && r.k == 2) {
+        if (yf) launch_rows_nt<T, true, 256, 2>(s, P, parity, err, r, grid, st);
+        else    launch_rows_nt<T, false, 256, 2>(s, P, parity, err, r, grid, st);
+    } else if (r.threads == 256) {
+        if (yf) launch_rows_nt<T, true, 256, 1>(s, P, parity, err, r, grid, st);
+        else    launch_rows_nt<T, false, 256, 1>(s, P, parity, err, r, grid, st);
     } else {
-        if (yf) launch_rows_nt<T, true, 512>(s, P, parity, err, r, grid, st);
-        else    launch_rows_nt<T, false, 512>(s, P, parity, err, r, grid, st);
+        if (yf) launch_rows_nt<T, true, 512, 1>(s, P, parity, err, r, grid, st);
+        else    launch_rows_nt<T, false, 512, 1>(s, P, parity, err, r, grid, st);
     }
     return cudaGetLastError();
 }
 
-template <typename T, bool YF, int NT>
+template <typename T, bool YF, int NT, int K>
 cudaError_t set_attr_nt() {
     const int b = (int)(kSmemPerSM / (512 / NT));
-    cudaError_t e = cudaFuncSetAttribute(k_step_rows<T, false, YF, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_step_rows<T, true, YF, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaError_t e = cudaFuncSetAttribute(k_step_rows<T, false, YF, NT, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_step_rows<T, true, YF, NT, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
     return e;
 }
 
 template <typename T>
 cudaError_t set_smem_attr() {
-    cudaError_t e = set_attr_nt<T, false, 512>();
-    if (e == cudaSuccess) e = set_attr_nt<T, true, 512>();
-    if (e == cudaSuccess) e = set_attr_nt<T, false, 256>();
-    if (e == cudaSuccess) e = set_attr_nt<T, true, 256>();
+    cudaError_t e = set_attr_nt<T, false, 512, 1>();
+    if (e == cudaSuccess) e = set_attr_nt<T, true, 512, 1>();
+    if (e == cudaSuccess) e = set_attr_nt<T, false, 256, 1>();
+    if (e == cudaSuccess) e = set_attr_nt<T, true, 256, 1>();
+    if (e == cudaSuccess) e = set_attr_nt<T, false, 256, 2>();
+    if (e == cudaSuccess) e = set_attr_nt<T, true, 256, 2>();
     return e;
 }
 

@@ -53,7 +53,8 @@ def run_both(pkg, debug_lib, run, f0, steps, pos=None, vel=None, radius=4.0):
 
 
 @pytest.mark.parametrize("prec", ["fp32", "fp16"])
-@pytest.mark.parametrize("shape", [(5, 16, 3), (3, 24, 1), (6, 32, 9), (4, 1024, 3), (3, 1536, 2)])
+@pytest.mark.parametrize("shape", [(5, 16, 3), (3, 24, 1), (6, 32, 9), (4, 1024, 3), (3, 1536, 2), (4, 512, 4),
+                                   (5, 16, 6)])
 def test_row_kernels_checked(pkg, orc, debug_lib, prec, shape):
     nx, ny, nz = shape
     run = pkg.RunParams(nx=nx, ny=ny, nz=nz, visc=0.0012, force_y=2e-5, mrt_type=1, precision=pkg.PRECISIONS[prec])

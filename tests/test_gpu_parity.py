@@ -322,16 +322,18 @@ def test_avedensity_removes_mean(pkg, orc):
 
 @pytest.mark.parametrize("prec", ["fp32", "fp16"])
 @pytest.mark.parametrize("shape", [(5, 16, 3), (8, 64, 7), (3, 24, 1), (6, 32, 9), (4, 512, 3), (4, 1024, 3),
-                                   (3, 1536, 2), (2, 3072, 2)])
+                                   (3, 1536, 2), (2, 3072, 2), (5, 16, 6), (4, 512, 4), (3, 256, 2)])
 def test_row_pipelined_kernels_match_simple_kernels(pkg, orc, prec, shape):
     """The bulk-copy row kernels (FP32/FP16 storage, rows of 16-byte multiples)
     against the one-node-per-thread kernels: same arithmetic per node, so the
     populations agree to rounding of the storage type.  The streamwise rows
-    cover the launch shapes: two CTAs of 256 threads with idle threads in
-    each item (short rows) and with two pairs per thread (FP16 rows of
-    1024), one CTA of 512 threads with two pairs each (FP16 rows of 1536),
-    and rows too long for two stages, which run the one-node-per-thread
-    kernels under either flag (FP16 3072, FP32 1536)."""
+    cover the launch shapes: two CTAs of 256 threads with one row per item
+    (short rows with an odd spanwise count, idle threads in each item; FP16
+    rows of 1024, two pairs per thread) and with two rows per item (rows of
+    up to 512 with an even spanwise count, including the pair of rows split
+    by the periodic wrap), one CTA of 512 threads (FP16 rows of 1536, FP32
+    of 1024), and rows too long for two stages, which run the
+    one-node-per-thread kernels under either flag (FP16 3072, FP32 1536)."""
     f = random_state(orc, shape, 21)
     out = {}
     for flags in (0, pkg.FLAG_SIMPLE_STEP):
